@@ -1,0 +1,336 @@
+#!/usr/bin/env python
+"""bench.py -- seconds to a converged temperature field, DOM-FVM phonon BTE on one GB300.
+
+Workload (default): the 2D configuration of the reference's measurement set --
+a 1e-7 m square, 2 x 100^2 jittered-Delaunay triangles (20,000 cells), DM=2 with
+8 x 8 angles (32 directions), 40 Debye-like bands, left/right isothermal
+301/299 K, top/bottom diffuse -- written by staticbtesolver_gb300.synth
+(seeded synthetic data; the reference ships no such mesh).  One step is one
+complete solve: the source iteration from e = 0 to margin <= 1e-5 with all
+1,280 (band, direction) systems solved on the GPU every outer iteration.
+
+  value  device seconds per solve with inputs resident in HBM (CUDA events on
+         the solve stream, summed over the outer loop), max over ranks
+  e2e    host wall seconds per solve through the C ABI with host buffers:
+         bte_set_geometry/quadrature/bands/bcs (H2D), bte_solve,
+         bte_get_temperature + bte_get_heat_flux (D2H)
+  roofline  the dominant kernel of a profiled solve: algorithmic bytes per
+         launch / CUDA-event time per launch, against MEASURED_PEAKS.json
+  cpu_baseline  the oracle (CPU restatement of the reference's PETSc path:
+         GMRES(30)+ILU(0) per system, all host threads), timed on a bounded
+         sample of 2 outer iterations and scaled by the outer-iteration count
+
+--impl reference times the reference's CPU path the same way (the oracle
+port; the reference's own build needs its sources, which are not on the GPU
+host) and prints its line with "impl": "reference".
+
+--gpus N (under torchrun) runs N independent replicas: the solve does not
+shard across GPUs in this design (one GPU per solve).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "s to converged T (<=1e-5 rel L2 vs FP64): chosen form vs plain FP64 GPU; HBM GB/s"
+UNIT = "s"
+# Outer iterations of the square20k solve to margin <= 1e-5 (same for the
+# oracle and the plain GPU form, see tests/test_gpu_full.py); the CPU legs run
+# a 2-iteration sample and scale by it.
+OUTER_ITERS = {"square20k": None}
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="square20k")
+    ap.add_argument("--form", default="plain", choices=["plain", "mixed"])
+    ap.add_argument("--e2e-steps", type=int, default=1)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--max-iter", type=int, default=10000)
+    return ap.parse_args()
+
+
+def dist_setup(n):
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    local = int(os.environ.get("LOCAL_RANK", 0))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("gloo")
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic(kernel):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "bicgstab_square20k.md")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        m = re.match(r"\|\s*" + re.escape(kernel) + r"\s*\|.*\|\s*traffic_bytes_per_launch=([0-9.eE+]+)\s*\|", line)
+        if m:
+            return float(m.group(1))
+    return None
+
+
+def make_workload(name, tmp):
+    from staticbtesolver_gb300 import synth
+
+    return synth.make_problem(name, tmp)
+
+
+def cpu_sample(p, threads):
+    """Oracle (reference CPU algorithm) on 2 outer iterations of the full workload."""
+    from oracle import oracle as O
+
+    O.build()
+    o = O.Oracle(p.geo, p.bc_file, p.band_file, p.DM, p.num_theta, p.num_phi, p.T_ref, p.L_x, p.L_y, p.L_z)
+    t0 = time.perf_counter()
+    r = o.run(max_iter=2, outer_tol=0.0, threads=threads)
+    dt = time.perf_counter() - t0
+    return dt / 2.0, r.inner
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    with tempfile.TemporaryDirectory() as tmp:
+        p = make_workload(args.workload, tmp)
+        threads = os.cpu_count() or 1
+        n_outer = OUTER_ITERS.get(args.workload)
+        for _ in range(args.warmup):
+            cpu_sample(p, threads)
+        per_iter = []
+        for _ in range(args.steps):
+            t, inner = cpu_sample(p, threads)
+            per_iter.append(t)
+        t_iter = statistics.mean(per_iter)
+        value = t_iter * n_outer if n_outer else None
+        line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_iter * 1e3 * 2,
+                "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic", "config": {"workload": args.workload, "form": "reference CPU path (PETSc defaults: GMRES(30)+ILU(0)), oracle port",
+                                                "outer_iterations": n_outer, "extrapolated": True},
+                "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                                 "sample": f"2 outer iterations x {inner['solves'] // 2} systems per step, "
+                                           f"scaled by {n_outer} outer iterations"},
+                "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+
+
+def run_ours(args, rank, world, local):
+    import numpy as np
+    import torch
+
+    import staticbtesolver_gb300 as S
+
+    S.build()
+    form = S.FORM_PLAIN if args.form == "plain" else S.FORM_MIXED
+    with tempfile.TemporaryDirectory() as tmp:
+        t0 = time.perf_counter()
+        p = make_workload(args.workload, tmp)
+        t_gen = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        prob = S.Problem(p.geo, p.bc_file, p.band_file, p.DM, p.num_theta, p.num_phi, p.T_ref, p.L_x, p.L_y, p.L_z)
+        t_prep = time.perf_counter() - t0
+        arrays = prob.arrays()
+        torch.cuda.set_device(local)
+        ctx = S.Context(local).load(prob)
+        solve_kw = dict(max_iter=args.max_iter, tol=1e-5, form=form, inner_tol=1e-9, inner_maxit=1000)
+        for _ in range(args.warmup):
+            ctx.solve(**solve_kw)
+        barrier(world)
+        torch.cuda.synchronize()
+        clocks = ClockSampler(local)
+        clocks.start()
+        dev_ms, wall, reps = [], [], []
+        for _ in range(args.steps):
+            w0 = time.perf_counter()
+            st, rep = ctx.solve(**solve_kw)
+            wall.append(time.perf_counter() - w0)
+            dev_ms.append(rep.ms_total)
+            reps.append(rep.as_dict())
+        torch.cuda.synchronize()
+        clk = clocks.stop()
+        barrier(world)
+        t_step = max_over_ranks(statistics.mean(dev_ms) / 1e3, world)
+        T = ctx.temperature()
+        q, _ = ctx.heat_flux()
+        last = reps[-1]
+        launches = sum(r["kernel_launches"] for r in reps)
+
+        # e2e through the C ABI with host buffers (a second context, as a caller would hold)
+        e2e_t = []
+        h2d = sum(np.asarray(arrays[k]).nbytes for k in ("nbr", "area", "normal", "volume", "s", "S", "omega"))
+        h2d += sum(np.asarray(v).nbytes for v in arrays["bands"].values()) + sum(
+            np.asarray(v).nbytes for v in arrays["bcs"].values())
+        ctx2 = S.Context(local)
+        for _ in range(max(1, args.e2e_steps)):
+            w0 = time.perf_counter()
+            ctx2.set_arrays(arrays)
+            st2, rep2 = ctx2.solve(**solve_kw)
+            T2 = ctx2.temperature()
+            q2, _ = ctx2.heat_flux()
+            e2e_t.append(time.perf_counter() - w0)
+        d2h = T2.nbytes + q2.nbytes
+        e2e = max_over_ranks(statistics.mean(e2e_t), world)
+        ctx2.close()
+
+        # profiled solve (outside the timed region) for the per-kernel roofline
+        ctx.solve(profile=True, **solve_kw)
+        stats = ctx.kernel_stats()
+        dom_name, dom = max(((k, v) for k, v in stats.items() if v["launches"]), key=lambda kv: kv[1]["ms"])
+        tot_ms = sum(v["ms"] for v in stats.values())
+        peak, peak_kind = measured_peaks()
+        achieved = dom["bytes"] / (dom["ms"] / 1e3) / 1e9
+        traffic = ncu_traffic(dom_name)
+        per_kernel = {k: {"launches": v["launches"], "ms": round(v["ms"], 3),
+                          "GB/s": round(v["bytes"] / (v["ms"] / 1e3) / 1e9, 1) if v["ms"] > 0 else None,
+                          "share": round(v["ms"] / tot_ms, 4) if tot_ms else None}
+                      for k, v in stats.items() if v["launches"]}
+        ctx.close()
+
+        if rank != 0:
+            return
+        cpu = None
+        n_outer = last["n_iter"]
+        if not args.no_cpu_baseline and world == 1:
+            threads = os.cpu_count() or 1
+            t_iter, inner = cpu_sample(p, threads)
+            cpu = {"value": t_iter * n_outer, "unit": UNIT, "cores": threads, "kind": "port",
+                   "sample": f"oracle (GMRES(30)+ILU(0) per system, as the reference CPU path) on 2 outer "
+                             f"iterations x {inner['solves'] // 2} systems, {t_iter:.2f} s per outer iteration, "
+                             f"scaled by the {n_outer} outer iterations of this solve"}
+        line = {
+            "metric": METRIC, "value": t_step, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": args.workload, "form": args.form, "cells": prob.n_cell, "directions": prob.n_dir,
+                       "bands": prob.n_band, "systems": prob.n_dir * prob.n_band, "outer_iterations": n_outer,
+                       "inner_iterations": last["inner_iterations"], "final_margin": last["final_margin"],
+                       "ms_rhs": round(last["ms_rhs"], 2), "ms_inner": round(last["ms_inner"], 2),
+                       "ms_reduce": round(last["ms_reduce"], 2), "wall_s_per_step": statistics.mean(wall),
+                       "preprocess_s": t_prep, "generate_s": t_gen, "l2": "working set > L2 (2 GB of vectors)",
+                       "replicas": world, "q_left": float(q[0]), "q_right": float(q[2]),
+                       "T_min": float(T.min()), "T_max": float(T.max()), "kernels": per_kernel},
+            "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": round(achieved, 1), "peak": peak,
+                         "peak_source": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                         "traffic": traffic,
+                         "algorithmic_bytes_per_launch": dom["bytes"] / dom["launches"],
+                         "ms_per_launch": dom["ms"] / dom["launches"]},
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+            "gpu_launches": launches,
+            "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse_args()
+    rank, world, local = dist_setup(args.gpus)
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world, local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

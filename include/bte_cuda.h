@@ -1,0 +1,159 @@
+/*
+ * bte_cuda.h -- C ABI of the GB300 (sm_103a) phonon BTE solve.
+ *
+ * This is the drop-in boundary for the hot path of yuchengs/StaticBTESolver:
+ * the steady-state discrete-ordinates finite-volume source iteration
+ * (StaticBTESolver::_iteration, src/StaticBTESolver.cpp:690-808) with its upwind
+ * assembly (_get_Ke :122-160, _get_Re :162-269), its per-(band, direction)
+ * inner solve (CPU: _solve_matrix :271-308; GPU: BICGSTAB in
+ * src/bicgstab.hpp:33-321), the reductions that close each outer iteration
+ * (_get_cell_temperature :96-104, _recover_temperature :106-120,
+ * _get_margin :311-321) and the heat flux (_get_heat_flux :323-370).
+ *
+ * Plain pointers and sizes only.  Every call returns a bte_status; nothing
+ * exits the process.  A context owns one CUDA stream and all device memory it
+ * allocates; it is not thread-safe (one host thread per context at a time).
+ * Host input arrays are copied during the call and may be freed afterwards.
+ */
+#ifndef BTE_CUDA_H
+#define BTE_CUDA_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum bte_status {
+    BTE_OK = 0,
+    BTE_ERR_INVALID_ARGUMENT = 1, /* bad size, index or pointer */
+    BTE_ERR_STATE = 2,            /* call out of order (e.g. solve before set_geometry) */
+    BTE_ERR_CUDA = 3,             /* a CUDA runtime call failed; see bte_last_error */
+    BTE_ERR_OUT_OF_MEMORY = 4,
+    BTE_ERR_UNSUPPORTED_BC = 5,   /* boundary type the reference aborts on (:218, :244, :254) */
+    BTE_ERR_NOT_CONVERGED = 6,    /* outer iteration hit max_iter (results are still valid) */
+    BTE_ERR_NUMERICAL = 7,        /* NaN/Inf in the outer iterate */
+    BTE_ERR_NO_DEVICE = 8
+} bte_status;
+
+/* How each (band, direction) system is solved inside one outer iteration. */
+typedef enum bte_form {
+    /* FP64 right-Jacobi BiCGSTAB, x0 = 0, ||r||/||r0|| < inner_tol, at most
+     * inner_maxit iterations, breakdown restart with r_hat = 6.8 b + 0.6:
+     * the reference GPU inner solve (src/bicgstab.hpp:138-300), all systems of
+     * an outer iteration batched into one launch per BiCGSTAB phase. */
+    BTE_FORM_PLAIN = 0,
+    /* FP32 BiCGSTAB inside FP64 iterative refinement: the FP64 residual
+     * b - A x is recomputed after every FP32 cycle and the solve stops when
+     * ||b - A x|| <= inner_tol * ||b||, the reference's criterion for x0 = 0.
+     * The inner iterate starts from the previous outer iterate. */
+    BTE_FORM_MIXED = 1
+} bte_form;
+
+typedef struct bte_ctx bte_ctx;
+
+/* Per-outer-iteration callback: iteration index, margin, milliseconds spent. */
+typedef void (*bte_iteration_cb)(void* user, int iteration, double margin, double ms);
+
+typedef struct bte_options {
+    int max_iter;         /* outer iterations (StaticBTESolver::solve(max_iter)) */
+    double tol;           /* stop when margin <= tol (reference: 1e-5, :798) */
+    int form;             /* bte_form */
+    double inner_tol;     /* 1e-9 in the reference (:699) */
+    int inner_maxit;      /* 1000 in the reference (:699) */
+    int batch_systems;    /* systems per batch; 0 = as many as fit in device memory */
+    bte_iteration_cb on_iteration; /* may be NULL */
+    void* user;
+    int profile;          /* nonzero: time every inner-solve kernel with CUDA events
+                             (bte_get_kernel_stats); adds event records between launches */
+} bte_options;
+
+/* Per-kernel totals of the last profiled bte_solve. */
+typedef struct bte_kernel_stat {
+    char name[32];
+    long long launches;
+    double ms;          /* summed CUDA-event durations on the solve stream */
+    double bytes;       /* algorithmic HBM bytes of the work done by those launches */
+} bte_kernel_stat;
+
+typedef struct bte_report {
+    int n_iter;                /* outer iterations run */
+    int converged;             /* margin <= tol reached */
+    double final_margin;
+    long long inner_solves;    /* (band, direction) systems solved */
+    long long inner_iterations;/* BiCGSTAB iterations summed over systems */
+    long long inner_unconverged;
+    long long refinements;     /* FP64 refinement cycles (mixed form) */
+    double ms_total;           /* device time of the outer loop */
+    double ms_rhs;             /* right-hand-side assembly */
+    double ms_inner;           /* inner solves */
+    double ms_reduce;          /* temperature / margin reductions */
+    long long kernel_launches; /* kernels this library launched during the solve */
+} bte_report;
+
+/* Fill opts with the reference's defaults (max_iter 10000 as BTEcmd's -I default,
+ * tol 1e-5, FP64 plain form, inner_tol 1e-9, inner_maxit 1000). */
+void bte_default_options(bte_options* opts);
+const char* bte_status_string(bte_status s);
+/* Last error message recorded on ctx (or the thread's last create error if ctx is NULL). */
+const char* bte_last_error(const bte_ctx* ctx);
+
+/* Replaces the device binding in StaticBTESolver::StaticBTESolver
+ * (src/StaticBTESolver.cpp:35-38): device = rank % device_count there. */
+bte_status bte_create(bte_ctx** ctx, int device);
+bte_status bte_destroy(bte_ctx* ctx);
+
+/* Mesh geometry after StaticBTESolver::_preprocess (src/StaticBTESolver.cpp:494-688).
+ * dim 1/2/3; n_face 2/3/4.  nbr[c*n_face+f] >= 0 is the neighbouring cell,
+ * < 0 encodes boundary entity e as -e-1 (the reference's convention).
+ * area[c*n_face+f]; normal[(c*n_face+f)*3 + xyz] (outward unit normal);
+ * volume[c]. */
+bte_status bte_set_geometry(bte_ctx* ctx, int dim, int n_cell, int n_face, const int* nbr,
+                            const double* area, const double* normal, const double* volume);
+
+/* Angular quadrature (src/StaticBTESolver.cpp:48-94 and :373-492).
+ * s[d*3+xyz] unit directions, S[d*3+xyz] angle-integrated directions (unused in
+ * 1D), omega[d] control angles.  DM, num_theta, num_phi as given to setParam;
+ * solid_angle is 4 pi (2 pi for DM=2 on a 1D mesh); T_ref after setParam's
+ * 1D override (0 for 1D meshes). */
+bte_status bte_set_quadrature(bte_ctx* ctx, int n_dir, const double* s, const double* S,
+                              const double* omega, int DM, int num_theta, int num_phi,
+                              double solid_angle, double T_ref);
+
+/* Bands (src/BTEBand.cpp:8-26): group velocity, relaxation time, Ctot, Lr. */
+bte_status bte_set_bands(bte_ctx* ctx, int n_band, const double* vg, const double* tau,
+                         const double* C, const double* Lr);
+
+/* Boundary conditions (src/BTEBoundaryCondition.cpp:7-23): index = -entity-1,
+ * type 1 isothermal, 2 diffuse, 31/32/33 specular; T in kelvin. */
+bte_status bte_set_bcs(bte_ctx* ctx, int n_bc, const int* index, const int* type, const double* T);
+
+/* Run the source iteration (src/StaticBTESolver.cpp:690-808) from e = 0.
+ * report may be NULL.  Returns BTE_ERR_NOT_CONVERGED when max_iter ran out
+ * (the fields are still those of the last iteration, as in the reference). */
+bte_status bte_solve(bte_ctx* ctx, const bte_options* opts, bte_report* report);
+
+/* Results of the last bte_solve, copied to host arrays. */
+bte_status bte_get_temperature(bte_ctx* ctx, double* T /* [n_cell] */);
+bte_status bte_get_band_temperature(bte_ctx* ctx, double* Tb /* [n_cell*n_band] */);
+/* q_bc[n_bc] (the printed "heat flux of Boundary Condition #k"); q_bc_band
+ * [n_bc*n_band] may be NULL. */
+bte_status bte_get_heat_flux(bte_ctx* ctx, double* q_bc, double* q_bc_band);
+/* Energy density e[b][d][c] (the reference's ee_curr), n_band*n_dir*n_cell values. */
+bte_status bte_get_energy(bte_ctx* ctx, double* e);
+/* Margins of the outer iterations run, up to cap values; returns how many via *n. */
+bte_status bte_get_margins(bte_ctx* ctx, double* margins, int cap, int* n);
+
+/* Kernel statistics of the last solve run with opts->profile set; *n = entries. */
+bte_status bte_get_kernel_stats(bte_ctx* ctx, bte_kernel_stat* stats, int cap, int* n);
+
+/* The reference's inner-solve operator boundary (src/bicgstab.hpp:65,96,138):
+ * BICGSTAB(n, maxit, tol); init(rowptr, colind, val, nnz, b); solve(x) --
+ * right-Jacobi BiCGSTAB on one CSR system held in host memory.
+ * iterations and converged may be NULL. */
+bte_status bte_bicgstab_csr(int n, const int* rowptr, const int* colind, const double* val,
+                            int nnz, const double* b, double* x, int maxit, double tol,
+                            int* iterations, int* converged);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BTE_CUDA_H */

@@ -1,0 +1,897 @@
+// bte_api.cu -- C ABI (include/bte_cuda.h) of the GB300 phonon BTE solve.
+//
+// One context = one device, one stream, resident inputs and state.  bte_solve
+// runs the reference's source iteration (src/StaticBTESolver.cpp:690-808) with
+// every (band, direction) system of a batch solved together by the batched
+// BiCGSTAB kernels in bte_kernels.cuh, then the fused reductions and the heat
+// flux of bte_transport.cuh.  Nothing here synchronises with the host inside a
+// BiCGSTAB group; the host reads one counter per group and one margin per
+// outer iteration.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/bte_cuda.h"
+#include "bte_kernels.cuh"
+#include "bte_transport.cuh"
+
+namespace {
+
+thread_local std::string g_create_error;
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    cudaError_t alloc(size_t n) {
+        if (n <= bytes && p) return cudaSuccess;
+        release();
+        if (n == 0) n = 16;
+        cudaError_t e = cudaMalloc(&p, n);
+        if (e == cudaSuccess) bytes = n;
+        else p = nullptr;
+        return e;
+    }
+    template <typename T>
+    T* as() const { return static_cast<T*>(p); }
+};
+
+constexpr int kGroup = 8;  // BiCGSTAB iterations launched between host checks
+
+enum KernelKind { KK_P, KK_SPMV1, KK_S, KK_SPMV2, KK_X, KK_INIT, KK_RHS, KK_REDUCE, KK_DIFFUSE, KK_HEAT, kNumKinds };
+const char* kKindNames[kNumKinds] = {"bicg_p_update", "bicg_spmv1",   "bicg_s_update", "bicg_spmv2", "bicg_x_update",
+                                     "bicg_init",     "rhs_assembly", "reduce_margin", "diffuse_wall", "heat_flux"};
+
+}  // namespace
+
+struct bte_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    // inputs (host copies)
+    int dim = 0, n = 0, F = 0;
+    std::vector<int> nbr;
+    std::vector<double> area, normal, volume;
+    int n_dir = 0, DM = 0, num_theta = 0, num_phi = 0;
+    std::vector<double> s, S, omega;
+    double solid_angle = 0, T_ref = 0;
+    int n_band = 0;
+    std::vector<double> vg, tau, Cb, Lr;
+    int n_bc = 0;
+    std::vector<int> bc_index, bc_type;
+    std::vector<double> bc_T;
+    bool has_geom = false, has_quad = false, has_bands = false, has_bcs = false;
+    bool dirty = true;
+    // derived sizes
+    size_t Np = 0;
+    int nchunk = 0;
+    int nbf = 0, ndiff = 0;
+    std::vector<int> h_bf_bc;
+    // device state
+    DevBuf d_normal, d_area, d_nbr, d_volume, d_s, d_S, d_omega;
+    DevBuf d_dg, d_vo, d_fc, d_nb, d_kb, d_Cb, d_Lr, d_vg;
+    DevBuf d_bptr, d_bf_cell, d_bf_kind, d_bf_bc, d_bf_diff, d_cin, d_eiso, d_mirror, d_ediff;
+    DevBuf d_dlist, d_wdiff, d_wden, d_hw, d_bf_area;
+    DevBuf d_e0, d_e1, d_ebar, d_Tb, d_T, d_mpart, d_margin, d_hpart, d_qband, d_q;
+    // batch work
+    int nbb = 0;
+    DevBuf w_r, w_rw, w_p, w_ph, w_q, w_z, w_t, w_b, w_invD;
+    DevBuf s_done, s_iters, s_flagA, s_flagB, s_rho, s_alpha, s_omega, s_nrmr, s_nrm0, s_part, s_active;
+    int active_cap = 0;
+    double* h_pinned = nullptr;  // [4]
+    int* h_pinned_i = nullptr;   // [4]
+    std::vector<int> h_done, h_iters;
+    // profiling (opts->profile): events around each launch, resolved after a sync
+    bool profile = false;
+    std::vector<cudaEvent_t> ev_pool;
+    struct Pending { int kind, iter; size_t ev; double bytes_fixed, bytes_per_active; };
+    std::vector<Pending> pending;
+    size_t ev_next = 0;
+    bte_kernel_stat stats[kNumKinds];
+    std::vector<int> h_active;
+    // results
+    double* e_curr = nullptr;
+    double* e_prev = nullptr;
+    bool solved = false;
+    std::vector<double> margins;
+    long long launches = 0;
+};
+
+#define BTE_CUDA(call)                                                                    \
+    do {                                                                                  \
+        cudaError_t _e = (call);                                                          \
+        if (_e != cudaSuccess) {                                                          \
+            ctx->err = std::string(#call) + ": " + cudaGetErrorString(_e);                \
+            return _e == cudaErrorMemoryAllocation ? BTE_ERR_OUT_OF_MEMORY : BTE_ERR_CUDA; \
+        }                                                                                 \
+    } while (0)
+
+#define BTE_LAUNCHED()                                                                    \
+    do {                                                                                  \
+        ++ctx->launches;                                                                  \
+        cudaError_t _e = cudaGetLastError();                                              \
+        if (_e != cudaSuccess) {                                                          \
+            ctx->err = std::string("kernel launch: ") + cudaGetErrorString(_e);           \
+            return BTE_ERR_CUDA;                                                          \
+        }                                                                                 \
+    } while (0)
+
+static bte_status fail(bte_ctx* ctx, bte_status st, const std::string& msg) {
+    if (ctx) ctx->err = msg;
+    return st;
+}
+
+// Profiling: record an event pair around a launch; bytes = fixed + per_active * active[iter].
+static cudaError_t prof_begin(bte_ctx* ctx, size_t* slot) {
+    if (!ctx->profile) return cudaSuccess;
+    if (ctx->ev_next + 2 > ctx->ev_pool.size()) {
+        size_t add = std::max<size_t>(1024, ctx->ev_pool.size());
+        for (size_t k = 0; k < add; ++k) {
+            cudaEvent_t e;
+            cudaError_t err = cudaEventCreate(&e);
+            if (err != cudaSuccess) return err;
+            ctx->ev_pool.push_back(e);
+        }
+    }
+    *slot = ctx->ev_next;
+    ctx->ev_next += 2;
+    return cudaEventRecord(ctx->ev_pool[*slot], ctx->stream);
+}
+static cudaError_t prof_end(bte_ctx* ctx, size_t slot, int kind, int iter, double bytes_fixed,
+                            double bytes_per_active) {
+    if (!ctx->profile) return cudaSuccess;
+    ctx->pending.push_back({kind, iter, slot, bytes_fixed, bytes_per_active});
+    return cudaEventRecord(ctx->ev_pool[slot + 1], ctx->stream);
+}
+// After a stream sync: fold pending launches into the per-kind totals.
+static void prof_resolve(bte_ctx* ctx, const int* active, int n_active) {
+    for (const auto& p : ctx->pending) {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, ctx->ev_pool[p.ev], ctx->ev_pool[p.ev + 1]);
+        bte_kernel_stat& st = ctx->stats[p.kind];
+        st.launches += 1;
+        st.ms += ms;
+        const double act = (active && p.iter >= 0 && p.iter < n_active) ? active[p.iter] : 0.0;
+        st.bytes += p.bytes_fixed + p.bytes_per_active * act;
+    }
+    ctx->pending.clear();
+    ctx->ev_next = 0;
+}
+
+template <typename T>
+static cudaError_t upload(DevBuf& buf, const std::vector<T>& h, cudaStream_t st) {
+    cudaError_t e = buf.alloc(h.size() * sizeof(T));
+    if (e != cudaSuccess) return e;
+    if (h.empty()) return cudaSuccess;
+    return cudaMemcpyAsync(buf.p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, st);
+}
+
+extern "C" {
+
+void bte_default_options(bte_options* o) {
+    if (!o) return;
+    std::memset(o, 0, sizeof(*o));
+    o->max_iter = 10000;
+    o->tol = 1e-5;
+    o->form = BTE_FORM_PLAIN;
+    o->inner_tol = 1e-9;
+    o->inner_maxit = 1000;
+    o->batch_systems = 0;
+}
+
+const char* bte_status_string(bte_status s) {
+    switch (s) {
+        case BTE_OK: return "ok";
+        case BTE_ERR_INVALID_ARGUMENT: return "invalid argument";
+        case BTE_ERR_STATE: return "call out of order";
+        case BTE_ERR_CUDA: return "CUDA error";
+        case BTE_ERR_OUT_OF_MEMORY: return "out of device memory";
+        case BTE_ERR_UNSUPPORTED_BC: return "unsupported boundary condition";
+        case BTE_ERR_NOT_CONVERGED: return "outer iteration did not converge within max_iter";
+        case BTE_ERR_NUMERICAL: return "non-finite value in the outer iterate";
+        case BTE_ERR_NO_DEVICE: return "no CUDA device";
+    }
+    return "unknown status";
+}
+
+const char* bte_last_error(const bte_ctx* ctx) { return ctx ? ctx->err.c_str() : g_create_error.c_str(); }
+
+bte_status bte_create(bte_ctx** out, int device) {
+    if (!out) return BTE_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess || count == 0) {
+        g_create_error = std::string("no CUDA device: ") + cudaGetErrorString(e);
+        return BTE_ERR_NO_DEVICE;
+    }
+    if (device < 0) device = 0;
+    device %= count;
+    e = cudaSetDevice(device);
+    if (e != cudaSuccess) {
+        g_create_error = cudaGetErrorString(e);
+        return BTE_ERR_CUDA;
+    }
+    auto* ctx = new bte_ctx;
+    ctx->device = device;
+    e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMallocHost((void**)&ctx->h_pinned, 4 * sizeof(double));
+    if (e == cudaSuccess) e = cudaMallocHost((void**)&ctx->h_pinned_i, 4 * sizeof(int));
+    if (e != cudaSuccess) {
+        g_create_error = cudaGetErrorString(e);
+        delete ctx;
+        return BTE_ERR_CUDA;
+    }
+    *out = ctx;
+    return BTE_OK;
+}
+
+bte_status bte_destroy(bte_ctx* ctx) {
+    if (!ctx) return BTE_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    for (cudaEvent_t e : ctx->ev_pool) cudaEventDestroy(e);
+    if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);
+    if (ctx->h_pinned_i) cudaFreeHost(ctx->h_pinned_i);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return BTE_OK;
+}
+
+bte_status bte_set_geometry(bte_ctx* ctx, int dim, int n_cell, int n_face, const int* nbr,
+                            const double* area, const double* normal, const double* volume) {
+    if (!ctx) return BTE_ERR_INVALID_ARGUMENT;
+    if (dim < 1 || dim > 3 || n_face != dim + 1 || n_cell <= 0 || !nbr || !area || !normal || !volume)
+        return fail(ctx, BTE_ERR_INVALID_ARGUMENT, "bte_set_geometry: bad dim/n_cell/n_face or null array");
+    const size_t nf = (size_t)n_cell * n_face;
+    for (size_t i = 0; i < nf; ++i) {
+        if (nbr[i] >= n_cell)
+            return fail(ctx, BTE_ERR_INVALID_ARGUMENT, "bte_set_geometry: neighbour index out of range");
+        if (!std::isfinite(area[i]) || !std::isfinite(normal[3 * i]) || !std::isfinite(normal[3 * i + 1]) ||
+            !std::isfinite(normal[3 * i + 2]))
+            return fail(ctx, BTE_ERR_INVALID_ARGUMENT, "bte_set_geometry: non-finite area or normal");
+    }
+    for (int c = 0; c < n_cell; ++c)
+        if (!std::isfinite(volume[c]))
+            return fail(ctx, BTE_ERR_INVALID_ARGUMENT, "bte_set_geometry: non-finite volume");
+    ctx->dim = dim; ctx->n = n_cell; ctx->F = n_face;
+    ctx->nbr.assign(nbr, nbr + nf);
+    ctx->area.assign(area, area + nf);
+    ctx->normal.assign(normal, normal + 3 * nf);
+    ctx->volume.assign(volume, volume + n_cell);
+    ctx->has_geom = true;
+    ctx->dirty = true;
+    ctx->solved = false;
+    return BTE_OK;
+}
+
+bte_status bte_set_quadrature(bte_ctx* ctx, int n_dir, const double* s, const double* S,
+                              const double* omega, int DM, int num_theta, int num_phi,
+                              double solid_angle, double T_ref) {
+    if (!ctx) return BTE_ERR_INVALID_ARGUMENT;
+    if (n_dir <= 0 || !s || !S || !omega || (DM != 2 && DM != 3) || num_phi <= 0 || num_theta <= 0)
+        return fail(ctx, BTE_ERR_INVALID_ARGUMENT, "bte_set_quadrature: bad n_dir/DM/angles or null array");
+    ctx->n_dir = n_dir; ctx->DM = DM; ctx->num_theta = num_theta; ctx->num_phi = num_phi;
+    ctx->s.assign(s, s + 3 * n_dir);
+    ctx->S.assign(S, S + 3 * n_dir);
+    ctx->omega.assign(omega, omega + n_dir);
+    ctx->solid_angle = solid_angle;
+    ctx->T_ref = T_ref;
+    ctx->has_quad = true;
+    ctx->dirty = true;
+    ctx->solved = false;
+    return BTE_OK;
+}
+
+bte_status bte_set_bands(bte_ctx* ctx, int n_band, const double* vg, const double* tau,
+                         const double* C, const double* Lr) {
+    if (!ctx) return BTE_ERR_INVALID_ARGUMENT;
+    if (n_band <= 0 || !vg || !tau || !C || !Lr)
+        return fail(ctx, BTE_ERR_INVALID_ARGUMENT, "bte_set_bands: n_band <= 0 or null array");
+    ctx->n_band = n_band;
+    ctx->vg.assign(vg, vg + n_band);
+    ctx->tau.assign(tau, tau + n_band);
+    ctx->Cb.assign(C, C + n_band);
+    ctx->Lr.assign(Lr, Lr + n_band);
+    ctx->has_bands = true;
+    ctx->dirty = true;
+    ctx->solved = false;
+    return BTE_OK;
+}
+
+bte_status bte_set_bcs(bte_ctx* ctx, int n_bc, const int* index, const int* type, const double* T) {
+    if (!ctx) return BTE_ERR_INVALID_ARGUMENT;
+    if (n_bc < 0 || (n_bc > 0 && (!index || !type || !T)))
+        return fail(ctx, BTE_ERR_INVALID_ARGUMENT, "bte_set_bcs: bad n_bc or null array");
+    for (int i = 0; i < n_bc; ++i)
+        for (int j = 0; j < i; ++j)
+            if (index[i] == index[j])
+                return fail(ctx, BTE_ERR_INVALID_ARGUMENT,
+                            "bte_set_bcs: two boundary-condition rows name the same boundary entity");
+    ctx->n_bc = n_bc;
+    ctx->bc_index.assign(index, index + n_bc);
+    ctx->bc_type.assign(type, type + n_bc);
+    ctx->bc_T.assign(T, T + n_bc);
+    ctx->has_bcs = true;
+    ctx->dirty = true;
+    ctx->solved = false;
+    return BTE_OK;
+}
+
+}  // extern "C"
+
+// Specular partner of direction d (src/StaticBTESolver.cpp:205-252).
+static int mirror_of(int type, int dim, int d, int num_phi) {
+    const int it = d / (4 * num_phi);
+    int ip = d % (4 * num_phi);
+    if (type == 31) {
+        if (dim == 2) ip = ip >= 2 * num_phi ? 6 * num_phi - ip - 1 : 2 * num_phi - ip - 1;
+        else ip = 4 * num_phi - ip - 1;
+        return it * 4 * num_phi + ip;
+    }
+    if (type == 32) {
+        if (dim == 2) return it * 4 * num_phi + (4 * num_phi - ip - 1);
+        const int ix = ip / (2 * num_phi), isx = 2 * num_phi - ip % (2 * num_phi) - 1;
+        return it * 4 * num_phi + isx + ix * 2 * num_phi;
+    }
+    // 33: the polar index is mirrored with num_phi, as the reference does (:250)
+    const int iz = 2 * num_phi - it - 1;
+    return ip + iz * 4 * num_phi;
+}
+
+// Upload inputs, build boundary tables, per-direction geometry and state buffers.
+static bte_status setup(bte_ctx* ctx, int batch_systems) {
+    const int n = ctx->n, F = ctx->F, ND = ctx->n_dir, NB = ctx->n_band, dim = ctx->dim;
+    ctx->Np = (size_t)((n + bte::CH - 1) / bte::CH) * bte::CH;
+    ctx->nchunk = (int)(ctx->Np / bte::CH);
+    const size_t Np = ctx->Np;
+    cudaStream_t st = ctx->stream;
+
+    // ---- boundary faces matched to boundary-condition rows, sorted by (cell, face)
+    std::vector<int> bptr(Np + 1, 0), bf_cell, bf_face, bf_kind, bf_bc, bf_diff;
+    for (int c = 0; c < n; ++c) {
+        bptr[c] = (int)bf_cell.size();
+        for (int f = 0; f < F; ++f) {
+            const int code = ctx->nbr[(size_t)c * F + f];
+            if (code >= 0) continue;
+            for (int i = 0; i < ctx->n_bc; ++i) {
+                if (ctx->bc_index[i] != code) continue;
+                const int t = ctx->bc_type[i];
+                const bool ok = t == 1 || t == 2 || ((t == 31 || t == 32) && dim >= 2) || (t == 33 && dim == 3);
+                if (!ok) {
+                    char buf[160];
+                    std::snprintf(buf, sizeof(buf),
+                                  "boundary condition type %d on entity %d is not supported for a %dD mesh", t,
+                                  -code - 1, dim);
+                    return fail(ctx, BTE_ERR_UNSUPPORTED_BC, buf);
+                }
+                bf_cell.push_back(c); bf_face.push_back(f); bf_kind.push_back(t); bf_bc.push_back(i);
+                bf_diff.push_back(-1);
+                break;
+            }
+        }
+    }
+    for (size_t c = n; c <= Np; ++c) bptr[c] = (int)bf_cell.size();
+    const int nbf = (int)bf_cell.size();
+    ctx->nbf = nbf;
+    ctx->h_bf_bc = bf_bc;
+    std::vector<double> cin((size_t)ND * std::max(nbf, 1), 0.0), hw((size_t)std::max(nbf, 1) * ND, 0.0),
+        bf_area(std::max(nbf, 1), 0.0);
+    std::vector<int> dlist;
+    std::vector<double> wdiff, wden;
+    for (int k = 0; k < nbf; ++k) {
+        const size_t cf = (size_t)bf_cell[k] * F + bf_face[k];
+        const double* nn = &ctx->normal[3 * cf];
+        const double A = ctx->area[cf];
+        bf_area[k] = A;
+        double wsum = 0.0;
+        std::vector<double> w(ND, 0.0);
+        for (int d = 0; d < ND; ++d) {
+            const double sn = ctx->s[3 * d] * nn[0] + ctx->s[3 * d + 1] * nn[1] + ctx->s[3 * d + 2] * nn[2];
+            const double Sn = ctx->S[3 * d] * nn[0] + ctx->S[3 * d + 1] * nn[1] + ctx->S[3 * d + 2] * nn[2];
+            const double g = dim > 1 ? Sn : sn;
+            if (sn < 0) cin[(size_t)d * nbf + k] = A * g;
+            // heat-flux weights (:336-351)
+            if (ctx->DM == 3 && dim == 3) hw[(size_t)k * ND + d] = sn * A * ctx->omega[d];
+            else if (dim == 1) hw[(size_t)k * ND + d] = sn * ctx->omega[d];
+            else hw[(size_t)k * ND + d] = Sn * A;
+            // diffuse-wall weights over outgoing directions (:183-203)
+            if (sn > 0) {
+                if (dim == 3) { w[d] = Sn * ctx->omega[d]; wsum += Sn * ctx->omega[d]; }
+                else if (dim == 2) { w[d] = Sn; wsum += Sn; }
+                else w[d] = sn * ctx->omega[d];
+            }
+        }
+        if (bf_kind[k] == 2) {
+            bf_diff[k] = (int)dlist.size();
+            dlist.push_back(k);
+            wdiff.insert(wdiff.end(), w.begin(), w.end());
+            wden.push_back(dim != 1 ? wsum : M_PI);
+        }
+    }
+    ctx->ndiff = (int)dlist.size();
+    std::vector<double> eiso((size_t)NB * std::max(ctx->n_bc, 1), 0.0);
+    for (int b = 0; b < NB; ++b)
+        for (int i = 0; i < ctx->n_bc; ++i)
+            eiso[(size_t)b * ctx->n_bc + i] = ctx->Cb[b] / ctx->solid_angle * (ctx->bc_T[i] - ctx->T_ref);
+    std::vector<int> mir(3 * ND, 0);
+    for (int d = 0; d < ND; ++d) {
+        mir[d] = dim >= 2 ? mirror_of(31, dim, d, ctx->num_phi) : d;
+        mir[ND + d] = dim >= 2 ? mirror_of(32, dim, d, ctx->num_phi) : d;
+        mir[2 * ND + d] = dim == 3 ? mirror_of(33, dim, d, ctx->num_phi) : d;
+    }
+    for (int t = 0; t < 3; ++t)
+        for (int d = 0; d < ND; ++d)
+            if (mir[t * ND + d] < 0 || mir[t * ND + d] >= ND) {
+                bool used = false;
+                for (int k = 0; k < nbf; ++k) used |= bf_kind[k] == 31 + t;
+                if (used)
+                    return fail(ctx, BTE_ERR_UNSUPPORTED_BC,
+                                "specular boundary needs num_theta == num_phi for this direction set");
+                mir[t * ND + d] = d;
+            }
+    std::vector<double> kb(NB);
+    double Lr_sum = 0;
+    for (int b = 0; b < NB; ++b) kb[b] = ctx->vg[b] * ctx->tau[b];
+    (void)Lr_sum;
+    if (dlist.empty()) { dlist.push_back(0); wdiff.assign(ND, 0.0); wden.push_back(1.0); }
+    if (bf_cell.empty()) { bf_cell.push_back(0); bf_kind.push_back(1); bf_bc.push_back(0); bf_diff.push_back(-1); }
+
+    // ---- uploads
+    std::vector<int> nbpad((size_t)F * Np);
+    for (int f = 0; f < F; ++f)
+        for (size_t c = 0; c < Np; ++c) {
+            int v = c < (size_t)n ? ctx->nbr[c * F + f] : -1;
+            nbpad[(size_t)f * Np + c] = v >= 0 ? v : (int)c;
+        }
+    BTE_CUDA(upload(ctx->d_normal, ctx->normal, st));
+    BTE_CUDA(upload(ctx->d_area, ctx->area, st));
+    BTE_CUDA(upload(ctx->d_nbr, ctx->nbr, st));
+    BTE_CUDA(upload(ctx->d_volume, ctx->volume, st));
+    BTE_CUDA(upload(ctx->d_s, ctx->s, st));
+    BTE_CUDA(upload(ctx->d_S, ctx->S, st));
+    BTE_CUDA(upload(ctx->d_omega, ctx->omega, st));
+    BTE_CUDA(upload(ctx->d_nb, nbpad, st));
+    BTE_CUDA(upload(ctx->d_kb, kb, st));
+    BTE_CUDA(upload(ctx->d_Cb, ctx->Cb, st));
+    BTE_CUDA(upload(ctx->d_Lr, ctx->Lr, st));
+    BTE_CUDA(upload(ctx->d_vg, ctx->vg, st));
+    BTE_CUDA(upload(ctx->d_bptr, bptr, st));
+    BTE_CUDA(upload(ctx->d_bf_cell, bf_cell, st));
+    BTE_CUDA(upload(ctx->d_bf_kind, bf_kind, st));
+    BTE_CUDA(upload(ctx->d_bf_bc, bf_bc, st));
+    BTE_CUDA(upload(ctx->d_bf_diff, bf_diff, st));
+    BTE_CUDA(upload(ctx->d_cin, cin, st));
+    BTE_CUDA(upload(ctx->d_eiso, eiso, st));
+    BTE_CUDA(upload(ctx->d_mirror, mir, st));
+    BTE_CUDA(upload(ctx->d_dlist, dlist, st));
+    BTE_CUDA(upload(ctx->d_wdiff, wdiff, st));
+    BTE_CUDA(upload(ctx->d_wden, wden, st));
+    BTE_CUDA(upload(ctx->d_hw, hw, st));
+    BTE_CUDA(upload(ctx->d_bf_area, bf_area, st));
+    BTE_CUDA(ctx->d_ediff.alloc(sizeof(double) * NB * std::max(nbf, 1)));
+    BTE_CUDA(cudaMemsetAsync(ctx->d_ediff.p, 0, ctx->d_ediff.bytes, st));
+
+    // ---- per-direction geometry (one launch)
+    BTE_CUDA(ctx->d_dg.alloc(sizeof(double) * ND * Np));
+    BTE_CUDA(ctx->d_vo.alloc(sizeof(double) * ND * Np));
+    BTE_CUDA(ctx->d_fc.alloc(sizeof(double) * ND * F * Np));
+    {
+        dim3 grid((unsigned)((Np + 255) / 256), ND);
+        bte::k_direction_geometry<<<grid, 256, 0, st>>>(
+            ctx->d_normal.as<double>(), ctx->d_area.as<double>(), ctx->d_nbr.as<int>(), ctx->d_volume.as<double>(),
+            ctx->d_s.as<double>(), ctx->d_S.as<double>(), ctx->d_omega.as<double>(), n, F, dim, Np,
+            ctx->d_dg.as<double>(), ctx->d_vo.as<double>(), ctx->d_fc.as<double>());
+        BTE_LAUNCHED();
+    }
+
+    // ---- state
+    const size_t ne = (size_t)NB * ND * Np;
+    BTE_CUDA(ctx->d_e0.alloc(sizeof(double) * ne));
+    BTE_CUDA(ctx->d_e1.alloc(sizeof(double) * ne));
+    BTE_CUDA(ctx->d_ebar.alloc(sizeof(double) * NB * Np));
+    BTE_CUDA(ctx->d_Tb.alloc(sizeof(double) * NB * Np));
+    BTE_CUDA(ctx->d_T.alloc(sizeof(double) * Np));
+    BTE_CUDA(ctx->d_mpart.alloc(sizeof(double) * (Np / bte::THREADS + 1)));
+    BTE_CUDA(ctx->d_margin.alloc(sizeof(double) * 2));
+    BTE_CUDA(ctx->d_hpart.alloc(sizeof(double) * NB * std::max(nbf, 1)));
+    BTE_CUDA(ctx->d_qband.alloc(sizeof(double) * std::max(ctx->n_bc, 1) * NB));
+    BTE_CUDA(ctx->d_q.alloc(sizeof(double) * std::max(ctx->n_bc, 1)));
+
+    // ---- batch work buffers: nbb bands x all directions per batch
+    size_t free_b = 0, total_b = 0;
+    BTE_CUDA(cudaMemGetInfo(&free_b, &total_b));
+    const size_t per_sys = sizeof(double) * Np * 9 + sizeof(double) * 7 * ctx->nchunk + 64;
+    int nbb = NB;
+    if (batch_systems > 0) nbb = std::max(1, std::min(NB, batch_systems / ND));
+    const size_t reserve = (size_t)2 << 30;
+    while (nbb > 1 && (size_t)nbb * ND * per_sys + reserve > free_b) nbb = (nbb + 1) / 2;
+    ctx->nbb = nbb;
+    const size_t S = (size_t)nbb * ND;
+    for (DevBuf* b : {&ctx->w_r, &ctx->w_rw, &ctx->w_p, &ctx->w_ph, &ctx->w_q, &ctx->w_z, &ctx->w_t, &ctx->w_b,
+                      &ctx->w_invD})
+        BTE_CUDA(b->alloc(sizeof(double) * S * Np));
+    BTE_CUDA(ctx->s_done.alloc(sizeof(int) * S));
+    BTE_CUDA(ctx->s_iters.alloc(sizeof(int) * S));
+    BTE_CUDA(ctx->s_flagA.alloc(sizeof(int) * 2 * S));
+    BTE_CUDA(ctx->s_flagB.alloc(sizeof(int) * 2 * S));
+    BTE_CUDA(ctx->s_rho.alloc(sizeof(double) * 2 * S));
+    BTE_CUDA(ctx->s_alpha.alloc(sizeof(double) * S));
+    BTE_CUDA(ctx->s_omega.alloc(sizeof(double) * S));
+    BTE_CUDA(ctx->s_nrmr.alloc(sizeof(double) * S));
+    BTE_CUDA(ctx->s_nrm0.alloc(sizeof(double) * S));
+    BTE_CUDA(ctx->s_part.alloc(sizeof(double) * 7 * S * ctx->nchunk));
+    ctx->h_done.resize(S);
+    ctx->h_iters.resize(S);
+    ctx->dirty = false;
+    return BTE_OK;
+}
+
+// Launch a kernel, optionally bracketed by profiling events.
+#define BTE_LAUNCH(kind, iter, bytes_fixed, bytes_per_active, ...)                      \
+    do {                                                                                \
+        size_t _slot = 0;                                                               \
+        BTE_CUDA(prof_begin(ctx, &_slot));                                              \
+        __VA_ARGS__;                                                                    \
+        BTE_LAUNCHED();                                                                 \
+        BTE_CUDA(prof_end(ctx, _slot, (kind), (iter), (bytes_fixed), (bytes_per_active))); \
+    } while (0)
+
+// Solve all systems of one batch (bands b0 .. b0+nbb-1, every direction) with
+// the plain FP64 BiCGSTAB; x lands in e_curr.
+static bte_status solve_batch_plain(bte_ctx* ctx, int b0, int nbb, const bte_options& o, bte_report& rep) {
+    cudaStream_t st = ctx->stream;
+    const int S = nbb * ctx->n_dir;
+    const double N = ctx->n, w = sizeof(double);
+    // algorithmic HBM bytes: vector passes per active system, plus the
+    // per-direction geometry of an SpMV read once per direction in the launch
+    const double geo = N * ((ctx->F + 2) * w + ctx->F * 4.0) * std::min(S, ctx->n_dir);
+    bte::FaceFluxOp op{ctx->d_dg.as<double>(), ctx->d_vo.as<double>(), ctx->d_fc.as<double>(),
+                       ctx->d_nb.as<int>(), ctx->d_kb.as<double>(), ctx->e_curr, ctx->F, nbb, b0,
+                       ctx->n_dir, ctx->Np};
+    bte::Boundary bd{ctx->d_bptr.as<int>(), ctx->d_bf_cell.as<int>(), ctx->d_bf_kind.as<int>(),
+                     ctx->d_bf_bc.as<int>(), ctx->d_bf_diff.as<int>(), ctx->d_cin.as<double>(),
+                     ctx->d_eiso.as<double>(), ctx->d_mirror.as<int>(), ctx->d_ediff.as<double>(),
+                     ctx->nbf, std::max(ctx->n_bc, 1)};
+    dim3 grid(ctx->nchunk, S);
+    BTE_LAUNCH(KK_RHS, -1, S * N * 2 * w + geo / 2, 0,
+               bte::k_rhs<<<grid, bte::THREADS, 0, st>>>(op, bd, ctx->d_ebar.as<double>(), ctx->e_prev,
+                                                         ctx->w_b.as<double>(), ctx->n));
+
+    const int maxit = o.inner_maxit;
+    if (ctx->active_cap < maxit + 2) {
+        BTE_CUDA(ctx->s_active.alloc(sizeof(int) * (maxit + 2)));
+        ctx->active_cap = maxit + 2;
+    }
+    BTE_CUDA(cudaMemsetAsync(ctx->s_active.p, 0, sizeof(int) * (maxit + 2), st));
+    bte::BicgState bs{ctx->s_done.as<int>(), ctx->s_iters.as<int>(), ctx->s_flagA.as<int>(), ctx->s_flagB.as<int>(),
+                      ctx->s_rho.as<double>(), ctx->s_alpha.as<double>(), ctx->s_omega.as<double>(),
+                      ctx->s_nrmr.as<double>(), ctx->s_nrm0.as<double>(), ctx->s_part.as<double>(),
+                      ctx->s_active.as<int>(), S, ctx->nchunk, o.inner_tol, maxit};
+    bte::BicgVecs<double> v{ctx->w_r.as<double>(), ctx->w_rw.as<double>(), ctx->w_p.as<double>(),
+                            ctx->w_ph.as<double>(), ctx->w_q.as<double>(), ctx->w_z.as<double>(),
+                            ctx->w_t.as<double>(), ctx->w_b.as<double>(), ctx->w_invD.as<double>(), ctx->Np};
+    BTE_LAUNCH(KK_INIT, -1, S * N * 7 * w + geo / 2, 0, bte::k_bicg_init<<<grid, bte::THREADS, 0, st>>>(op, v, bs));
+    BTE_LAUNCH(KK_INIT, -1, 0, 0, bte::k_bicg_init_scalars<<<(S + 127) / 128, 128, 0, st>>>(bs));
+    int i = 1;
+    for (;;) {
+        int last = i;
+        for (int g = 0; g < kGroup && i <= maxit + 1; ++g, ++i) {
+            BTE_LAUNCH(KK_P, i, 0, N * 6 * w, bte::k_bicg_p<<<grid, bte::THREADS, 0, st>>>(op, v, bs, i));
+            last = i;
+            if (i > maxit) break;
+            BTE_LAUNCH(KK_SPMV1, i, geo, N * 3 * w, bte::k_bicg_spmv1<<<grid, bte::THREADS, 0, st>>>(op, v, bs, i));
+            BTE_LAUNCH(KK_S, i, 0, N * 5 * w, bte::k_bicg_s<<<grid, bte::THREADS, 0, st>>>(op, v, bs, i));
+            BTE_LAUNCH(KK_SPMV2, i, geo, N * 3 * w, bte::k_bicg_spmv2<<<grid, bte::THREADS, 0, st>>>(op, v, bs, i));
+            BTE_LAUNCH(KK_X, i, 0, N * 8 * w, bte::k_bicg_x<<<grid, bte::THREADS, 0, st>>>(op, v, bs, i));
+        }
+        BTE_CUDA(cudaMemcpyAsync(ctx->h_pinned_i, ctx->s_active.as<int>() + last, sizeof(int),
+                                 cudaMemcpyDeviceToHost, st));
+        BTE_CUDA(cudaStreamSynchronize(st));
+        if (ctx->h_pinned_i[0] == 0 || last > maxit) break;
+        if (i > maxit + 1) break;
+    }
+    BTE_CUDA(cudaMemcpyAsync(ctx->h_done.data(), ctx->s_done.p, sizeof(int) * S, cudaMemcpyDeviceToHost, st));
+    BTE_CUDA(cudaMemcpyAsync(ctx->h_iters.data(), ctx->s_iters.p, sizeof(int) * S, cudaMemcpyDeviceToHost, st));
+    if (ctx->profile) {
+        ctx->h_active.resize(maxit + 2);
+        BTE_CUDA(cudaMemcpyAsync(ctx->h_active.data(), ctx->s_active.p, sizeof(int) * (maxit + 2),
+                                 cudaMemcpyDeviceToHost, st));
+    }
+    BTE_CUDA(cudaStreamSynchronize(st));
+    if (ctx->profile) prof_resolve(ctx, ctx->h_active.data(), maxit + 2);
+    for (int y = 0; y < S; ++y) {
+        rep.inner_iterations += ctx->h_iters[y];
+        if (ctx->h_done[y] == 3 || ctx->h_done[y] == 0) ++rep.inner_unconverged;
+    }
+    rep.inner_solves += S;
+    return BTE_OK;
+}
+
+extern "C" bte_status bte_solve(bte_ctx* ctx, const bte_options* opts, bte_report* report) {
+    if (!ctx) return BTE_ERR_INVALID_ARGUMENT;
+    if (!(ctx->has_geom && ctx->has_quad && ctx->has_bands && ctx->has_bcs))
+        return fail(ctx, BTE_ERR_STATE, "bte_solve: set geometry, quadrature, bands and boundary conditions first");
+    bte_options o;
+    if (opts) o = *opts;
+    else bte_default_options(&o);
+    if (o.max_iter < 0 || o.inner_maxit <= 0 || !(o.inner_tol > 0))
+        return fail(ctx, BTE_ERR_INVALID_ARGUMENT, "bte_solve: bad options");
+    if (o.form != BTE_FORM_PLAIN)
+        return fail(ctx, BTE_ERR_INVALID_ARGUMENT, "bte_solve: form not available in this build");
+    if (ctx->dim == 1 && ctx->F != 2) return fail(ctx, BTE_ERR_INVALID_ARGUMENT, "1D mesh needs 2 faces");
+    BTE_CUDA(cudaSetDevice(ctx->device));
+    bte_report rep;
+    std::memset(&rep, 0, sizeof(rep));
+    ctx->launches = 0;
+    ctx->profile = o.profile != 0;
+    ctx->pending.clear();
+    ctx->ev_next = 0;
+    for (int k = 0; k < kNumKinds; ++k) {
+        std::memset(&ctx->stats[k], 0, sizeof(bte_kernel_stat));
+        std::snprintf(ctx->stats[k].name, sizeof(ctx->stats[k].name), "%s", kKindNames[k]);
+    }
+    if (ctx->dirty) {
+        bte_status s = setup(ctx, o.batch_systems);
+        if (s != BTE_OK) return s;
+    }
+    cudaStream_t st = ctx->stream;
+    const int NB = ctx->n_band, ND = ctx->n_dir;
+    const size_t Np = ctx->Np;
+    ctx->e_curr = ctx->d_e0.as<double>();
+    ctx->e_prev = ctx->d_e1.as<double>();
+    BTE_CUDA(cudaMemsetAsync(ctx->e_curr, 0, sizeof(double) * NB * ND * Np, st));
+    BTE_CUDA(cudaMemsetAsync(ctx->d_ebar.p, 0, sizeof(double) * NB * Np, st));  // cell_band_density = 0 (:92)
+    ctx->margins.clear();
+    double Lr_sum = 0;
+    for (int b = 0; b < NB; ++b) Lr_sum += ctx->Lr[b];
+    cudaEvent_t ev[5];
+    for (auto& e : ev) BTE_CUDA(cudaEventCreate(&e));
+    struct EvGuard { cudaEvent_t* e; ~EvGuard() { for (int k = 0; k < 5; ++k) cudaEventDestroy(e[k]); } } guard{ev};
+    bte_status result = BTE_ERR_NOT_CONVERGED;
+    const int nred = (int)(Np / bte::THREADS);
+    for (int it = 0; it < o.max_iter; ++it) {
+        std::swap(ctx->e_curr, ctx->e_prev);
+        BTE_CUDA(cudaEventRecord(ev[0], st));
+        if (ctx->ndiff > 0) {
+            const int nt = ctx->ndiff * NB;
+            BTE_LAUNCH(KK_DIFFUSE, -1, (double)nt * (ND + 1) * 8.0, 0,
+                       bte::k_diffuse_wall<<<(nt + 127) / 128, 128, 0, st>>>(
+                           ctx->e_prev, ctx->d_dlist.as<int>(), ctx->d_bf_cell.as<int>(), ctx->d_wdiff.as<double>(),
+                           ctx->d_wden.as<double>(), ctx->ndiff, NB, ND, Np, ctx->nbf, ctx->d_ediff.as<double>()));
+        }
+        BTE_CUDA(cudaEventRecord(ev[1], st));
+        for (int b0 = 0; b0 < NB; b0 += ctx->nbb) {
+            const int nbb = std::min(ctx->nbb, NB - b0);
+            bte_status s = solve_batch_plain(ctx, b0, nbb, o, rep);
+            if (s != BTE_OK) return s;
+        }
+        BTE_CUDA(cudaEventRecord(ev[2], st));
+        BTE_LAUNCH(KK_REDUCE, -1, (2.0 * NB * ND + 2.0 * NB + 1) * ctx->n * 8.0, 0,
+                   bte::k_reduce<<<nred, bte::THREADS, 0, st>>>(ctx->e_curr, ctx->e_prev, ctx->d_omega.as<double>(),
+                                                              ctx->d_Cb.as<double>(), ctx->d_Lr.as<double>(), Lr_sum,
+                                                              ctx->T_ref, ctx->solid_angle, ctx->n, NB, ND, Np,
+                                                              ctx->d_Tb.as<double>(), ctx->d_T.as<double>(),
+                                                              ctx->d_ebar.as<double>(), ctx->d_mpart.as<double>()));
+        bte::k_margin_final<<<1, 32, 0, st>>>(ctx->d_mpart.as<double>(), nred, (double)NB * ctx->n,
+                                             ctx->d_margin.as<double>());
+        BTE_LAUNCHED();
+        BTE_CUDA(cudaEventRecord(ev[3], st));
+        BTE_CUDA(cudaMemcpyAsync(ctx->h_pinned, ctx->d_margin.p, sizeof(double), cudaMemcpyDeviceToHost, st));
+        BTE_CUDA(cudaStreamSynchronize(st));
+        if (ctx->profile) prof_resolve(ctx, nullptr, 0);
+        const double m = ctx->h_pinned[0];
+        float t01 = 0, t12 = 0, t23 = 0;
+        cudaEventElapsedTime(&t01, ev[0], ev[1]);
+        cudaEventElapsedTime(&t12, ev[1], ev[2]);
+        cudaEventElapsedTime(&t23, ev[2], ev[3]);
+        rep.ms_rhs += t01;
+        rep.ms_inner += t12;
+        rep.ms_reduce += t23;
+        rep.ms_total += t01 + t12 + t23;
+        ctx->margins.push_back(m);
+        rep.n_iter = it + 1;
+        rep.final_margin = m;
+        if (o.on_iteration) o.on_iteration(o.user, it, m, (double)(t01 + t12 + t23));
+        if (!std::isfinite(m)) {
+            result = BTE_ERR_NUMERICAL;
+            ctx->err = "non-finite margin in outer iteration " + std::to_string(it);
+            break;
+        }
+        if (m <= o.tol) {
+            rep.converged = 1;
+            result = BTE_OK;
+            break;
+        }
+    }
+    if (o.max_iter == 0) result = BTE_OK;
+    // heat flux (src/StaticBTESolver.cpp:323-370)
+    if (ctx->nbf > 0) {
+        const int nt = ctx->nbf * NB;
+        BTE_LAUNCH(KK_HEAT, -1, (double)nt * ND * 16.0, 0,
+                   bte::k_heat_face<<<(nt + 127) / 128, 128, 0, st>>>(ctx->e_curr, ctx->d_bf_cell.as<int>(),
+                                                                    ctx->d_hw.as<double>(), ctx->nbf, NB, ND, Np,
+                                                                    ctx->d_hpart.as<double>()));
+    }
+    bte::k_heat_final<<<1, 256, 0, st>>>(ctx->d_hpart.as<double>(), ctx->d_bf_bc.as<int>(),
+                                        ctx->d_bf_area.as<double>(), ctx->d_vg.as<double>(), ctx->nbf, NB,
+                                        ctx->n_bc, ctx->dim, ctx->d_qband.as<double>(), ctx->d_q.as<double>());
+    BTE_LAUNCHED();
+    BTE_CUDA(cudaStreamSynchronize(st));
+    if (ctx->profile) prof_resolve(ctx, nullptr, 0);
+    rep.kernel_launches = ctx->launches;
+    ctx->solved = true;
+    if (report) *report = rep;
+    if (result == BTE_ERR_NOT_CONVERGED && ctx->err.empty()) ctx->err = "max_iter reached";
+    return result;
+}
+
+extern "C" {
+
+bte_status bte_get_temperature(bte_ctx* ctx, double* T) {
+    if (!ctx || !T) return BTE_ERR_INVALID_ARGUMENT;
+    if (!ctx->solved) return fail(ctx, BTE_ERR_STATE, "no solution yet");
+    BTE_CUDA(cudaSetDevice(ctx->device));
+    BTE_CUDA(cudaMemcpyAsync(T, ctx->d_T.p, sizeof(double) * ctx->n, cudaMemcpyDeviceToHost, ctx->stream));
+    BTE_CUDA(cudaStreamSynchronize(ctx->stream));
+    return BTE_OK;
+}
+
+bte_status bte_get_band_temperature(bte_ctx* ctx, double* Tb) {
+    if (!ctx || !Tb) return BTE_ERR_INVALID_ARGUMENT;
+    if (!ctx->solved) return fail(ctx, BTE_ERR_STATE, "no solution yet");
+    BTE_CUDA(cudaSetDevice(ctx->device));
+    std::vector<double> tmp((size_t)ctx->n_band * ctx->n);
+    BTE_CUDA(cudaMemcpy2DAsync(tmp.data(), sizeof(double) * ctx->n, ctx->d_Tb.p, sizeof(double) * ctx->Np,
+                               sizeof(double) * ctx->n, ctx->n_band, cudaMemcpyDeviceToHost, ctx->stream));
+    BTE_CUDA(cudaStreamSynchronize(ctx->stream));
+    for (int c = 0; c < ctx->n; ++c)
+        for (int b = 0; b < ctx->n_band; ++b) Tb[(size_t)c * ctx->n_band + b] = tmp[(size_t)b * ctx->n + c];
+    return BTE_OK;
+}
+
+bte_status bte_get_heat_flux(bte_ctx* ctx, double* q_bc, double* q_bc_band) {
+    if (!ctx || !q_bc) return BTE_ERR_INVALID_ARGUMENT;
+    if (!ctx->solved) return fail(ctx, BTE_ERR_STATE, "no solution yet");
+    BTE_CUDA(cudaSetDevice(ctx->device));
+    if (ctx->n_bc > 0) {
+        BTE_CUDA(cudaMemcpyAsync(q_bc, ctx->d_q.p, sizeof(double) * ctx->n_bc, cudaMemcpyDeviceToHost, ctx->stream));
+        if (q_bc_band)
+            BTE_CUDA(cudaMemcpyAsync(q_bc_band, ctx->d_qband.p, sizeof(double) * ctx->n_bc * ctx->n_band,
+                                     cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    BTE_CUDA(cudaStreamSynchronize(ctx->stream));
+    return BTE_OK;
+}
+
+bte_status bte_get_energy(bte_ctx* ctx, double* e) {
+    if (!ctx || !e) return BTE_ERR_INVALID_ARGUMENT;
+    if (!ctx->solved) return fail(ctx, BTE_ERR_STATE, "no solution yet");
+    BTE_CUDA(cudaSetDevice(ctx->device));
+    BTE_CUDA(cudaMemcpy2DAsync(e, sizeof(double) * ctx->n, ctx->e_curr, sizeof(double) * ctx->Np,
+                               sizeof(double) * ctx->n, (size_t)ctx->n_band * ctx->n_dir, cudaMemcpyDeviceToHost,
+                               ctx->stream));
+    BTE_CUDA(cudaStreamSynchronize(ctx->stream));
+    return BTE_OK;
+}
+
+bte_status bte_get_margins(bte_ctx* ctx, double* m, int cap, int* n) {
+    if (!ctx) return BTE_ERR_INVALID_ARGUMENT;
+    int k = (int)ctx->margins.size();
+    for (int i = 0; i < k && i < cap && m; ++i) m[i] = ctx->margins[i];
+    if (n) *n = k;
+    return BTE_OK;
+}
+
+bte_status bte_get_kernel_stats(bte_ctx* ctx, bte_kernel_stat* stats, int cap, int* n) {
+    if (!ctx) return BTE_ERR_INVALID_ARGUMENT;
+    for (int k = 0; k < kNumKinds && k < cap && stats; ++k) stats[k] = ctx->stats[k];
+    if (n) *n = kNumKinds;
+    return BTE_OK;
+}
+
+// Single CSR system (the reference's BICGSTAB::init + solve), host buffers.
+bte_status bte_bicgstab_csr(int n, const int* rowptr, const int* colind, const double* val, int nnz,
+                            const double* b, double* x, int maxit, double tol, int* iterations,
+                            int* converged) {
+    if (n <= 0 || !rowptr || !colind || !val || !b || !x || nnz < 0 || maxit <= 0 || !(tol > 0))
+        return BTE_ERR_INVALID_ARGUMENT;
+    if (rowptr[0] != 0 || rowptr[n] != nnz) return BTE_ERR_INVALID_ARGUMENT;
+    for (int i = 0; i < n; ++i)
+        if (rowptr[i + 1] < rowptr[i]) return BTE_ERR_INVALID_ARGUMENT;
+    for (int k = 0; k < nnz; ++k)
+        if (colind[k] < 0 || colind[k] >= n) return BTE_ERR_INVALID_ARGUMENT;
+    bte_ctx tmp;  // scratch holder for error text and buffers
+    bte_ctx* ctx = &tmp;
+    int dev = 0;
+    BTE_CUDA(cudaGetDevice(&dev));
+    BTE_CUDA(cudaStreamCreateWithFlags(&tmp.stream, cudaStreamNonBlocking));
+    struct StreamGuard { cudaStream_t s; ~StreamGuard() { cudaStreamSynchronize(s); cudaStreamDestroy(s); } } sg{tmp.stream};
+    cudaStream_t st = tmp.stream;
+    const size_t Np = (size_t)((n + bte::CH - 1) / bte::CH) * bte::CH;
+    const int nchunk = (int)(Np / bte::CH);
+    DevBuf d_rp, d_ci, d_v, d_x;
+    BTE_CUDA(d_rp.alloc(sizeof(int) * (n + 1)));
+    BTE_CUDA(d_ci.alloc(sizeof(int) * std::max(nnz, 1)));
+    BTE_CUDA(d_v.alloc(sizeof(double) * std::max(nnz, 1)));
+    BTE_CUDA(d_x.alloc(sizeof(double) * Np));
+    for (DevBuf* w : {&tmp.w_r, &tmp.w_rw, &tmp.w_p, &tmp.w_ph, &tmp.w_q, &tmp.w_z, &tmp.w_t, &tmp.w_b, &tmp.w_invD})
+        BTE_CUDA(w->alloc(sizeof(double) * Np));
+    BTE_CUDA(tmp.s_done.alloc(sizeof(int)));
+    BTE_CUDA(tmp.s_iters.alloc(sizeof(int)));
+    BTE_CUDA(tmp.s_flagA.alloc(sizeof(int) * 2));
+    BTE_CUDA(tmp.s_flagB.alloc(sizeof(int) * 2));
+    BTE_CUDA(tmp.s_rho.alloc(sizeof(double) * 2));
+    BTE_CUDA(tmp.s_alpha.alloc(sizeof(double)));
+    BTE_CUDA(tmp.s_omega.alloc(sizeof(double)));
+    BTE_CUDA(tmp.s_nrmr.alloc(sizeof(double)));
+    BTE_CUDA(tmp.s_nrm0.alloc(sizeof(double)));
+    BTE_CUDA(tmp.s_part.alloc(sizeof(double) * 7 * nchunk));
+    BTE_CUDA(tmp.s_active.alloc(sizeof(int) * (maxit + 2)));
+    BTE_CUDA(cudaMemcpyAsync(d_rp.p, rowptr, sizeof(int) * (n + 1), cudaMemcpyHostToDevice, st));
+    if (nnz > 0) {
+        BTE_CUDA(cudaMemcpyAsync(d_ci.p, colind, sizeof(int) * nnz, cudaMemcpyHostToDevice, st));
+        BTE_CUDA(cudaMemcpyAsync(d_v.p, val, sizeof(double) * nnz, cudaMemcpyHostToDevice, st));
+    }
+    BTE_CUDA(cudaMemsetAsync(tmp.w_b.p, 0, sizeof(double) * Np, st));
+    BTE_CUDA(cudaMemcpyAsync(tmp.w_b.p, b, sizeof(double) * n, cudaMemcpyHostToDevice, st));
+    BTE_CUDA(cudaMemsetAsync(tmp.s_active.p, 0, sizeof(int) * (maxit + 2), st));
+    bte::CsrOp op{d_rp.as<int>(), d_ci.as<int>(), d_v.as<double>(), d_x.as<double>(), n, Np};
+    bte::BicgState bs{tmp.s_done.as<int>(), tmp.s_iters.as<int>(), tmp.s_flagA.as<int>(), tmp.s_flagB.as<int>(),
+                      tmp.s_rho.as<double>(), tmp.s_alpha.as<double>(), tmp.s_omega.as<double>(),
+                      tmp.s_nrmr.as<double>(), tmp.s_nrm0.as<double>(), tmp.s_part.as<double>(),
+                      tmp.s_active.as<int>(), 1, nchunk, tol, maxit};
+    bte::BicgVecs<double> v{tmp.w_r.as<double>(), tmp.w_rw.as<double>(), tmp.w_p.as<double>(),
+                            tmp.w_ph.as<double>(), tmp.w_q.as<double>(), tmp.w_z.as<double>(),
+                            tmp.w_t.as<double>(), tmp.w_b.as<double>(), tmp.w_invD.as<double>(), Np};
+    dim3 grid(nchunk, 1);
+    bte::k_bicg_init<<<grid, bte::THREADS, 0, st>>>(op, v, bs);
+    BTE_LAUNCHED();
+    bte::k_bicg_init_scalars<<<1, 32, 0, st>>>(bs);
+    BTE_LAUNCHED();
+    int i = 1;
+    for (;;) {
+        int last = i;
+        for (int g = 0; g < kGroup && i <= maxit + 1; ++g, ++i) {
+            bte::k_bicg_p<<<grid, bte::THREADS, 0, st>>>(op, v, bs, i);
+            BTE_LAUNCHED();
+            last = i;
+            if (i > maxit) break;
+            bte::k_bicg_spmv1<<<grid, bte::THREADS, 0, st>>>(op, v, bs, i);
+            BTE_LAUNCHED();
+            bte::k_bicg_s<<<grid, bte::THREADS, 0, st>>>(op, v, bs, i);
+            BTE_LAUNCHED();
+            bte::k_bicg_spmv2<<<grid, bte::THREADS, 0, st>>>(op, v, bs, i);
+            BTE_LAUNCHED();
+            bte::k_bicg_x<<<grid, bte::THREADS, 0, st>>>(op, v, bs, i);
+            BTE_LAUNCHED();
+        }
+        BTE_CUDA(cudaMemcpyAsync(&tmp.h_done.emplace_back(0), bs.active + last, sizeof(int),
+                                 cudaMemcpyDeviceToHost, st));
+        BTE_CUDA(cudaStreamSynchronize(st));
+        if (tmp.h_done.back() == 0 || last > maxit || i > maxit + 1) break;
+    }
+    int done = 0, its = 0;
+    BTE_CUDA(cudaMemcpyAsync(x, d_x.p, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+    BTE_CUDA(cudaMemcpyAsync(&done, bs.done, sizeof(int), cudaMemcpyDeviceToHost, st));
+    BTE_CUDA(cudaMemcpyAsync(&its, bs.iters, sizeof(int), cudaMemcpyDeviceToHost, st));
+    BTE_CUDA(cudaStreamSynchronize(st));
+    if (iterations) *iterations = its;
+    if (converged) *converged = (done == 1 || done == 2) ? 1 : 0;
+    return BTE_OK;
+}
+
+}  // extern "C"

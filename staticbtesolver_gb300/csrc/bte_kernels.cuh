@@ -1,0 +1,368 @@
+// bte_kernels.cuh -- sm_103a kernels of the batched DOM-FVM phonon BTE solve.
+//
+// Data layout in HBM (Np = n_cell rounded up to CH; padded cells carry an
+// identity row and a zero right-hand side, so they stay zero and never enter
+// a dot product):
+//   e_curr/e_prev   [n_band][n_dir][Np]  FP64, the reference's ee_curr/ee_prev
+//                                        (src/StaticBTESolver.cpp:702-717)
+//   dg, vo          [n_dir][Np]          per-direction diagonal geometry
+//   fc              [n_dir][n_face][Np]  per-direction inflow face coefficients
+//   nb              [n_face][Np]         neighbour cell (self when none)
+//   BiCGSTAB work   [batch systems][Np]  one row per (band, direction) system
+//
+// A (band b, direction d) system of the reference (_get_Ke, :122-160) is
+//   A[c][c]      = k_b * sum_{outflow f} A_cf g_dcf + V_c Omega_d      (1D: + V_c)
+//   A[c][nb(c,f)] = k_b * A_cf g_dcf            for inflow faces with a neighbour
+// with k_b = v_g,b tau_b and g_dcf = S_d . n_cf (1D: s_d . n_cf), so it is
+// applied matrix-free from band-independent per-direction geometry:
+//   (A x)[c] = (k_b dg[d][c] + vo[d][c]) x[c] + k_b sum_f fc[d][f][c] x[nb[f][c]].
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace bte {
+
+constexpr int THREADS = 256;
+constexpr int CPT = 4;                 // cells per thread per chunk
+constexpr int CH = THREADS * CPT;      // cells per block ("chunk")
+constexpr int NWARP = THREADS / 32;
+
+// ----------------------------------------------------------------------------
+// Deterministic block reductions (fixed shuffle tree + fixed warp order).
+template <int K>
+__device__ __forceinline__ void block_sum(double (&v)[K], double (*smem)[NWARP]) {
+#pragma unroll
+    for (int k = 0; k < K; ++k)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < K; ++k) smem[k][warp] = v[k];
+    __syncthreads();
+    if (threadIdx.x == 0)
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            double s = 0;
+#pragma unroll
+            for (int w = 0; w < NWARP; ++w) s += smem[k][w];
+            v[k] = s;
+        }
+}
+
+// Sum of the per-chunk partials of one system, in chunk order.
+__device__ __forceinline__ double sum_parts(const double* p, int n) {
+    double s = 0;
+    for (int i = 0; i < n; ++i) s += p[i];
+    return s;
+}
+
+// ----------------------------------------------------------------------------
+// Batched BiCGSTAB state.  One row per system y of the batch.
+struct BicgState {
+    int* done;        // 0 active, 1 converged, 2 zero residual, 3 iteration limit
+    int* iters;       // iterations used (set when done)
+    int* flagA;       // [2][S] restart in the p-update phase of iteration parity
+    int* flagB;       // [2][S] restart in the s-update phase
+    double* rho;      // [2][S]
+    double* alpha;    // [S]
+    double* omega;    // [S]
+    double* nrmr;     // [S] last ||r||
+    double* nrm0;     // [S] ||b||
+    double* part;     // [7][S][nchunk] partial dot products
+    int* active;      // [maxit + 2] number of active systems at each iteration
+    int S, nchunk;
+    double tol;
+    int maxit;
+    __device__ double* P(int kind, int y) const { return part + ((size_t)kind * S + y) * nchunk; }
+};
+enum { PK_RR0 = 0, PK_RR1 = 1, PK_RWR0 = 2, PK_RWR1 = 3, PK_RWQ = 4, PK_TS = 5, PK_TT = 6 };
+
+template <typename T>
+struct BicgVecs {
+    T* r; T* rw; T* p; T* ph; T* q; T* z; T* t; const T* b; T* invD;
+    size_t Np;
+};
+
+// Matrix-free upwind operator of all (band, direction) systems of a batch.
+// Batch row y -> direction y / nbb, band b0 + y % nbb (the bands of one
+// direction are adjacent so they share that direction's geometry in L2).
+struct FaceFluxOp {
+    const double* dg;
+    const double* vo;
+    const double* fc;
+    const int* nb;
+    const double* kb;  // k_b = v_g tau per band
+    double* x_out;     // e_curr base [n_band][n_dir][Np]
+    int F, nbb, b0, n_dir;
+    size_t Np;
+    __device__ __forceinline__ void bd(int y, int& b, int& d) const {
+        d = y / nbb;
+        b = b0 + y % nbb;
+    }
+    __device__ __forceinline__ double* x_of(int y) const {
+        int b, d;
+        bd(y, b, d);
+        return x_out + ((size_t)b * n_dir + d) * Np;
+    }
+    __device__ __forceinline__ double diag(int y, int c) const {
+        int b, d;
+        bd(y, b, d);
+        return fma(kb[b], dg[(size_t)d * Np + c], vo[(size_t)d * Np + c]);
+    }
+    template <typename T>
+    __device__ __forceinline__ T apply(int y, int c, const T* __restrict__ xs) const {
+        int b, d;
+        bd(y, b, d);
+        const double k = kb[b];
+        const size_t dc = (size_t)d * Np + c;
+        double acc = fma(k, dg[dc], vo[dc]) * (double)xs[c];
+        double off = 0.0;
+        for (int f = 0; f < F; ++f)
+            off = fma(fc[((size_t)d * F + f) * Np + c], (double)xs[nb[(size_t)f * Np + c]], off);
+        return (T)fma(k, off, acc);
+    }
+};
+
+// One or more independent CSR systems (the reference's BICGSTAB boundary).
+struct CsrOp {
+    const int* rowptr;
+    const int* col;
+    const double* val;
+    double* x_out;
+    int n;
+    size_t Np;
+    __device__ __forceinline__ double* x_of(int) const { return x_out; }
+    __device__ __forceinline__ double diag(int, int c) const {
+        if (c >= n) return 1.0;
+        double dv = 0.0;  // src/bicgstab.hpp:125-131: the last diagonal entry wins
+        for (int k = rowptr[c]; k < rowptr[c + 1]; ++k)
+            if (col[k] == c) dv = val[k];
+        return dv;
+    }
+    template <typename T>
+    __device__ __forceinline__ T apply(int, int c, const T* __restrict__ xs) const {
+        if (c >= n) return xs[c];
+        double s = 0.0;
+        for (int k = rowptr[c]; k < rowptr[c + 1]; ++k) s = fma(val[k], (double)xs[col[k]], s);
+        return (T)s;
+    }
+};
+
+#define BTE_CELL_LOOP(c)                                                     \
+    for (int _k = 0, c = blockIdx.x * CH + threadIdx.x; _k < CPT; ++_k, c += THREADS)
+
+// K0: x = 0, r = p = r_hat = b, q = 0, invD; partial ||b||^2 (src/bicgstab.hpp:146-162).
+template <typename Op>
+__global__ void __launch_bounds__(THREADS) k_bicg_init(Op op, BicgVecs<double> v, BicgState st) {
+    __shared__ double sm[2][NWARP];
+    const int y = blockIdx.y;
+    const size_t o = (size_t)y * v.Np;
+    double* x = op.x_of(y);
+    double acc[2] = {0, 0};
+    BTE_CELL_LOOP(c) {
+        double bb = v.b[o + c];
+        double dv = op.diag(y, c);
+        v.invD[o + c] = 1.0 / dv;
+        v.r[o + c] = bb; v.p[o + c] = bb; v.rw[o + c] = bb; v.q[o + c] = 0.0;
+        x[c] = 0.0;
+        acc[0] = fma(bb, bb, acc[0]);
+    }
+    acc[1] = acc[0];
+    block_sum<2>(acc, sm);
+    if (threadIdx.x == 0) {
+        st.P(PK_RR0, y)[blockIdx.x] = acc[0];
+        st.P(PK_RWR0, y)[blockIdx.x] = acc[1];
+    }
+}
+
+// One thread per system: scalars after K0.
+__global__ void k_bicg_init_scalars(BicgState st) {
+    int y = blockIdx.x * blockDim.x + threadIdx.x;
+    if (y >= st.S) return;
+    double n0 = sqrt(sum_parts(st.P(PK_RR0, y), st.nchunk));
+    st.nrm0[y] = n0;
+    st.nrmr[y] = n0;
+    st.rho[y] = 1.0; st.rho[st.S + y] = 1.0;
+    st.alpha[y] = 1.0; st.omega[y] = 1.0;
+    st.done[y] = 0; st.iters[y] = 0;
+    st.flagA[y] = st.flagA[st.S + y] = 0;
+    st.flagB[y] = st.flagB[st.S + y] = 0;
+}
+
+// Breakdown restart on this block's chunk (src/bicgstab.hpp:170-179, :224-234):
+// x = q = p = 0, r = b, r_hat = 6.8 b + 0.6; partial r_hat.r for the next rho.
+template <typename Op>
+__device__ __forceinline__ void bicg_restart_chunk(const Op& op, const BicgVecs<double>& v,
+                                                   const BicgState& st, int y, int par,
+                                                   double (*sm)[NWARP]) {
+    const size_t o = (size_t)y * v.Np;
+    double* x = op.x_of(y);
+    double acc[1] = {0};
+    BTE_CELL_LOOP(c) {
+        // Padded cells get r_hat = 0.6 but keep r = p = q = 0, so they add
+        // nothing to any dot product.
+        double bb = v.b[o + c];
+        double rh = bb * 6.8 + 0.6;
+        x[c] = 0.0; v.q[o + c] = 0.0; v.p[o + c] = 0.0; v.r[o + c] = bb;
+        v.rw[o + c] = rh;
+        acc[0] = fma(rh, bb, acc[0]);
+    }
+    block_sum<1>(acc, sm);
+    if (threadIdx.x == 0) st.P(par ? PK_RWR1 : PK_RWR0, y)[blockIdx.x] = acc[0];
+}
+
+// K1 (iteration i): convergence bookkeeping, rho, beta; p = r + beta (p - omega q); ph = M p.
+template <typename Op>
+__global__ void __launch_bounds__(THREADS) k_bicg_p(Op op, BicgVecs<double> v, BicgState st, int i) {
+    __shared__ double sm[2][NWARP];
+    const int y = blockIdx.y;
+    if (st.done[y]) return;
+    const int par = i & 1, pp = par ^ 1;
+    const bool lead = blockIdx.x == 0 && threadIdx.x == 0;
+    double nr;
+    if (i > 1 && !(st.flagA[pp * st.S + y] | st.flagB[pp * st.S + y])) {
+        nr = sqrt(sum_parts(st.P(pp ? PK_RR1 : PK_RR0, y), st.nchunk));
+        if (nr / st.nrm0[y] < st.tol) {  // src/bicgstab.hpp:295
+            if (lead) { st.done[y] = 1; st.iters[y] = i - 1; }
+            return;
+        }
+        if (lead) st.nrmr[y] = nr;
+    } else {
+        nr = st.nrmr[y];
+    }
+    if (i > st.maxit) {
+        if (lead) { st.done[y] = 3; st.iters[y] = st.maxit; }
+        return;
+    }
+    if (nr < 1e-50) {  // src/bicgstab.hpp:166
+        if (lead) { st.done[y] = 2; st.iters[y] = i - 1; }
+        return;
+    }
+    if (lead) atomicAdd(&st.active[i], 1);
+    const double rho_new = sum_parts(st.P(pp ? PK_RWR1 : PK_RWR0, y), st.nchunk);
+    if (rho_new < 1e-200 && rho_new > -1e-200) {
+        if (lead) {
+            st.rho[par * st.S + y] = 1.0; st.alpha[y] = 1.0; st.omega[y] = 1.0;
+            st.flagA[par * st.S + y] = 1; st.flagB[par * st.S + y] = 0;
+        }
+        bicg_restart_chunk(op, v, st, y, par, sm);
+        return;
+    }
+    const double beta = (rho_new / st.rho[pp * st.S + y]) * (st.alpha[y] / st.omega[y]);
+    const double om = st.omega[y];
+    if (lead) {
+        st.rho[par * st.S + y] = rho_new;
+        st.flagA[par * st.S + y] = 0; st.flagB[par * st.S + y] = 0;
+    }
+    const size_t o = (size_t)y * v.Np;
+    BTE_CELL_LOOP(c) {
+        // cublasDaxpy(-omega, q, p); cublasDscal(beta, p); cublasDaxpy(1, r, p)
+        double pv = fma(-om, v.q[o + c], v.p[o + c]);
+        pv = fma(beta, pv, v.r[o + c]);
+        v.p[o + c] = pv;
+        v.ph[o + c] = v.invD[o + c] * pv;
+    }
+}
+
+// K2: q = A ph; partial r_hat . q
+template <typename Op>
+__global__ void __launch_bounds__(THREADS) k_bicg_spmv1(Op op, BicgVecs<double> v, BicgState st, int i) {
+    __shared__ double sm[1][NWARP];
+    const int y = blockIdx.y;
+    const int par = i & 1;
+    if (st.done[y] | st.flagA[par * st.S + y]) return;
+    const size_t o = (size_t)y * v.Np;
+    const double* ph = v.ph + o;
+    double acc[1] = {0};
+    BTE_CELL_LOOP(c) {
+        double qv = op.template apply<double>(y, c, ph);
+        v.q[o + c] = qv;
+        acc[0] = fma(v.rw[o + c], qv, acc[0]);
+    }
+    block_sum<1>(acc, sm);
+    if (threadIdx.x == 0) st.P(PK_RWQ, y)[blockIdx.x] = acc[0];
+}
+
+// K3: alpha; s = r - alpha q (in place in r); z = M s
+template <typename Op>
+__global__ void __launch_bounds__(THREADS) k_bicg_s(Op op, BicgVecs<double> v, BicgState st, int i) {
+    __shared__ double sm[1][NWARP];
+    const int y = blockIdx.y;
+    const int par = i & 1;
+    if (st.done[y] | st.flagA[par * st.S + y]) return;
+    const bool lead = blockIdx.x == 0 && threadIdx.x == 0;
+    const double temp = sum_parts(st.P(PK_RWQ, y), st.nchunk);
+    if (temp < 1e-200 && temp > -1e-200) {
+        if (lead) {
+            st.rho[par * st.S + y] = 1.0; st.alpha[y] = 1.0; st.omega[y] = 1.0;
+            st.flagB[par * st.S + y] = 1;
+        }
+        bicg_restart_chunk(op, v, st, y, par, sm);
+        return;
+    }
+    const double alpha = st.rho[par * st.S + y] / temp;
+    if (lead) st.alpha[y] = alpha;
+    const size_t o = (size_t)y * v.Np;
+    BTE_CELL_LOOP(c) {
+        double s = fma(-alpha, v.q[o + c], v.r[o + c]);
+        v.r[o + c] = s;
+        v.z[o + c] = v.invD[o + c] * s;
+    }
+}
+
+// K4: t = A z; partials t.s, t.t
+template <typename Op>
+__global__ void __launch_bounds__(THREADS) k_bicg_spmv2(Op op, BicgVecs<double> v, BicgState st, int i) {
+    __shared__ double sm[2][NWARP];
+    const int y = blockIdx.y;
+    const int par = i & 1;
+    if (st.done[y] | st.flagA[par * st.S + y] | st.flagB[par * st.S + y]) return;
+    const size_t o = (size_t)y * v.Np;
+    const double* z = v.z + o;
+    double acc[2] = {0, 0};
+    BTE_CELL_LOOP(c) {
+        double tv = op.template apply<double>(y, c, z);
+        v.t[o + c] = tv;
+        acc[0] = fma(tv, v.r[o + c], acc[0]);
+        acc[1] = fma(tv, tv, acc[1]);
+    }
+    block_sum<2>(acc, sm);
+    if (threadIdx.x == 0) {
+        st.P(PK_TS, y)[blockIdx.x] = acc[0];
+        st.P(PK_TT, y)[blockIdx.x] = acc[1];
+    }
+}
+
+// K5: omega; x += alpha ph; x += omega z; r = s - omega t; partials r.r, r_hat.r
+template <typename Op>
+__global__ void __launch_bounds__(THREADS) k_bicg_x(Op op, BicgVecs<double> v, BicgState st, int i) {
+    __shared__ double sm[2][NWARP];
+    const int y = blockIdx.y;
+    const int par = i & 1;
+    if (st.done[y] | st.flagA[par * st.S + y] | st.flagB[par * st.S + y]) return;
+    const bool lead = blockIdx.x == 0 && threadIdx.x == 0;
+    const double omega = sum_parts(st.P(PK_TS, y), st.nchunk) / sum_parts(st.P(PK_TT, y), st.nchunk);
+    const double alpha = st.alpha[y];
+    if (lead) st.omega[y] = omega;
+    const size_t o = (size_t)y * v.Np;
+    double* x = op.x_of(y);
+    double acc[2] = {0, 0};
+    BTE_CELL_LOOP(c) {
+        double xv = fma(alpha, v.ph[o + c], x[c]);
+        xv = fma(omega, v.z[o + c], xv);
+        x[c] = xv;
+        double r = fma(-omega, v.t[o + c], v.r[o + c]);
+        v.r[o + c] = r;
+        acc[0] = fma(r, r, acc[0]);
+        acc[1] = fma(v.rw[o + c], r, acc[1]);
+    }
+    block_sum<2>(acc, sm);
+    if (threadIdx.x == 0) {
+        st.P(par ? PK_RR1 : PK_RR0, y)[blockIdx.x] = acc[0];
+        st.P(par ? PK_RWR1 : PK_RWR0, y)[blockIdx.x] = acc[1];
+    }
+}
+
+}  // namespace bte

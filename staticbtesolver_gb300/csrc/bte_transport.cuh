@@ -1,0 +1,205 @@
+// bte_transport.cuh -- assembly, boundary conditions, reductions and heat flux.
+#pragma once
+#include "bte_kernels.cuh"
+
+namespace bte {
+
+// Per-direction, band-independent geometry of the upwind operator (the parts of
+// _get_Ke, src/StaticBTESolver.cpp:122-160, that do not depend on the band):
+//   dg[d][c]    = sum over faces with s_d.n >= 0 of A_cf g_dcf
+//   fc[d][f][c] = A_cf g_dcf on faces with s_d.n < 0 and a neighbour, else 0
+//   vo[d][c]    = V_c Omega_d (1D: V_c)
+// g = S_d.n (s_d.n on 1D meshes).  One launch per solve set-up.
+__global__ void k_direction_geometry(const double* __restrict__ normal,  // [n][F][3]
+                                     const double* __restrict__ area,    // [n][F]
+                                     const int* __restrict__ nbr,        // [n][F]
+                                     const double* __restrict__ volume,  // [n]
+                                     const double* __restrict__ s, const double* __restrict__ S,
+                                     const double* __restrict__ omega, int n, int F, int dim,
+                                     size_t Np, double* dg, double* vo, double* fc) {
+    const int d = blockIdx.y;
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= Np) return;
+    const size_t dc = (size_t)d * Np + c;
+    if (c >= n) {  // padded cell: identity row
+        dg[dc] = 0.0;
+        vo[dc] = 1.0;
+        for (int f = 0; f < F; ++f) fc[((size_t)d * F + f) * Np + c] = 0.0;
+        return;
+    }
+    const double sx = s[3 * d], sy = s[3 * d + 1], sz = s[3 * d + 2];
+    const double Sx = S[3 * d], Sy = S[3 * d + 1], Sz = S[3 * d + 2];
+    double acc = 0.0;
+    for (int f = 0; f < F; ++f) {
+        const double* nn = normal + ((size_t)c * F + f) * 3;
+        const double sn = sx * nn[0] + sy * nn[1] + sz * nn[2];
+        const double g = dim > 1 ? Sx * nn[0] + Sy * nn[1] + Sz * nn[2] : sn;
+        const double ag = area[(size_t)c * F + f] * g;
+        double cf = 0.0;
+        if (sn >= 0) acc += ag;
+        else if (nbr[(size_t)c * F + f] >= 0) cf = ag;
+        fc[((size_t)d * F + f) * Np + c] = cf;
+    }
+    dg[dc] = acc;
+    vo[dc] = dim > 1 ? volume[c] * omega[d] : volume[c];
+}
+
+// Boundary description (host-built): faces whose neighbour code matches a
+// boundary-condition row, sorted by (cell, face).  bptr[c]..bptr[c+1] are the
+// entries of cell c.
+struct Boundary {
+    const int* bptr;      // [Np+1]
+    const int* bf_cell;   // [nbf]
+    const int* bf_kind;   // [nbf] 1, 2, 31, 32, 33
+    const int* bf_bc;     // [nbf] boundary-condition row
+    const int* bf_diff;   // [nbf] row in the diffuse list, or -1
+    const double* cin;    // [n_dir][nbf] A g on inflow directions (s.n < 0), else 0
+    const double* eiso;   // [n_band][n_bc] C_b / Omega_tot (T_bc - T_ref)
+    const int* mirror;    // [3][n_dir] specular partner for 31, 32, 33
+    const double* ediff;  // [n_band][nbf] diffuse wall energy (this outer iteration)
+    int nbf, n_bc;
+};
+
+// Right-hand sides of one batch (_get_Re, src/StaticBTESolver.cpp:162-269):
+//   R[c] = - sum_{inflow boundary faces} e_wall k_b A g + ebar[b][c] V_c Omega_d
+// e_wall: isothermal C_b/Omega_tot (T_bc - T_ref); diffuse: the outgoing
+// energy of the previous iterate averaged over the wall; specular: the previous
+// iterate at the mirrored direction.
+__global__ void __launch_bounds__(THREADS) k_rhs(FaceFluxOp op, Boundary bd, const double* __restrict__ ebar,
+                                                 const double* __restrict__ e_prev, double* rhs, int n) {
+    const int y = blockIdx.y;
+    int b, d;
+    op.bd(y, b, d);
+    const double k = op.kb[b];
+    const size_t o = (size_t)y * op.Np;
+    const double* ep_bd_base = e_prev + (size_t)b * op.n_dir * op.Np;
+    BTE_CELL_LOOP(c) {
+        double r = 0.0;
+        if (c < n) {
+            const int e0 = bd.bptr[c], e1 = bd.bptr[c + 1];
+            for (int e = e0; e < e1; ++e) {
+                const double cf = bd.cin[(size_t)d * bd.nbf + e];
+                if (cf == 0.0) continue;
+                double ew;
+                switch (bd.bf_kind[e]) {
+                    case 1: ew = bd.eiso[(size_t)b * bd.n_bc + bd.bf_bc[e]]; break;
+                    case 2: ew = bd.ediff[(size_t)b * bd.nbf + e]; break;
+                    case 31: ew = ep_bd_base[(size_t)bd.mirror[d] * op.Np + c]; break;
+                    case 32: ew = ep_bd_base[(size_t)bd.mirror[op.n_dir + d] * op.Np + c]; break;
+                    default: ew = ep_bd_base[(size_t)bd.mirror[2 * op.n_dir + d] * op.Np + c]; break;
+                }
+                r -= ew * (k * cf);
+            }
+            r += ebar[(size_t)b * op.Np + c] * op.vo[(size_t)d * op.Np + c];
+        }
+        rhs[o + c] = r;
+    }
+}
+
+// Diffuse wall energy per (band, diffuse face) from the previous iterate
+// (src/StaticBTESolver.cpp:180-204): sum over outgoing directions of
+// e w / sum w, w = (S.n) Omega in 3D, S.n in 2D; 1D: sum e (s.n) Omega / pi.
+__global__ void k_diffuse_wall(const double* __restrict__ e_prev, const int* __restrict__ dlist,  // [ndiff] -> bf
+                               const int* __restrict__ bf_cell, const double* __restrict__ wdiff,  // [ndiff][n_dir]
+                               const double* __restrict__ wden,  // [ndiff]
+                               int ndiff, int n_band, int n_dir, size_t Np, int nbf, double* ediff) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ndiff * n_band) return;
+    const int b = t / ndiff, k = t % ndiff;
+    const int e = dlist[k];
+    const int c = bf_cell[e];
+    const double* ep = e_prev + (size_t)b * n_dir * Np + c;
+    const double* w = wdiff + (size_t)k * n_dir;
+    double acc = 0.0;
+    for (int d = 0; d < n_dir; ++d)
+        if (w[d] != 0.0) acc += ep[(size_t)d * Np] * w[d];
+    ediff[(size_t)b * nbf + e] = acc / wden[k];
+}
+
+// The reductions that close an outer iteration, fused in one pass over
+// e_curr and e_prev (src/StaticBTESolver.cpp:96-120 and :311-321):
+//   Tb[b][c] = sum_d e Omega_d / C_b + T_ref
+//   T[c]     = sum_b Lr_b Tb[b][c] / sum_b Lr_b
+//   ebar[b][c] = C_b / Omega_tot (T[c] - T_ref)
+//   margin partial = sum_{b,d} (e_curr - e_prev)^2 over this block's cells
+__global__ void __launch_bounds__(THREADS) k_reduce(const double* __restrict__ e_curr, const double* __restrict__ e_prev,
+                                                    const double* __restrict__ omega, const double* __restrict__ Cb,
+                                                    const double* __restrict__ Lr, double Lr_sum, double T_ref,
+                                                    double solid_angle, int n, int n_band, int n_dir, size_t Np,
+                                                    double* Tb, double* T, double* ebar, double* part) {
+    __shared__ double sm[1][NWARP];
+    const int c = blockIdx.x * THREADS + threadIdx.x;
+    double m[1] = {0.0};
+    if (c < n) {
+        double tacc = 0.0;
+        for (int b = 0; b < n_band; ++b) {
+            const double* ec = e_curr + (size_t)b * n_dir * Np + c;
+            const double* ep = e_prev + (size_t)b * n_dir * Np + c;
+            double e0 = 0.0;
+            for (int d = 0; d < n_dir; ++d) {
+                const double a = ec[(size_t)d * Np], p = ep[(size_t)d * Np];
+                e0 += a * omega[d];
+                const double df = a - p;
+                m[0] = fma(df, df, m[0]);
+            }
+            const double tb = e0 / Cb[b] + T_ref;
+            Tb[(size_t)b * Np + c] = tb;
+            tacc += Lr[b] * tb;
+        }
+        const double Tc = tacc / Lr_sum;
+        T[c] = Tc;
+        for (int b = 0; b < n_band; ++b) ebar[(size_t)b * Np + c] = Cb[b] / solid_angle * (Tc - T_ref);
+    }
+    block_sum<1>(m, sm);
+    if (threadIdx.x == 0) part[blockIdx.x] = m[0];
+}
+
+// margin = sum of partials / (n_band n_cell), in block order.
+__global__ void k_margin_final(const double* part, int nparts, double denom, double* out) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double s = 0.0;
+    for (int i = 0; i < nparts; ++i) s += part[i];
+    out[0] = s / denom;
+}
+
+// Heat flux, step 1 (src/StaticBTESolver.cpp:331-354): per (band, boundary face),
+// sum over all directions of e * hw[face][d], hw = (s.n) A Omega (DM 3 on a 3D
+// mesh), (S.n) A (other 2D/3D), (s.n) Omega (1D).
+__global__ void k_heat_face(const double* __restrict__ e, const int* __restrict__ bf_cell,
+                            const double* __restrict__ hw, int nbf, int n_band, int n_dir, size_t Np,
+                            double* part) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nbf * n_band) return;
+    const int b = t / nbf, k = t % nbf;
+    const double* ep = e + (size_t)b * n_dir * Np + bf_cell[k];
+    const double* w = hw + (size_t)k * n_dir;
+    double acc = 0.0;
+    for (int d = 0; d < n_dir; ++d) acc += ep[(size_t)d * Np] * w[d];
+    part[(size_t)b * nbf + k] = acc;
+}
+
+// Heat flux, step 2 (:357-364): per (boundary condition, band), sum the faces
+// in (cell, face) order, divide by the wall length (not in 1D), times v_g;
+// q[i] = sum over bands.  One block.
+__global__ void k_heat_final(const double* __restrict__ part, const int* __restrict__ bf_bc,
+                             const double* __restrict__ bf_area, const double* __restrict__ vg, int nbf,
+                             int n_band, int n_bc, int dim, double* q_band, double* q) {
+    for (int t = threadIdx.x; t < n_bc * n_band; t += blockDim.x) {
+        const int i = t / n_band, b = t % n_band;
+        double heat = 0.0, length = 0.0;
+        for (int k = 0; k < nbf; ++k) {
+            if (bf_bc[k] != i) continue;
+            heat += part[(size_t)b * nbf + k];
+            length += bf_area[k];
+        }
+        q_band[(size_t)i * n_band + b] = dim != 1 ? heat / length * vg[b] : heat * vg[b];
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < n_bc; i += blockDim.x) {
+        double s = 0.0;
+        for (int b = 0; b < n_band; ++b) s += q_band[(size_t)i * n_band + b];
+        q[i] = s;
+    }
+}
+
+}  // namespace bte

@@ -58,8 +58,10 @@ def parse_args():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="square20k")
-    ap.add_argument("--form", default="plain", choices=["plain", "mixed"])
-    ap.add_argument("--e2e-steps", type=int, default=1)
+    ap.add_argument("--form", default="sweep", choices=["plain", "mixed", "sweep"])
+    ap.add_argument("--plain-iters", type=int, default=3,
+                    help="outer iterations of the plain FP64 BiCGSTAB form timed for the comparison")
+    ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--max-iter", type=int, default=10000)
     return ap.parse_args()
@@ -218,7 +220,7 @@ def run_ours(args, rank, world, local):
     import staticbtesolver_gb300 as S
 
     S.build()
-    form = S.FORM_PLAIN if args.form == "plain" else S.FORM_MIXED
+    form = {"plain": S.FORM_PLAIN, "mixed": S.FORM_MIXED, "sweep": S.FORM_SWEEP}[args.form]
     with tempfile.TemporaryDirectory() as tmp:
         t0 = time.perf_counter()
         p = make_workload(args.workload, tmp)
@@ -269,6 +271,23 @@ def run_ours(args, rank, world, local):
         e2e = max_over_ranks(statistics.mean(e2e_t), world)
         ctx2.close()
 
+        # plain FP64 form (the reference GPU algorithm, batched): a bounded number
+        # of outer iterations, scaled by the outer-iteration count of the solve
+        plain = None
+        if form != S.FORM_PLAIN and args.plain_iters > 0:
+            pkw = dict(solve_kw, form=S.FORM_PLAIN, max_iter=args.plain_iters)
+            ctx.solve(**pkw)  # warm
+            st_p, rep_p = ctx.solve(**pkw)
+            per_outer = rep_p.ms_total / 1e3 / rep_p.n_iter
+            ctx.solve(profile=True, **pkw)
+            pstats = ctx.kernel_stats()
+            plain = {"s_per_outer_iteration": per_outer, "outer_iterations_timed": rep_p.n_iter,
+                     "s_extrapolated": per_outer * last["n_iter"],
+                     "inner_iterations_per_system": rep_p.inner_iterations / max(rep_p.inner_solves, 1),
+                     "kernels": {k: {"launches": v["launches"], "ms": round(v["ms"], 3),
+                                     "GB/s": round(v["bytes"] / (v["ms"] / 1e3) / 1e9, 1) if v["ms"] > 0 else None}
+                                 for k, v in pstats.items() if v["launches"]}}
+
         # profiled solve (outside the timed region) for the per-kernel roofline
         ctx.solve(profile=True, **solve_kw)
         stats = ctx.kernel_stats()
@@ -305,7 +324,9 @@ def run_ours(args, rank, world, local):
                        "ms_reduce": round(last["ms_reduce"], 2), "wall_s_per_step": statistics.mean(wall),
                        "preprocess_s": t_prep, "generate_s": t_gen, "l2": "working set > L2 (2 GB of vectors)",
                        "replicas": world, "q_left": float(q[0]), "q_right": float(q[2]),
-                       "T_min": float(T.min()), "T_max": float(T.max()), "kernels": per_kernel},
+                       "T_min": float(T.min()), "T_max": float(T.max()), "kernels": per_kernel,
+                       "plain_fp64_form": plain,
+                       "speedup_vs_plain_fp64": (plain["s_extrapolated"] / t_step) if plain else None},
             "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": round(achieved, 1), "peak": peak,
                          "peak_source": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),
                          "traffic": traffic,

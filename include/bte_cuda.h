@@ -45,7 +45,14 @@ typedef enum bte_form {
      * b - A x is recomputed after every FP32 cycle and the solve stops when
      * ||b - A x|| <= inner_tol * ||b||, the reference's criterion for x0 = 0.
      * The inner iterate starts from the previous outer iterate. */
-    BTE_FORM_MIXED = 1
+    BTE_FORM_MIXED = 1,
+    /* FP64 upwind sweep: each system is lower triangular in the topological
+     * order of its direction's upwind graph, so one level-scheduled forward
+     * substitution solves it exactly (to rounding).  Edges closing a cycle of
+     * the upwind graph are lagged and Gauss-Seidel sweeps repeat until
+     * ||b - A x|| <= inner_tol ||b|| (at most inner_maxit sweeps).  The level
+     * order is built once per geometry and quadrature. */
+    BTE_FORM_SWEEP = 2
 } bte_form;
 
 typedef struct bte_ctx bte_ctx;

@@ -22,10 +22,11 @@ import numpy as np
 from . import _build
 
 __all__ = ["build", "Problem", "Context", "Options", "Report", "StaticBTESolver", "bicgstab_csr",
-           "FORM_PLAIN", "FORM_MIXED", "BteError", "lib_paths"]
+           "FORM_PLAIN", "FORM_MIXED", "FORM_SWEEP", "BteError", "lib_paths"]
 
 FORM_PLAIN = 0
 FORM_MIXED = 1
+FORM_SWEEP = 2
 
 STATUS = {0: "ok", 1: "invalid argument", 2: "call out of order", 3: "CUDA error", 4: "out of device memory",
           5: "unsupported boundary condition", 6: "not converged", 7: "non-finite value", 8: "no CUDA device"}

@@ -14,6 +14,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/bte_cuda.h"
@@ -51,9 +52,11 @@ struct DevBuf {
 
 constexpr int kGroup = 8;  // BiCGSTAB iterations launched between host checks
 
-enum KernelKind { KK_P, KK_SPMV1, KK_S, KK_SPMV2, KK_X, KK_INIT, KK_RHS, KK_REDUCE, KK_DIFFUSE, KK_HEAT, kNumKinds };
-const char* kKindNames[kNumKinds] = {"bicg_p_update", "bicg_spmv1",   "bicg_s_update", "bicg_spmv2", "bicg_x_update",
-                                     "bicg_init",     "rhs_assembly", "reduce_margin", "diffuse_wall", "heat_flux"};
+enum KernelKind { KK_P, KK_SPMV1, KK_S, KK_SPMV2, KK_X, KK_INIT, KK_RHS, KK_REDUCE, KK_DIFFUSE, KK_HEAT, KK_SWEEP,
+                  KK_SWEEP_RES, kNumKinds };
+const char* kKindNames[kNumKinds] = {"bicg_p_update", "bicg_spmv1",   "bicg_s_update", "bicg_spmv2",
+                                     "bicg_x_update", "bicg_init",    "rhs_assembly",  "reduce_margin",
+                                     "diffuse_wall",  "heat_flux",    "upwind_sweep",  "sweep_residual"};
 
 }  // namespace
 
@@ -94,6 +97,12 @@ struct bte_ctx {
     double* h_pinned = nullptr;  // [4]
     int* h_pinned_i = nullptr;   // [4]
     std::vector<int> h_done, h_iters;
+    // upwind sweep plan (form BTE_FORM_SWEEP)
+    bool plan_ready = false;
+    int plan_lagged_dirs = 0;
+    long long plan_levels = 0;
+    DevBuf p_cell, p_dg, p_vo, p_nb, p_fc, p_lvl, p_lvl_off, p_part, p_bad;
+    int sweep_group = 8, sweep_threads = 512;
     // profiling (opts->profile): events around each launch, resolved after a sync
     bool profile = false;
     std::vector<cudaEvent_t> ev_pool;
@@ -536,7 +545,118 @@ static bte_status setup(bte_ctx* ctx, int batch_systems) {
     BTE_CUDA(ctx->s_part.alloc(sizeof(double) * 7 * S * ctx->nchunk));
     ctx->h_done.resize(S);
     ctx->h_iters.resize(S);
+    ctx->plan_ready = false;
     ctx->dirty = false;
+    return BTE_OK;
+}
+
+// Level order of one direction's upwind graph (Kahn's algorithm in waves).
+// mask[c] bit f: face f of c is an inflow face with a neighbour.  When no cell
+// is free the unprocessed cell with the fewest unresolved inflow edges (lowest
+// index on ties) starts the next level alone and those edges become lagged.
+static void level_order(int n, int F, const uint8_t* mask, const int* nbr, std::vector<int>& perm,
+                        std::vector<int>& lvl, std::vector<int>& lagged /* [F][n] */) {
+    std::vector<int> indeg(n), dptr(n + 1, 0), down;
+    for (int c = 0; c < n; ++c) {
+        int k = 0;
+        for (int f = 0; f < F; ++f)
+            if (mask[c] >> f & 1) { ++k; ++dptr[nbr[(size_t)c * F + f] + 1]; }
+        indeg[c] = k;
+    }
+    for (int c = 0; c < n; ++c) dptr[c + 1] += dptr[c];
+    down.resize(dptr[n]);
+    std::vector<int> fill(dptr.begin(), dptr.end() - 1);
+    for (int c = 0; c < n; ++c)
+        for (int f = 0; f < F; ++f)
+            if (mask[c] >> f & 1) down[fill[nbr[(size_t)c * F + f]]++] = c;
+    std::vector<char> done(n, 0);
+    std::vector<int> wave, next;
+    for (int c = 0; c < n; ++c)
+        if (indeg[c] == 0) wave.push_back(c);
+    perm.clear();
+    lvl.clear();
+    lagged.assign((size_t)F * n, 0);
+    int processed = 0;
+    while (processed < n) {
+        if (wave.empty()) {
+            int best = -1;
+            for (int c = 0; c < n; ++c)
+                if (!done[c] && (best < 0 || indeg[c] < indeg[best])) best = c;
+            for (int f = 0; f < F; ++f)
+                if ((mask[best] >> f & 1) && !done[nbr[(size_t)best * F + f]]) lagged[(size_t)f * n + best] = 1;
+            wave.push_back(best);
+        }
+        std::sort(wave.begin(), wave.end());
+        lvl.push_back((int)perm.size());
+        for (int c : wave) { done[c] = 1; perm.push_back(c); }
+        processed += (int)wave.size();
+        next.clear();
+        for (int c : wave)
+            for (int k = dptr[c]; k < dptr[c + 1]; ++k) {
+                const int c2 = down[k];
+                if (done[c2]) continue;
+                if (--indeg[c2] == 0) next.push_back(c2);
+            }
+        wave.swap(next);
+    }
+    lvl.push_back(n);
+}
+
+// Build the sweep plan for every direction from the device's inflow coefficients.
+static bte_status build_sweep_plan(bte_ctx* ctx) {
+    const int n = ctx->n, F = ctx->F, ND = ctx->n_dir;
+    const size_t Np = ctx->Np;
+    cudaStream_t st = ctx->stream;
+    DevBuf d_mask;
+    BTE_CUDA(d_mask.alloc((size_t)ND * n));
+    bte::k_inflow_mask<<<dim3((n + 255) / 256, ND), 256, 0, st>>>(ctx->d_fc.as<double>(), F, n, Np, ND,
+                                                                  d_mask.as<uint8_t>());
+    BTE_LAUNCHED();
+    std::vector<uint8_t> mask((size_t)ND * n);
+    BTE_CUDA(cudaMemcpyAsync(mask.data(), d_mask.p, mask.size(), cudaMemcpyDeviceToHost, st));
+    BTE_CUDA(cudaStreamSynchronize(st));
+    std::vector<std::vector<int>> perm(ND), lvl(ND), lag(ND);
+    const int nth = std::max(1, std::min<int>(ND, (int)std::thread::hardware_concurrency()));
+    std::vector<std::thread> pool;
+    for (int t = 0; t < nth; ++t)
+        pool.emplace_back([&, t]() {
+            for (int d = t; d < ND; d += nth)
+                level_order(n, F, &mask[(size_t)d * n], ctx->nbr.data(), perm[d], lvl[d], lag[d]);
+        });
+    for (auto& th : pool) th.join();
+    std::vector<int> h_perm((size_t)ND * n), h_lag((size_t)ND * F * n), h_lvl, h_off(ND + 1, 0);
+    int lagged_dirs = 0;
+    long long levels = 0;
+    for (int d = 0; d < ND; ++d) {
+        std::copy(perm[d].begin(), perm[d].end(), h_perm.begin() + (size_t)d * n);
+        std::copy(lag[d].begin(), lag[d].end(), h_lag.begin() + (size_t)d * F * n);
+        h_off[d] = (int)h_lvl.size();
+        h_lvl.insert(h_lvl.end(), lvl[d].begin(), lvl[d].end());
+        levels += (long long)lvl[d].size() - 1;
+        bool any = false;
+        for (int v : lag[d]) any |= v != 0;
+        lagged_dirs += any;
+    }
+    h_off[ND] = (int)h_lvl.size();
+    DevBuf d_perm, d_lag;
+    BTE_CUDA(upload(d_perm, h_perm, st));
+    BTE_CUDA(upload(d_lag, h_lag, st));
+    BTE_CUDA(upload(ctx->p_lvl, h_lvl, st));
+    BTE_CUDA(upload(ctx->p_lvl_off, h_off, st));
+    BTE_CUDA(ctx->p_cell.alloc(sizeof(int) * ND * n));
+    BTE_CUDA(ctx->p_dg.alloc(sizeof(double) * ND * n));
+    BTE_CUDA(ctx->p_vo.alloc(sizeof(double) * ND * n));
+    BTE_CUDA(ctx->p_nb.alloc(sizeof(int) * ND * F * n));
+    BTE_CUDA(ctx->p_fc.alloc(sizeof(double) * ND * F * n));
+    bte::k_sweep_layout<<<dim3((n + 255) / 256, ND), 256, 0, st>>>(
+        d_perm.as<int>(), d_lag.as<int>(), ctx->d_dg.as<double>(), ctx->d_vo.as<double>(), ctx->d_fc.as<double>(),
+        ctx->d_nbr.as<int>(), F, n, Np, ND, ctx->p_cell.as<int>(), ctx->p_dg.as<double>(), ctx->p_vo.as<double>(),
+        ctx->p_nb.as<int>(), ctx->p_fc.as<double>());
+    BTE_LAUNCHED();
+    BTE_CUDA(cudaStreamSynchronize(st));  // d_perm / d_lag go out of scope
+    ctx->plan_lagged_dirs = lagged_dirs;
+    ctx->plan_levels = levels;
+    ctx->plan_ready = true;
     return BTE_OK;
 }
 
@@ -621,6 +741,65 @@ static bte_status solve_batch_plain(bte_ctx* ctx, int b0, int nbb, const bte_opt
     return BTE_OK;
 }
 
+// Solve all systems of one batch by upwind sweeps (exact in one sweep when no
+// edge is lagged; otherwise Gauss-Seidel sweeps until ||R - A x|| <= inner_tol ||R||).
+static bte_status solve_batch_sweep(bte_ctx* ctx, int b0, int nbb, const bte_options& o, bte_report& rep) {
+    cudaStream_t st = ctx->stream;
+    const int S = nbb * ctx->n_dir;
+    const double N = ctx->n, w = sizeof(double);
+    bte::FaceFluxOp op{ctx->d_dg.as<double>(), ctx->d_vo.as<double>(), ctx->d_fc.as<double>(),
+                       ctx->d_nb.as<int>(), ctx->d_kb.as<double>(), ctx->e_curr, ctx->F, nbb, b0,
+                       ctx->n_dir, ctx->Np};
+    bte::Boundary bd{ctx->d_bptr.as<int>(), ctx->d_bf_cell.as<int>(), ctx->d_bf_kind.as<int>(),
+                     ctx->d_bf_bc.as<int>(), ctx->d_bf_diff.as<int>(), ctx->d_cin.as<double>(),
+                     ctx->d_eiso.as<double>(), ctx->d_mirror.as<int>(), ctx->d_ediff.as<double>(),
+                     ctx->nbf, std::max(ctx->n_bc, 1)};
+    const double geo = N * ((ctx->F + 2) * w + ctx->F * 4.0) * ctx->n_dir;
+    dim3 grid(ctx->nchunk, S);
+    BTE_LAUNCH(KK_RHS, -1, S * N * 2 * w + geo / 2, 0,
+               bte::k_rhs<<<grid, bte::THREADS, 0, st>>>(op, bd, ctx->d_ebar.as<double>(), ctx->e_prev,
+                                                         ctx->w_b.as<double>(), ctx->n));
+    bte::SweepPlan sp{ctx->p_cell.as<int>(), ctx->p_dg.as<double>(), ctx->p_vo.as<double>(), ctx->p_nb.as<int>(),
+                      ctx->p_fc.as<double>(), ctx->p_lvl.as<int>(), ctx->p_lvl_off.as<int>(), ctx->n, ctx->F};
+    const int G = std::max(1, std::min(ctx->sweep_group, nbb));
+    dim3 sgrid((nbb + G - 1) / G, ctx->n_dir);
+    // algorithmic bytes of a sweep: rhs read + x write per system, level-ordered
+    // geometry per direction, one upstream gather per inflow face
+    const double sweep_bytes = S * N * (2 * w + 1.5 * w) + geo;
+    int sweeps = 0;
+    for (;;) {
+        BTE_LAUNCH(KK_SWEEP, -1, sweep_bytes, 0,
+                   bte::k_sweep<<<sgrid, ctx->sweep_threads, 0, st>>>(sp, ctx->d_kb.as<double>(), ctx->w_b.as<double>(),
+                                                                     ctx->e_curr, ctx->e_prev, sweeps == 0, G, nbb, b0,
+                                                                     ctx->n_dir, ctx->Np));
+        ++sweeps;
+        if (ctx->plan_lagged_dirs == 0) break;
+        BTE_CUDA(ctx->p_part.alloc(sizeof(double) * 2 * (size_t)S * ctx->nchunk));
+        BTE_CUDA(ctx->p_bad.alloc(sizeof(int)));
+        BTE_CUDA(cudaMemsetAsync(ctx->p_bad.p, 0, sizeof(int), st));
+        BTE_LAUNCH(KK_SWEEP_RES, -1, S * N * 2 * w + geo, 0,
+                   bte::k_sweep_residual<<<grid, bte::THREADS, 0, st>>>(op, ctx->w_b.as<double>(),
+                                                                        ctx->p_part.as<double>(), ctx->nchunk));
+        bte::k_sweep_check<<<(S + 127) / 128, 128, 0, st>>>(ctx->p_part.as<double>(), S, ctx->nchunk, o.inner_tol,
+                                                             ctx->p_bad.as<int>());
+        BTE_LAUNCHED();
+        BTE_CUDA(cudaMemcpyAsync(ctx->h_pinned_i, ctx->p_bad.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+        BTE_CUDA(cudaStreamSynchronize(st));
+        if (ctx->h_pinned_i[0] == 0) break;
+        if (sweeps >= o.inner_maxit) {
+            rep.inner_unconverged += ctx->h_pinned_i[0];
+            break;
+        }
+    }
+    if (ctx->profile) {
+        BTE_CUDA(cudaStreamSynchronize(st));
+        prof_resolve(ctx, nullptr, 0);
+    }
+    rep.inner_iterations += (long long)S * sweeps;
+    rep.inner_solves += S;
+    return BTE_OK;
+}
+
 extern "C" bte_status bte_solve(bte_ctx* ctx, const bte_options* opts, bte_report* report) {
     if (!ctx) return BTE_ERR_INVALID_ARGUMENT;
     if (!(ctx->has_geom && ctx->has_quad && ctx->has_bands && ctx->has_bcs))
@@ -630,7 +809,7 @@ extern "C" bte_status bte_solve(bte_ctx* ctx, const bte_options* opts, bte_repor
     else bte_default_options(&o);
     if (o.max_iter < 0 || o.inner_maxit <= 0 || !(o.inner_tol > 0))
         return fail(ctx, BTE_ERR_INVALID_ARGUMENT, "bte_solve: bad options");
-    if (o.form != BTE_FORM_PLAIN)
+    if (o.form != BTE_FORM_PLAIN && o.form != BTE_FORM_SWEEP)
         return fail(ctx, BTE_ERR_INVALID_ARGUMENT, "bte_solve: form not available in this build");
     if (ctx->dim == 1 && ctx->F != 2) return fail(ctx, BTE_ERR_INVALID_ARGUMENT, "1D mesh needs 2 faces");
     BTE_CUDA(cudaSetDevice(ctx->device));
@@ -646,6 +825,10 @@ extern "C" bte_status bte_solve(bte_ctx* ctx, const bte_options* opts, bte_repor
     }
     if (ctx->dirty) {
         bte_status s = setup(ctx, o.batch_systems);
+        if (s != BTE_OK) return s;
+    }
+    if (o.form == BTE_FORM_SWEEP && !ctx->plan_ready) {
+        bte_status s = build_sweep_plan(ctx);
         if (s != BTE_OK) return s;
     }
     cudaStream_t st = ctx->stream;
@@ -676,7 +859,8 @@ extern "C" bte_status bte_solve(bte_ctx* ctx, const bte_options* opts, bte_repor
         BTE_CUDA(cudaEventRecord(ev[1], st));
         for (int b0 = 0; b0 < NB; b0 += ctx->nbb) {
             const int nbb = std::min(ctx->nbb, NB - b0);
-            bte_status s = solve_batch_plain(ctx, b0, nbb, o, rep);
+            bte_status s = o.form == BTE_FORM_SWEEP ? solve_batch_sweep(ctx, b0, nbb, o, rep)
+                                                    : solve_batch_plain(ctx, b0, nbb, o, rep);
             if (s != BTE_OK) return s;
         }
         BTE_CUDA(cudaEventRecord(ev[2], st));

@@ -203,3 +203,144 @@ __global__ void k_heat_final(const double* __restrict__ part, const int* __restr
 }
 
 }  // namespace bte
+
+namespace bte {
+
+// ---------------------------------------------------------------------------
+// Upwind sweep: for direction d the system couples a cell only to its inflow
+// neighbours, so in topological ("level") order of the upwind graph it is
+// lower triangular and one forward substitution solves it exactly:
+//   x[c] = (R[c] - k_b sum_{inflow f} fc[d][f][c] x[nb]) / (k_b dg[d][c] + vo[d][c]).
+// Cells of one level depend only on earlier levels.  Edges that close a cycle
+// of the upwind graph (none on Delaunay triangulations) are "lagged": their
+// upstream cell sits on a later level, so the substitution reads its previous
+// value (a Gauss-Seidel sweep) and the host repeats sweeps until the
+// residual test passes.
+//
+// Sweep-ordered arrays, direction-major, position j in level order:
+//   sw_cell[d][j], sw_dg[d][j], sw_vo[d][j], sw_nb[d][f][j] (upstream cell,
+//   -1 none, -2-cell for a lagged edge), sw_fc[d][f][j]; levels
+//   lvl[lvl_off[d] .. lvl_off[d+1]] are start positions (the last entry is n).
+struct SweepPlan {
+    const int* cell;
+    const double* dg;
+    const double* vo;
+    const int* nb;
+    const double* fc;
+    const int* lvl;
+    const int* lvl_off;
+    int n, F;
+};
+
+// One block sweeps direction blockIdx.y for bands b0 + blockIdx.x * G .. + G - 1.
+// rhs is batch-local ([batch row y][Np], y = d * nbb + (b - b0)); x and x_old are
+// e_curr / e_prev ([band][n_dir][Np]).
+__global__ void __launch_bounds__(512) k_sweep(SweepPlan sp, const double* __restrict__ kb, const double* __restrict__ rhs,
+                                               double* x, const double* __restrict__ x_old, int first_sweep,
+                                               int G, int nbb, int b0, int n_dir, size_t Np) {
+    const int d = blockIdx.y;
+    const int g0 = blockIdx.x * G;
+    const int gn = min(G, nbb - g0);
+    if (gn <= 0) return;
+    const int L0 = sp.lvl_off[d], L1 = sp.lvl_off[d + 1];
+    const size_t pd = (size_t)d * sp.n;
+    for (int l = L0; l < L1 - 1; ++l) {
+        const int j0 = sp.lvl[l], j1 = sp.lvl[l + 1];
+        const int items = (j1 - j0) * gn;
+        for (int it = threadIdx.x; it < items; it += blockDim.x) {
+            const int j = j0 + it / gn;
+            const int bl = g0 + it % gn;  // band within the batch
+            const int b = b0 + bl;
+            const size_t pj = pd + j;
+            const int c = sp.cell[pj];
+            const double k = kb[b];
+            double* xb = x + ((size_t)b * n_dir + d) * Np;
+            const double* xo = x_old + ((size_t)b * n_dir + d) * Np;
+            double off = 0.0;
+            for (int f = 0; f < sp.F; ++f) {
+                const int u = sp.nb[((size_t)d * sp.F + f) * sp.n + j];
+                if (u == -1) continue;
+                const double cf = sp.fc[((size_t)d * sp.F + f) * sp.n + j];
+                const double xu = u >= 0 ? xb[u] : (first_sweep ? xo[-u - 2] : xb[-u - 2]);
+                off = fma(cf, xu, off);
+            }
+            const double D = fma(k, sp.dg[pj], sp.vo[pj]);
+            xb[c] = (rhs[((size_t)d * nbb + bl) * Np + c] - k * off) / D;
+        }
+        __syncthreads();
+    }
+}
+
+// Residual test of the sweep solution for batch rows (directions with lagged
+// edges only): partials of ||R - A x||^2 and ||R||^2 per (row, chunk).
+__global__ void __launch_bounds__(THREADS) k_sweep_residual(FaceFluxOp op, const double* __restrict__ rhs,
+                                                            double* part, int nchunk) {
+    __shared__ double sm[2][NWARP];
+    const int y = blockIdx.y;
+    const size_t o = (size_t)y * op.Np;
+    const double* xs = op.x_of(y);
+    double acc[2] = {0, 0};
+    BTE_CELL_LOOP(c) {
+        const double r = rhs[o + c] - op.template apply<double>(y, c, xs);
+        acc[0] = fma(r, r, acc[0]);
+        acc[1] = fma(rhs[o + c], rhs[o + c], acc[1]);
+    }
+    block_sum<2>(acc, sm);
+    if (threadIdx.x == 0) {
+        part[((size_t)y * nchunk + blockIdx.x) * 2] = acc[0];
+        part[((size_t)y * nchunk + blockIdx.x) * 2 + 1] = acc[1];
+    }
+}
+
+// Count rows whose residual still fails ||R - A x|| <= tol ||R||.
+__global__ void k_sweep_check(const double* part, int S, int nchunk, double tol, int* n_bad) {
+    const int y = blockIdx.x * blockDim.x + threadIdx.x;
+    if (y >= S) return;
+    double rr = 0, bb = 0;
+    for (int i = 0; i < nchunk; ++i) {
+        rr += part[((size_t)y * nchunk + i) * 2];
+        bb += part[((size_t)y * nchunk + i) * 2 + 1];
+    }
+    if (!(rr <= tol * tol * bb)) atomicAdd(n_bad, 1);
+}
+
+// Inflow-face bit mask per (direction, cell) from the device's own
+// coefficients, so the host builds the level order from exactly the couplings
+// the kernels use.
+__global__ void k_inflow_mask(const double* __restrict__ fc, int F, int n, size_t Np, int n_dir, uint8_t* mask) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    const int d = blockIdx.y;
+    if (c >= n) return;
+    uint8_t m = 0;
+    for (int f = 0; f < F; ++f)
+        if (fc[((size_t)d * F + f) * Np + c] != 0.0) m |= (uint8_t)(1u << f);
+    mask[(size_t)d * n + c] = m;
+}
+
+// Gather the per-direction geometry into level order.
+__global__ void k_sweep_layout(const int* __restrict__ perm, const int* __restrict__ lagged,  // [n_dir][F][n] 0/1
+                               const double* __restrict__ dg, const double* __restrict__ vo,
+                               const double* __restrict__ fc, const int* __restrict__ nbr,  // nbr [n][F]
+                               int F, int n, size_t Np, int n_dir, int* cell, double* sdg, double* svo, int* snb,
+                               double* sfc) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int d = blockIdx.y;
+    if (j >= n) return;
+    const size_t pj = (size_t)d * n + j;
+    const int c = perm[pj];
+    cell[pj] = c;
+    sdg[pj] = dg[(size_t)d * Np + c];
+    svo[pj] = vo[(size_t)d * Np + c];
+    for (int f = 0; f < F; ++f) {
+        const double v = fc[((size_t)d * F + f) * Np + c];
+        const size_t q = ((size_t)d * F + f) * n + j;
+        sfc[q] = v;
+        if (v == 0.0) snb[q] = -1;
+        else {
+            const int u = nbr[(size_t)c * F + f];
+            snb[q] = lagged[((size_t)d * F + f) * n + c] ? -2 - u : u;
+        }
+    }
+}
+
+}  // namespace bte

@@ -1,7 +1,7 @@
 // BTEMain.cpp -- BTEcmd: the reference's command-line tool (src/BTEMain.cpp:22-196)
 // with the same flags (-g -m -b -d -t -p -T -I -x -y -z, long names as there),
 // plus opt-in flags that leave the default behaviour unchanged:
-//   --form plain|mixed   inner-solve form (default plain: FP64 BiCGSTAB as the reference GPU path)
+//   --form plain|mixed|sweep   inner-solve form (default plain: FP64 BiCGSTAB as the reference GPU path)
 //   --tol X              outer margin threshold (default 1e-5)
 //   --inner-tol X        inner relative residual (default 1e-9)
 #include <getopt.h>
@@ -51,7 +51,7 @@ extern "C" int sbte_main(int argc, char** argv) {
             case 'x': L_x = std::stod(optarg); break;
             case 'y': L_y = std::stod(optarg); break;
             case 'z': L_z = std::stod(optarg); break;
-            case 1001: form = std::string(optarg) == "mixed" ? 1 : 0; break;
+            case 1001: form = std::string(optarg) == "mixed" ? 1 : std::string(optarg) == "sweep" ? 2 : 0; break;
             case 1002: tol = std::stod(optarg); break;
             case 1003: inner_tol = std::stod(optarg); break;
             default: std::cerr << "Unknown option " << c << std::endl; return 1;

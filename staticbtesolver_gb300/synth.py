@@ -106,6 +106,12 @@ def _lawson_flip(P: np.ndarray, tris: np.ndarray) -> np.ndarray:
             tri = [b, a, c]
         if _incircle(*P[tri[0]], *P[tri[1]], *P[tri[2]], *P[d]) <= 1e-30:
             continue
+        # flip only a strictly convex quadrilateral (c and d on opposite sides of a-b,
+        # a and b on opposite sides of c-d)
+        def _o(u, v, w):
+            return (P[v, 0] - P[u, 0]) * (P[w, 1] - P[u, 1]) - (P[v, 1] - P[u, 1]) * (P[w, 0] - P[u, 0])
+        if _o(c, d, a) * _o(c, d, b) >= 0 or _o(a, b, c) * _o(a, b, d) >= 0:
+            continue
         # flip a-b to c-d
         for tt in (t0, t1):
             for k in range(3):
@@ -137,8 +143,11 @@ def _morton_order(xy: np.ndarray, bits: int = 16) -> np.ndarray:
     return np.argsort(code, kind="stable")
 
 
-def square_mesh(n: int, jitter: float = 0.3, seed: int = 20261203):
-    """Jittered (n+1)^2 grid on [0,1]^2, Delaunay-triangulated (2 n^2 triangles)."""
+def square_mesh(n: int, jitter: float = 0.3, seed: int = 20261203, delaunay: bool = True):
+    """Jittered (n+1)^2 grid on [0,1]^2, Delaunay-triangulated (2 n^2 triangles).
+
+    delaunay=False keeps the first valid diagonal of every quad instead (a valid
+    triangulation whose upwind graphs may contain cycles)."""
     rng = np.random.default_rng(seed)
     h = 1.0 / n
     ii, jj = np.meshgrid(np.arange(n + 1), np.arange(n + 1), indexing="ij")
@@ -150,13 +159,19 @@ def square_mesh(n: int, jitter: float = 0.3, seed: int = 20261203):
     dy[(jj == 0) | (jj == n)] = 0.0  # bottom/top edge points slide along x only
     P = np.stack([x + dx, y + dy], axis=1)
     pid = lambda i, j: i * (n + 1) + j
+    def orient(u, v, w):
+        return (P[v, 0] - P[u, 0]) * (P[w, 1] - P[u, 1]) - (P[v, 1] - P[u, 1]) * (P[w, 0] - P[u, 0])
+
     tris = []
     for i in range(n):
         for j in range(n):
             a, b, c, d = pid(i, j), pid(i + 1, j), pid(i + 1, j + 1), pid(i, j + 1)
-            tris.append([a, b, c])
-            tris.append([a, c, d])
-    tris = _lawson_flip(P, np.array(tris))
+            # a jittered quad can be non-convex: take the diagonal that keeps both triangles positive
+            if orient(a, b, c) > 0 and orient(a, c, d) > 0:
+                tris += [[a, b, c], [a, c, d]]
+            else:
+                tris += [[a, b, d], [b, c, d]]
+    tris = _lawson_flip(P, np.array(tris)) if delaunay else np.array(tris)
     # canonical form: counter-clockwise, smallest vertex first, Morton order of centroids
     out = []
     for t in tris:
@@ -320,14 +335,15 @@ def make_problem(name: str, out_dir: str, seed: int = 20261203) -> Problem:
                         radius 0.2 (diffuse wall), 128 directions, 40 bands.
       square<N>_b<B>    2D square 1e-7 m with 2 N^2 triangles and B bands (small parity cases).
       cube<N>_b<B>      3D cube 1e-8 m with 6 N^3 tetrahedra and B bands.
+      nondelaunay<N>_b<B>  as square<N>_b<B> without the Delaunay edge flips.
     """
     os.makedirs(out_dir, exist_ok=True)
     geo = os.path.join(out_dir, f"{name}.mphtxt")
     band_file = os.path.join(out_dir, f"{name}.band.dat")
     bc_file = os.path.join(out_dir, f"{name}.bc.dat")
 
-    def square(n, n_band, side, bc_rows=None):
-        write_mphtxt(geo, square_mesh(n, seed=seed))
+    def square(n, n_band, side, bc_rows=None, delaunay=True):
+        write_mphtxt(geo, square_mesh(n, seed=seed, delaunay=delaunay))
         write_band_file(band_file, debye_bands(n_band))
         write_bc_file(bc_file, bc_rows or [(0, 1, 301.0), (1, 2, 300.0), (2, 1, 299.0), (3, 2, 300.0)])
         return Problem(name, geo, band_file, bc_file, 2, 8, 8, 300.0, 1000, side, side, 0.0)
@@ -355,6 +371,9 @@ def make_problem(name: str, out_dir: str, seed: int = 20261203) -> Problem:
         return p
     if name == "cube1m":
         return cube(55, 40, 1e-6, pore=0.2)
+    if name.startswith("nondelaunay") and "_b" in name:
+        n, b = name[len("nondelaunay"):].split("_b")
+        return square(int(n), int(b), 1e-7, delaunay=False)
     if name.startswith("square") and "_b" in name:
         n, b = name[len("square"):].split("_b")
         return square(int(n), int(b), 1e-7)

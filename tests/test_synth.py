@@ -5,8 +5,8 @@ from staticbtesolver_gb300 import synth
 
 
 def test_square_mesh_is_valid_and_deterministic():
-    a = synth.square_mesh(12, seed=7)
-    b = synth.square_mesh(12, seed=7)
+    a = synth.square_mesh(60, seed=7)
+    b = synth.square_mesh(60, seed=7)
     np.testing.assert_array_equal(a["tri"], b["tri"])
     np.testing.assert_array_equal(a["points"], b["points"])
     P, T = a["points"], a["tri"]
@@ -23,7 +23,7 @@ def test_square_mesh_is_valid_and_deterministic():
     bnd = {tuple(sorted(s)) for s in a["seg"]}
     for e, n in edges.items():
         assert n == 2 or (n == 1 and e in bnd)
-    assert len(bnd) == 4 * 12
+    assert len(bnd) == 4 * 60
 
 
 def test_square_mesh_is_delaunay():

@@ -94,6 +94,8 @@ typedef struct bte_report {
     double ms_inner;           /* inner solves */
     double ms_reduce;          /* temperature / margin reductions */
     long long kernel_launches; /* kernels this library launched during the solve */
+    int sweep_group;           /* sweep form: bands per block and threads per block */
+    int sweep_threads;         /* chosen by timing candidate shapes on a plan's first sweep */
 } bte_report;
 
 /* Fill opts with the reference's defaults (max_iter 10000 as BTEcmd's -I default,

@@ -101,8 +101,12 @@ struct bte_ctx {
     bool plan_ready = false;
     int plan_lagged_dirs = 0;
     long long plan_levels = 0;
-    DevBuf p_cell, p_dg, p_vo, p_nb, p_fc, p_lvl, p_lvl_off, p_part, p_bad;
-    int sweep_group = 8, sweep_threads = 512;
+    DevBuf p_cell, p_dg, p_vo, p_nb, p_fc, p_lvl, p_lvl_off, p_part, p_bad, p_invd;
+    // sweep launch shape (bands per block, threads per block) picked by timing
+    // the candidates on the first sweep of a plan
+    int sweep_group = 4, sweep_threads = 256;
+    bool sweep_tuned = false;
+    float sweep_tune_ms[16] = {};
     // profiling (opts->profile): events around each launch, resolved after a sync
     bool profile = false;
     std::vector<cudaEvent_t> ev_pool;
@@ -514,7 +518,7 @@ static bte_status setup(bte_ctx* ctx, int batch_systems) {
     BTE_CUDA(ctx->d_ebar.alloc(sizeof(double) * NB * Np));
     BTE_CUDA(ctx->d_Tb.alloc(sizeof(double) * NB * Np));
     BTE_CUDA(ctx->d_T.alloc(sizeof(double) * Np));
-    BTE_CUDA(ctx->d_mpart.alloc(sizeof(double) * (Np / bte::THREADS + 1)));
+    BTE_CUDA(ctx->d_mpart.alloc(sizeof(double) * NB * (Np / bte::THREADS + 1)));
     BTE_CUDA(ctx->d_margin.alloc(sizeof(double) * 2));
     BTE_CUDA(ctx->d_hpart.alloc(sizeof(double) * NB * std::max(nbf, 1)));
     BTE_CUDA(ctx->d_qband.alloc(sizeof(double) * std::max(ctx->n_bc, 1) * NB));
@@ -653,7 +657,16 @@ static bte_status build_sweep_plan(bte_ctx* ctx) {
         ctx->d_nbr.as<int>(), F, n, Np, ND, ctx->p_cell.as<int>(), ctx->p_dg.as<double>(), ctx->p_vo.as<double>(),
         ctx->p_nb.as<int>(), ctx->p_fc.as<double>());
     BTE_LAUNCHED();
+    BTE_CUDA(ctx->p_invd.alloc(sizeof(double) * ctx->n_band * ND * n));
+    {
+        bte::SweepPlan sp{ctx->p_cell.as<int>(), ctx->p_dg.as<double>(), ctx->p_vo.as<double>(), ctx->p_nb.as<int>(),
+                          ctx->p_fc.as<double>(), ctx->p_lvl.as<int>(), ctx->p_lvl_off.as<int>(), n, F};
+        bte::k_sweep_invd<<<dim3((n + 255) / 256, ND), 256, 0, st>>>(sp, ctx->d_kb.as<double>(), ctx->n_band, ND,
+                                                                     ctx->p_invd.as<double>());
+        BTE_LAUNCHED();
+    }
     BTE_CUDA(cudaStreamSynchronize(st));  // d_perm / d_lag go out of scope
+    ctx->sweep_tuned = false;
     ctx->plan_lagged_dirs = lagged_dirs;
     ctx->plan_levels = levels;
     ctx->plan_ready = true;
@@ -761,17 +774,44 @@ static bte_status solve_batch_sweep(bte_ctx* ctx, int b0, int nbb, const bte_opt
                                                          ctx->w_b.as<double>(), ctx->n));
     bte::SweepPlan sp{ctx->p_cell.as<int>(), ctx->p_dg.as<double>(), ctx->p_vo.as<double>(), ctx->p_nb.as<int>(),
                       ctx->p_fc.as<double>(), ctx->p_lvl.as<int>(), ctx->p_lvl_off.as<int>(), ctx->n, ctx->F};
+    // launch-shape autotuning on the first sweep of this plan (each candidate
+    // computes the same x from the same inputs)
+    if (!ctx->sweep_tuned) {
+        static const int cand[][2] = {{1, 128}, {2, 128}, {2, 256}, {4, 256}, {8, 256}, {8, 512}, {16, 512}};
+        const int ncand = (int)(sizeof(cand) / sizeof(cand[0]));
+        cudaEvent_t e0, e1;
+        BTE_CUDA(cudaEventCreate(&e0));
+        BTE_CUDA(cudaEventCreate(&e1));
+        float best = 1e30f;
+        for (int k = 0; k < ncand; ++k) {
+            const int Gk = std::max(1, std::min(cand[k][0], nbb));
+            BTE_CUDA(cudaEventRecord(e0, st));
+            bte::k_sweep<<<dim3((nbb + Gk - 1) / Gk, ctx->n_dir), cand[k][1], 0, st>>>(
+                sp, ctx->d_kb.as<double>(), ctx->p_invd.as<double>(), ctx->w_b.as<double>(), ctx->e_curr,
+                ctx->e_prev, 1, Gk, nbb, b0, ctx->n_dir, ctx->Np);
+            BTE_LAUNCHED();
+            BTE_CUDA(cudaEventRecord(e1, st));
+            BTE_CUDA(cudaEventSynchronize(e1));
+            float ms = 0;
+            cudaEventElapsedTime(&ms, e0, e1);
+            ctx->sweep_tune_ms[k] = ms;
+            if (ms < best) { best = ms; ctx->sweep_group = cand[k][0]; ctx->sweep_threads = cand[k][1]; }
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        ctx->sweep_tuned = true;
+    }
     const int G = std::max(1, std::min(ctx->sweep_group, nbb));
     dim3 sgrid((nbb + G - 1) / G, ctx->n_dir);
-    // algorithmic bytes of a sweep: rhs read + x write per system, level-ordered
+    // algorithmic bytes of a sweep: rhs gather, 1/D and x per system, level-ordered
     // geometry per direction, one upstream gather per inflow face
-    const double sweep_bytes = S * N * (2 * w + 1.5 * w) + geo;
+    const double sweep_bytes = S * N * (3 * w + 1.5 * w) + geo;
     int sweeps = 0;
     for (;;) {
         BTE_LAUNCH(KK_SWEEP, -1, sweep_bytes, 0,
-                   bte::k_sweep<<<sgrid, ctx->sweep_threads, 0, st>>>(sp, ctx->d_kb.as<double>(), ctx->w_b.as<double>(),
-                                                                     ctx->e_curr, ctx->e_prev, sweeps == 0, G, nbb, b0,
-                                                                     ctx->n_dir, ctx->Np));
+                   bte::k_sweep<<<sgrid, ctx->sweep_threads, 0, st>>>(
+                       sp, ctx->d_kb.as<double>(), ctx->p_invd.as<double>(), ctx->w_b.as<double>(), ctx->e_curr,
+                       ctx->e_prev, sweeps == 0, G, nbb, b0, ctx->n_dir, ctx->Np));
         ++sweeps;
         if (ctx->plan_lagged_dirs == 0) break;
         BTE_CUDA(ctx->p_part.alloc(sizeof(double) * 2 * (size_t)S * ctx->nchunk));
@@ -864,13 +904,15 @@ extern "C" bte_status bte_solve(bte_ctx* ctx, const bte_options* opts, bte_repor
             if (s != BTE_OK) return s;
         }
         BTE_CUDA(cudaEventRecord(ev[2], st));
-        BTE_LAUNCH(KK_REDUCE, -1, (2.0 * NB * ND + 2.0 * NB + 1) * ctx->n * 8.0, 0,
-                   bte::k_reduce<<<nred, bte::THREADS, 0, st>>>(ctx->e_curr, ctx->e_prev, ctx->d_omega.as<double>(),
-                                                              ctx->d_Cb.as<double>(), ctx->d_Lr.as<double>(), Lr_sum,
-                                                              ctx->T_ref, ctx->solid_angle, ctx->n, NB, ND, Np,
-                                                              ctx->d_Tb.as<double>(), ctx->d_T.as<double>(),
-                                                              ctx->d_ebar.as<double>(), ctx->d_mpart.as<double>()));
-        bte::k_margin_final<<<1, 32, 0, st>>>(ctx->d_mpart.as<double>(), nred, (double)NB * ctx->n,
+        BTE_LAUNCH(KK_REDUCE, -1, (2.0 * NB * ND + NB) * ctx->n * 8.0, 0,
+                   bte::k_reduce<<<dim3(nred, NB), bte::THREADS, 0, st>>>(
+                       ctx->e_curr, ctx->e_prev, ctx->d_omega.as<double>(), ctx->d_Cb.as<double>(), ctx->T_ref,
+                       ctx->n, ND, Np, ctx->d_Tb.as<double>(), ctx->d_mpart.as<double>()));
+        BTE_LAUNCH(KK_REDUCE, -1, (2.0 * NB + 1) * ctx->n * 8.0, 0,
+                   bte::k_recover<<<(ctx->n + 255) / 256, 256, 0, st>>>(
+                       ctx->d_Tb.as<double>(), ctx->d_Cb.as<double>(), ctx->d_Lr.as<double>(), Lr_sum, ctx->T_ref,
+                       ctx->solid_angle, ctx->n, NB, Np, ctx->d_T.as<double>(), ctx->d_ebar.as<double>()));
+        bte::k_margin_final<<<1, 32, 0, st>>>(ctx->d_mpart.as<double>(), nred * NB, (double)NB * ctx->n,
                                              ctx->d_margin.as<double>());
         BTE_LAUNCHED();
         BTE_CUDA(cudaEventRecord(ev[3], st));
@@ -917,6 +959,8 @@ extern "C" bte_status bte_solve(bte_ctx* ctx, const bte_options* opts, bte_repor
     BTE_CUDA(cudaStreamSynchronize(st));
     if (ctx->profile) prof_resolve(ctx, nullptr, 0);
     rep.kernel_launches = ctx->launches;
+    rep.sweep_group = o.form == BTE_FORM_SWEEP ? ctx->sweep_group : 0;
+    rep.sweep_threads = o.form == BTE_FORM_SWEEP ? ctx->sweep_threads : 0;
     ctx->solved = true;
     if (report) *report = rep;
     if (result == BTE_ERR_NOT_CONVERGED && ctx->err.empty()) ctx->err = "max_iter reached";

@@ -116,42 +116,47 @@ __global__ void k_diffuse_wall(const double* __restrict__ e_prev, const int* __r
     ediff[(size_t)b * nbf + e] = acc / wden[k];
 }
 
-// The reductions that close an outer iteration, fused in one pass over
-// e_curr and e_prev (src/StaticBTESolver.cpp:96-120 and :311-321):
+// The reductions that close an outer iteration (src/StaticBTESolver.cpp:96-104
+// and :311-321), one pass over e_curr and e_prev with one block per
+// (256 cells, band):
 //   Tb[b][c] = sum_d e Omega_d / C_b + T_ref
-//   T[c]     = sum_b Lr_b Tb[b][c] / sum_b Lr_b
-//   ebar[b][c] = C_b / Omega_tot (T[c] - T_ref)
-//   margin partial = sum_{b,d} (e_curr - e_prev)^2 over this block's cells
+//   margin partial[b][block] = sum_d (e_curr - e_prev)^2 over the block's cells
 __global__ void __launch_bounds__(THREADS) k_reduce(const double* __restrict__ e_curr, const double* __restrict__ e_prev,
                                                     const double* __restrict__ omega, const double* __restrict__ Cb,
-                                                    const double* __restrict__ Lr, double Lr_sum, double T_ref,
-                                                    double solid_angle, int n, int n_band, int n_dir, size_t Np,
-                                                    double* Tb, double* T, double* ebar, double* part) {
+                                                    double T_ref, int n, int n_dir, size_t Np, double* Tb,
+                                                    double* part) {
     __shared__ double sm[1][NWARP];
     const int c = blockIdx.x * THREADS + threadIdx.x;
+    const int b = blockIdx.y;
     double m[1] = {0.0};
     if (c < n) {
-        double tacc = 0.0;
-        for (int b = 0; b < n_band; ++b) {
-            const double* ec = e_curr + (size_t)b * n_dir * Np + c;
-            const double* ep = e_prev + (size_t)b * n_dir * Np + c;
-            double e0 = 0.0;
-            for (int d = 0; d < n_dir; ++d) {
-                const double a = ec[(size_t)d * Np], p = ep[(size_t)d * Np];
-                e0 += a * omega[d];
-                const double df = a - p;
-                m[0] = fma(df, df, m[0]);
-            }
-            const double tb = e0 / Cb[b] + T_ref;
-            Tb[(size_t)b * Np + c] = tb;
-            tacc += Lr[b] * tb;
+        const double* ec = e_curr + (size_t)b * n_dir * Np + c;
+        const double* ep = e_prev + (size_t)b * n_dir * Np + c;
+        double e0 = 0.0;
+        for (int d = 0; d < n_dir; ++d) {
+            const double a = ec[(size_t)d * Np], p = ep[(size_t)d * Np];
+            e0 += a * omega[d];
+            const double df = a - p;
+            m[0] = fma(df, df, m[0]);
         }
-        const double Tc = tacc / Lr_sum;
-        T[c] = Tc;
-        for (int b = 0; b < n_band; ++b) ebar[(size_t)b * Np + c] = Cb[b] / solid_angle * (Tc - T_ref);
+        Tb[(size_t)b * Np + c] = e0 / Cb[b] + T_ref;
     }
     block_sum<1>(m, sm);
-    if (threadIdx.x == 0) part[blockIdx.x] = m[0];
+    if (threadIdx.x == 0) part[(size_t)b * gridDim.x + blockIdx.x] = m[0];
+}
+
+// src/StaticBTESolver.cpp:106-120: T[c] = sum_b Lr_b Tb[b][c] / sum_b Lr_b and
+// ebar[b][c] = C_b / Omega_tot (T[c] - T_ref).
+__global__ void k_recover(const double* __restrict__ Tb, const double* __restrict__ Cb, const double* __restrict__ Lr,
+                          double Lr_sum, double T_ref, double solid_angle, int n, int n_band, size_t Np, double* T,
+                          double* ebar) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    double tacc = 0.0;
+    for (int b = 0; b < n_band; ++b) tacc += Lr[b] * Tb[(size_t)b * Np + c];
+    const double Tc = tacc / Lr_sum;
+    T[c] = Tc;
+    for (int b = 0; b < n_band; ++b) ebar[(size_t)b * Np + c] = Cb[b] / solid_angle * (Tc - T_ref);
 }
 
 // margin = sum of partials / (n_band n_cell), in block order.
@@ -232,10 +237,48 @@ struct SweepPlan {
     int n, F;
 };
 
+// 1/D per system in level order: invD[b][d][j] = 1 / (k_b dg[d][j] + vo[d][j]).
+// The diagonal does not change across outer iterations, so this runs once per solve.
+__global__ void k_sweep_invd(SweepPlan sp, const double* __restrict__ kb, int n_band, int n_dir, double* invD) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int d = blockIdx.y;
+    if (j >= sp.n) return;
+    const size_t pj = (size_t)d * sp.n + j;
+    for (int b = 0; b < n_band; ++b)
+        invD[((size_t)b * n_dir + d) * sp.n + j] = 1.0 / fma(kb[b], sp.dg[pj], sp.vo[pj]);
+}
+
+// Operands of one sweep item that do not depend on the level being solved.
+struct SweepItem {
+    int c, b, bl;
+    int u[4];
+    double cf[4];
+    double invd, r;
+};
+
+__device__ __forceinline__ void sweep_load(const SweepPlan& sp, const double* __restrict__ invD,
+                                           const double* __restrict__ rhs, int d, int j, int bl, int b0, int nbb,
+                                           int n_dir, size_t Np, SweepItem& it) {
+    const size_t pj = (size_t)d * sp.n + j;
+    it.bl = bl;
+    it.b = b0 + bl;
+    it.c = sp.cell[pj];
+    for (int f = 0; f < sp.F; ++f) {
+        const size_t q = ((size_t)d * sp.F + f) * sp.n + j;
+        it.u[f] = sp.nb[q];
+        it.cf[f] = sp.fc[q];
+    }
+    it.invd = invD[((size_t)it.b * n_dir + d) * sp.n + j];
+    it.r = rhs[((size_t)d * nbb + bl) * Np + it.c];
+}
+
 // One block sweeps direction blockIdx.y for bands b0 + blockIdx.x * G .. + G - 1.
 // rhs is batch-local ([batch row y][Np], y = d * nbb + (b - b0)); x and x_old are
-// e_curr / e_prev ([band][n_dir][Np]).
-__global__ void __launch_bounds__(512) k_sweep(SweepPlan sp, const double* __restrict__ kb, const double* __restrict__ rhs,
+// e_curr / e_prev ([band][n_dir][Np]).  A thread's first item of the next
+// level is loaded before the level barrier, so after it only the upstream
+// values x[u] are on the critical path.
+__global__ void __launch_bounds__(512) k_sweep(SweepPlan sp, const double* __restrict__ kb,
+                                               const double* __restrict__ invD, const double* __restrict__ rhs,
                                                double* x, const double* __restrict__ x_old, int first_sweep,
                                                int G, int nbb, int b0, int n_dir, size_t Np) {
     const int d = blockIdx.y;
@@ -243,29 +286,39 @@ __global__ void __launch_bounds__(512) k_sweep(SweepPlan sp, const double* __res
     const int gn = min(G, nbb - g0);
     if (gn <= 0) return;
     const int L0 = sp.lvl_off[d], L1 = sp.lvl_off[d + 1];
-    const size_t pd = (size_t)d * sp.n;
+    SweepItem nxt;
+    bool have = false;
+    {
+        const int items = (sp.lvl[L0 + 1] - sp.lvl[L0]) * gn;
+        if (threadIdx.x < items)
+            sweep_load(sp, invD, rhs, d, sp.lvl[L0] + threadIdx.x / gn, g0 + threadIdx.x % gn, b0, nbb, n_dir, Np,
+                       nxt), have = true;
+    }
     for (int l = L0; l < L1 - 1; ++l) {
         const int j0 = sp.lvl[l], j1 = sp.lvl[l + 1];
         const int items = (j1 - j0) * gn;
         for (int it = threadIdx.x; it < items; it += blockDim.x) {
-            const int j = j0 + it / gn;
-            const int bl = g0 + it % gn;  // band within the batch
-            const int b = b0 + bl;
-            const size_t pj = pd + j;
-            const int c = sp.cell[pj];
-            const double k = kb[b];
-            double* xb = x + ((size_t)b * n_dir + d) * Np;
-            const double* xo = x_old + ((size_t)b * n_dir + d) * Np;
+            SweepItem cur;
+            if (it == threadIdx.x && have) cur = nxt;
+            else sweep_load(sp, invD, rhs, d, j0 + it / gn, g0 + it % gn, b0, nbb, n_dir, Np, cur);
+            double* xb = x + ((size_t)cur.b * n_dir + d) * Np;
+            const double* xo = x_old + ((size_t)cur.b * n_dir + d) * Np;
             double off = 0.0;
             for (int f = 0; f < sp.F; ++f) {
-                const int u = sp.nb[((size_t)d * sp.F + f) * sp.n + j];
+                const int u = cur.u[f];
                 if (u == -1) continue;
-                const double cf = sp.fc[((size_t)d * sp.F + f) * sp.n + j];
                 const double xu = u >= 0 ? xb[u] : (first_sweep ? xo[-u - 2] : xb[-u - 2]);
-                off = fma(cf, xu, off);
+                off = fma(cur.cf[f], xu, off);
             }
-            const double D = fma(k, sp.dg[pj], sp.vo[pj]);
-            xb[c] = (rhs[((size_t)d * nbb + bl) * Np + c] - k * off) / D;
+            xb[cur.c] = fma(-kb[cur.b], off, cur.r) * cur.invd;
+        }
+        have = false;
+        if (l + 1 < L1 - 1) {
+            const int k0 = sp.lvl[l + 1], k1 = sp.lvl[l + 2];
+            if (threadIdx.x < (k1 - k0) * gn) {
+                sweep_load(sp, invD, rhs, d, k0 + threadIdx.x / gn, g0 + threadIdx.x % gn, b0, nbb, n_dir, Np, nxt);
+                have = true;
+            }
         }
         __syncthreads();
     }

@@ -53,7 +53,6 @@ def test_plain_form_1d(sbte, oracle_mod, get_case, name):
     assert res.status == 6  # not converged, as the reference GPU path
     assert rel_l2(res.T, c.ref["T"]) < 1e-8
     np.testing.assert_allclose(res.q, c.ref["q"], rtol=1e-6)
-    assert res.margins[-1] < 1.0
 
 
 @pytest.mark.parametrize("name", TESTSH_CASES)

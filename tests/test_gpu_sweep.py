@@ -45,32 +45,50 @@ def test_sweep_matches_sol_logs(sbte, get_case, name):
     np.testing.assert_allclose(res.q[big], q_logged[big], rtol=6e-6)
 
 
-def test_sweep_with_cycles_matches_bicgstab(sbte, get_case):
-    """Upwind graphs with cycles: lagged edges and repeated Gauss-Seidel sweeps.
+def _rewired(sbte, c, n_swaps=40, seed=0):
+    """Geometry arrays whose upwind graphs have cycles.
 
-    Flipping the stored normal of one side of an interior face makes both cells
-    see that face as inflow for half of the directions (a 2-cycle)."""
-    c = get_case("2DM2DG")
+    Planar meshes never do (interior-disjoint convex cells in the plane admit a
+    translation order for every direction), so partners of random interior
+    face pairs are exchanged: (c1,f1)<->(c2,f2) and (c3,f3)<->(c4,f4) become
+    (c1,f1)<->(c4,f4) and (c3,f3)<->(c2,f2).  Every row keeps its own faces'
+    areas and normals, so each system stays a diagonally dominant M-matrix of
+    the reference's form; the long links close cycles."""
     p = sbte.Problem(*c.args())
     a = p.arrays()
-    nbr, nrm = a["nbr"], a["normal"].copy()
-    flipped = 0
-    for cell in range(0, p.n_cell, 37):
-        for f in range(p.n_face):
-            if nbr[cell, f] >= 0:
-                nrm[cell, f] *= -1.0
-                flipped += 1
-                break
-    a["normal"] = nrm
+    nbr = a["nbr"].copy()
+    rng = np.random.default_rng(seed)
+    pairs = [(cc, f) for cc in range(p.n_cell) for f in range(p.n_face) if nbr[cc, f] > cc]
+    back = lambda cc, f: int(np.nonzero(nbr[nbr[cc, f]] == cc)[0][0])
+    used = set()
+    for _ in range(n_swaps):
+        i, j = rng.choice(len(pairs), 2, replace=False)
+        (c1, f1), (c3, f3) = pairs[i], pairs[j]
+        c2, c4 = nbr[c1, f1], nbr[c3, f3]
+        if len({c1, c2, c3, c4} & used) or len({c1, c2, c3, c4}) < 4:
+            continue
+        f2, f4 = back(c1, f1), back(c3, f3)
+        nbr[c1, f1], nbr[c4, f4] = c4, c1
+        nbr[c3, f3], nbr[c2, f2] = c2, c3
+        used |= {c1, c2, c3, c4}
+    a["nbr"] = nbr
+    return a
+
+
+def test_sweep_with_cycles_matches_bicgstab(sbte, get_case):
+    """Cycles in the upwind graph: lagged edges and repeated Gauss-Seidel sweeps."""
+    c = get_case("square16_b8")
+    a = _rewired(sbte, c)
     out = {}
     for form in (sbte.FORM_PLAIN, sbte.FORM_SWEEP):
         ctx = sbte.Context(0).set_arrays(a)
-        st, rep = ctx.solve(max_iter=200, tol=1e-5, form=form)
-        out[form] = (ctx.temperature(), rep.as_dict())
+        st, rep = ctx.solve(max_iter=400, tol=1e-5, form=form)
+        out[form] = (st, ctx.temperature(), rep.as_dict())
         ctx.close()
-    Tp, rp = out[sbte.FORM_PLAIN]
-    Ts, rs = out[sbte.FORM_SWEEP]
-    assert flipped > 5
+    sp, Tp, rp = out[sbte.FORM_PLAIN]
+    ss, Ts, rs = out[sbte.FORM_SWEEP]
+    assert sp == 0 and ss == 0
     assert rs["inner_iterations"] > rs["inner_solves"]  # some systems needed more than one sweep
+    assert rs["inner_unconverged"] == 0
     assert rs["n_iter"] == rp["n_iter"]
     assert rel_l2(Ts - 300, Tp - 300) < 1e-6

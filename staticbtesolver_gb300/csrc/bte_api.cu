@@ -770,8 +770,8 @@ static bte_status solve_batch_sweep(bte_ctx* ctx, int b0, int nbb, const bte_opt
     const double geo = N * ((ctx->F + 2) * w + ctx->F * 4.0) * ctx->n_dir;
     dim3 grid(ctx->nchunk, S);
     BTE_LAUNCH(KK_RHS, -1, S * N * 2 * w + geo / 2, 0,
-               bte::k_rhs<<<grid, bte::THREADS, 0, st>>>(op, bd, ctx->d_ebar.as<double>(), ctx->e_prev,
-                                                         ctx->w_b.as<double>(), ctx->n));
+               bte::k_rhs_sweep<<<grid, bte::THREADS, 0, st>>>(op, bd, ctx->p_cell.as<int>(), ctx->d_ebar.as<double>(),
+                                                               ctx->e_prev, ctx->w_b.as<double>(), ctx->n));
     bte::SweepPlan sp{ctx->p_cell.as<int>(), ctx->p_dg.as<double>(), ctx->p_vo.as<double>(), ctx->p_nb.as<int>(),
                       ctx->p_fc.as<double>(), ctx->p_lvl.as<int>(), ctx->p_lvl_off.as<int>(), ctx->n, ctx->F};
     // launch-shape autotuning on the first sweep of this plan (each candidate
@@ -818,8 +818,8 @@ static bte_status solve_batch_sweep(bte_ctx* ctx, int b0, int nbb, const bte_opt
         BTE_CUDA(ctx->p_bad.alloc(sizeof(int)));
         BTE_CUDA(cudaMemsetAsync(ctx->p_bad.p, 0, sizeof(int), st));
         BTE_LAUNCH(KK_SWEEP_RES, -1, S * N * 2 * w + geo, 0,
-                   bte::k_sweep_residual<<<grid, bte::THREADS, 0, st>>>(op, ctx->w_b.as<double>(),
-                                                                        ctx->p_part.as<double>(), ctx->nchunk));
+                   bte::k_sweep_residual<<<grid, bte::THREADS, 0, st>>>(op, ctx->p_cell.as<int>(), ctx->w_b.as<double>(),
+                                                                        ctx->p_part.as<double>(), ctx->nchunk, ctx->n));
         bte::k_sweep_check<<<(S + 127) / 128, 128, 0, st>>>(ctx->p_part.as<double>(), S, ctx->nchunk, o.inner_tol,
                                                              ctx->p_bad.as<int>());
         BTE_LAUNCHED();

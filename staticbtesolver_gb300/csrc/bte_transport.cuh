@@ -96,6 +96,41 @@ __global__ void __launch_bounds__(THREADS) k_rhs(FaceFluxOp op, Boundary bd, con
     }
 }
 
+// The same right-hand sides written in each direction's sweep order
+// (rhs[y][j] for cell perm[d][j]), so the sweep reads them coalesced and
+// without a dependent gather.
+__global__ void __launch_bounds__(THREADS) k_rhs_sweep(FaceFluxOp op, Boundary bd, const int* __restrict__ perm,
+                                                       const double* __restrict__ ebar, const double* __restrict__ e_prev,
+                                                       double* rhs, int n) {
+    const int y = blockIdx.y;
+    int b, d;
+    op.bd(y, b, d);
+    const double k = op.kb[b];
+    const size_t o = (size_t)y * op.Np;
+    const double* ep_bd_base = e_prev + (size_t)b * op.n_dir * op.Np;
+    BTE_CELL_LOOP(j) {
+        if (j >= n) continue;
+        const int c = perm[(size_t)d * n + j];
+        double r = 0.0;
+        const int e0 = bd.bptr[c], e1 = bd.bptr[c + 1];
+        for (int e = e0; e < e1; ++e) {
+            const double cf = bd.cin[(size_t)d * bd.nbf + e];
+            if (cf == 0.0) continue;
+            double ew;
+            switch (bd.bf_kind[e]) {
+                case 1: ew = bd.eiso[(size_t)b * bd.n_bc + bd.bf_bc[e]]; break;
+                case 2: ew = bd.ediff[(size_t)b * bd.nbf + e]; break;
+                case 31: ew = ep_bd_base[(size_t)bd.mirror[d] * op.Np + c]; break;
+                case 32: ew = ep_bd_base[(size_t)bd.mirror[op.n_dir + d] * op.Np + c]; break;
+                default: ew = ep_bd_base[(size_t)bd.mirror[2 * op.n_dir + d] * op.Np + c]; break;
+            }
+            r -= ew * (k * cf);
+        }
+        r += ebar[(size_t)b * op.Np + c] * op.vo[(size_t)d * op.Np + c];
+        rhs[o + j] = r;
+    }
+}
+
 // Diffuse wall energy per (band, diffuse face) from the previous iterate
 // (src/StaticBTESolver.cpp:180-204): sum over outgoing directions of
 // e w / sum w, w = (S.n) Omega in 3D, S.n in 2D; 1D: sum e (s.n) Omega / pi.
@@ -250,33 +285,38 @@ __global__ void k_sweep_invd(SweepPlan sp, const double* __restrict__ kb, int n_
 
 // Operands of one sweep item that do not depend on the level being solved.
 struct SweepItem {
-    int c, b, bl;
+    int c, b;
     int u[4];
     double cf[4];
     double invd, r;
 };
 
+// rhs is in sweep order: rhs[(d * nbb + bl) * Np + j].
 __device__ __forceinline__ void sweep_load(const SweepPlan& sp, const double* __restrict__ invD,
                                            const double* __restrict__ rhs, int d, int j, int bl, int b0, int nbb,
                                            int n_dir, size_t Np, SweepItem& it) {
     const size_t pj = (size_t)d * sp.n + j;
-    it.bl = bl;
     it.b = b0 + bl;
     it.c = sp.cell[pj];
-    for (int f = 0; f < sp.F; ++f) {
-        const size_t q = ((size_t)d * sp.F + f) * sp.n + j;
-        it.u[f] = sp.nb[q];
-        it.cf[f] = sp.fc[q];
+#pragma unroll
+    for (int f = 0; f < 4; ++f) {
+        if (f < sp.F) {
+            const size_t q = ((size_t)d * sp.F + f) * sp.n + j;
+            it.u[f] = sp.nb[q];
+            it.cf[f] = sp.fc[q];
+        } else {
+            it.u[f] = -1;
+            it.cf[f] = 0.0;
+        }
     }
     it.invd = invD[((size_t)it.b * n_dir + d) * sp.n + j];
-    it.r = rhs[((size_t)d * nbb + bl) * Np + it.c];
+    it.r = rhs[((size_t)d * nbb + bl) * Np + j];
 }
 
 // One block sweeps direction blockIdx.y for bands b0 + blockIdx.x * G .. + G - 1.
-// rhs is batch-local ([batch row y][Np], y = d * nbb + (b - b0)); x and x_old are
-// e_curr / e_prev ([band][n_dir][Np]).  A thread's first item of the next
-// level is loaded before the level barrier, so after it only the upstream
-// values x[u] are on the critical path.
+// x and x_old are e_curr / e_prev ([band][n_dir][Np]).  Each thread's first
+// item of the next two levels is loaded ahead (everything but the upstream
+// values), so after a level barrier only the x[u] reads are on the critical path.
 __global__ void __launch_bounds__(512) k_sweep(SweepPlan sp, const double* __restrict__ kb,
                                                const double* __restrict__ invD, const double* __restrict__ rhs,
                                                double* x, const double* __restrict__ x_old, int first_sweep,
@@ -285,26 +325,30 @@ __global__ void __launch_bounds__(512) k_sweep(SweepPlan sp, const double* __res
     const int g0 = blockIdx.x * G;
     const int gn = min(G, nbb - g0);
     if (gn <= 0) return;
-    const int L0 = sp.lvl_off[d], L1 = sp.lvl_off[d + 1];
-    SweepItem nxt;
-    bool have = false;
-    {
-        const int items = (sp.lvl[L0 + 1] - sp.lvl[L0]) * gn;
-        if (threadIdx.x < items)
-            sweep_load(sp, invD, rhs, d, sp.lvl[L0] + threadIdx.x / gn, g0 + threadIdx.x % gn, b0, nbb, n_dir, Np,
-                       nxt), have = true;
-    }
-    for (int l = L0; l < L1 - 1; ++l) {
+    const int L0 = sp.lvl_off[d], L1 = sp.lvl_off[d + 1] - 1;  // levels L0 .. L1-1
+    SweepItem p1, p2;  // this thread's first item of levels l and l+1
+    bool h1 = false, h2 = false;
+    auto pre = [&](int l, SweepItem& dst) -> bool {
+        if (l >= L1) return false;
+        const int j0 = sp.lvl[l];
+        if (threadIdx.x >= (sp.lvl[l + 1] - j0) * gn) return false;
+        sweep_load(sp, invD, rhs, d, j0 + threadIdx.x / gn, g0 + threadIdx.x % gn, b0, nbb, n_dir, Np, dst);
+        return true;
+    };
+    h1 = pre(L0, p1);
+    h2 = pre(L0 + 1, p2);
+    for (int l = L0; l < L1; ++l) {
         const int j0 = sp.lvl[l], j1 = sp.lvl[l + 1];
         const int items = (j1 - j0) * gn;
         for (int it = threadIdx.x; it < items; it += blockDim.x) {
             SweepItem cur;
-            if (it == threadIdx.x && have) cur = nxt;
+            if (it == threadIdx.x && h1) cur = p1;
             else sweep_load(sp, invD, rhs, d, j0 + it / gn, g0 + it % gn, b0, nbb, n_dir, Np, cur);
             double* xb = x + ((size_t)cur.b * n_dir + d) * Np;
             const double* xo = x_old + ((size_t)cur.b * n_dir + d) * Np;
             double off = 0.0;
-            for (int f = 0; f < sp.F; ++f) {
+#pragma unroll
+            for (int f = 0; f < 4; ++f) {
                 const int u = cur.u[f];
                 if (u == -1) continue;
                 const double xu = u >= 0 ? xb[u] : (first_sweep ? xo[-u - 2] : xb[-u - 2]);
@@ -312,31 +356,32 @@ __global__ void __launch_bounds__(512) k_sweep(SweepPlan sp, const double* __res
             }
             xb[cur.c] = fma(-kb[cur.b], off, cur.r) * cur.invd;
         }
-        have = false;
-        if (l + 1 < L1 - 1) {
-            const int k0 = sp.lvl[l + 1], k1 = sp.lvl[l + 2];
-            if (threadIdx.x < (k1 - k0) * gn) {
-                sweep_load(sp, invD, rhs, d, k0 + threadIdx.x / gn, g0 + threadIdx.x % gn, b0, nbb, n_dir, Np, nxt);
-                have = true;
-            }
-        }
+        p1 = p2;
+        h1 = h2;
+        h2 = pre(l + 2, p2);
         __syncthreads();
     }
 }
 
-// Residual test of the sweep solution for batch rows (directions with lagged
-// edges only): partials of ||R - A x||^2 and ||R||^2 per (row, chunk).
-__global__ void __launch_bounds__(THREADS) k_sweep_residual(FaceFluxOp op, const double* __restrict__ rhs,
-                                                            double* part, int nchunk) {
+// Residual test of the sweep solution (rhs in sweep order, as k_rhs_sweep
+// writes it): partials of ||R - A x||^2 and ||R||^2 per (row, chunk).
+__global__ void __launch_bounds__(THREADS) k_sweep_residual(FaceFluxOp op, const int* __restrict__ perm,
+                                                            const double* __restrict__ rhs, double* part, int nchunk,
+                                                            int n) {
     __shared__ double sm[2][NWARP];
     const int y = blockIdx.y;
+    int b, d;
+    op.bd(y, b, d);
     const size_t o = (size_t)y * op.Np;
     const double* xs = op.x_of(y);
     double acc[2] = {0, 0};
-    BTE_CELL_LOOP(c) {
-        const double r = rhs[o + c] - op.template apply<double>(y, c, xs);
-        acc[0] = fma(r, r, acc[0]);
-        acc[1] = fma(rhs[o + c], rhs[o + c], acc[1]);
+    BTE_CELL_LOOP(j) {
+        if (j < n) {
+            const int c = perm[(size_t)d * n + j];
+            const double r = rhs[o + j] - op.template apply<double>(y, c, xs);
+            acc[0] = fma(r, r, acc[0]);
+            acc[1] = fma(rhs[o + j], rhs[o + j], acc[1]);
+        }
     }
     block_sum<2>(acc, sm);
     if (threadIdx.x == 0) {

@@ -49,21 +49,27 @@ def _rewired(sbte, c, n_swaps=40, seed=0):
     """Geometry arrays whose upwind graphs have cycles.
 
     Planar meshes never do (interior-disjoint convex cells in the plane admit a
-    translation order for every direction), so partners of random interior
-    face pairs are exchanged: (c1,f1)<->(c2,f2) and (c3,f3)<->(c4,f4) become
-    (c1,f1)<->(c4,f4) and (c3,f3)<->(c2,f2).  Every row keeps its own faces'
-    areas and normals, so each system stays a diagonally dominant M-matrix of
-    the reference's form; the long links close cycles."""
+    translation order for every direction), so partners of interior face
+    pairs are exchanged: (c1,f1)<->(c2,f2) and (c3,f3)<->(c4,f4) become
+    (c1,f1)<->(c4,f4) and (c3,f3)<->(c2,f2), for faces with nearly the same
+    normal and area so the flux stays conserved.  Every row keeps its own
+    faces' areas and normals, so each system stays a diagonally dominant
+    M-matrix of the reference's form; the long links close cycles."""
     p = sbte.Problem(*c.args())
     a = p.arrays()
     nbr = a["nbr"].copy()
+    nrm, area = a["normal"], a["area"]
     rng = np.random.default_rng(seed)
     pairs = [(cc, f) for cc in range(p.n_cell) for f in range(p.n_face) if nbr[cc, f] > cc]
     back = lambda cc, f: int(np.nonzero(nbr[nbr[cc, f]] == cc)[0][0])
     used = set()
-    for _ in range(n_swaps):
+    for _ in range(200 * n_swaps):
+        if len(used) >= 4 * n_swaps:
+            break
         i, j = rng.choice(len(pairs), 2, replace=False)
         (c1, f1), (c3, f3) = pairs[i], pairs[j]
+        if np.dot(nrm[c1, f1], nrm[c3, f3]) < 0.995 or abs(area[c1, f1] / area[c3, f3] - 1) > 0.05:
+            continue
         c2, c4 = nbr[c1, f1], nbr[c3, f3]
         if len({c1, c2, c3, c4} & used) or len({c1, c2, c3, c4}) < 4:
             continue
@@ -78,16 +84,16 @@ def _rewired(sbte, c, n_swaps=40, seed=0):
 def test_sweep_with_cycles_matches_bicgstab(sbte, get_case):
     """Cycles in the upwind graph: lagged edges and repeated Gauss-Seidel sweeps."""
     c = get_case("square16_b8")
-    a = _rewired(sbte, c)
+    a = _rewired(sbte, c, n_swaps=10)
     out = {}
     for form in (sbte.FORM_PLAIN, sbte.FORM_SWEEP):
         ctx = sbte.Context(0).set_arrays(a)
-        st, rep = ctx.solve(max_iter=400, tol=1e-5, form=form)
+        st, rep = ctx.solve(max_iter=3000, tol=1e-5, form=form)
         out[form] = (st, ctx.temperature(), rep.as_dict())
         ctx.close()
     sp, Tp, rp = out[sbte.FORM_PLAIN]
     ss, Ts, rs = out[sbte.FORM_SWEEP]
-    assert sp == 0 and ss == 0
+    assert sp == 0 and ss == 0, (sp, ss, rp, rs)
     assert rs["inner_iterations"] > rs["inner_solves"]  # some systems needed more than one sweep
     assert rs["inner_unconverged"] == 0
     assert rs["n_iter"] == rp["n_iter"]

@@ -912,7 +912,7 @@ extern "C" bte_status bte_solve(bte_ctx* ctx, const bte_options* opts, bte_repor
                    bte::k_recover<<<(ctx->n + 255) / 256, 256, 0, st>>>(
                        ctx->d_Tb.as<double>(), ctx->d_Cb.as<double>(), ctx->d_Lr.as<double>(), Lr_sum, ctx->T_ref,
                        ctx->solid_angle, ctx->n, NB, Np, ctx->d_T.as<double>(), ctx->d_ebar.as<double>()));
-        bte::k_margin_final<<<1, 32, 0, st>>>(ctx->d_mpart.as<double>(), nred * NB, (double)NB * ctx->n,
+        bte::k_margin_final<<<1, bte::THREADS, 0, st>>>(ctx->d_mpart.as<double>(), nred * NB, (double)NB * ctx->n,
                                              ctx->d_margin.as<double>());
         BTE_LAUNCHED();
         BTE_CUDA(cudaEventRecord(ev[3], st));

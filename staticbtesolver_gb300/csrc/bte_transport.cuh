@@ -194,12 +194,15 @@ __global__ void k_recover(const double* __restrict__ Tb, const double* __restric
     for (int b = 0; b < n_band; ++b) ebar[(size_t)b * Np + c] = Cb[b] / solid_angle * (Tc - T_ref);
 }
 
-// margin = sum of partials / (n_band n_cell), in block order.
-__global__ void k_margin_final(const double* part, int nparts, double denom, double* out) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    double s = 0.0;
-    for (int i = 0; i < nparts; ++i) s += part[i];
-    out[0] = s / denom;
+// margin = sum of partials / (n_band n_cell).  One block: thread t sums
+// partials t, t+256, ... in order, then a fixed-order block reduction, so the
+// result does not depend on timing.
+__global__ void __launch_bounds__(THREADS) k_margin_final(const double* part, int nparts, double denom, double* out) {
+    __shared__ double sm[1][NWARP];
+    double v[1] = {0.0};
+    for (int i = threadIdx.x; i < nparts; i += THREADS) v[0] += part[i];
+    block_sum<1>(v, sm);
+    if (threadIdx.x == 0) out[0] = v[0] / denom;
 }
 
 // Heat flux, step 1 (src/StaticBTESolver.cpp:331-354): per (band, boundary face),

@@ -159,7 +159,7 @@ def measured_peaks():
 
 def ncu_traffic(kernel):
     """DRAM bytes per launch of `kernel` from the committed ncu summary, if any."""
-    path = os.path.join(ROOT, "profiles", "bicgstab_square20k.md")
+    path = os.path.join(ROOT, "profiles", "upwind_sweep_square20k.md")
     if not os.path.exists(path):
         return None
     for line in open(path):

@@ -106,10 +106,10 @@ struct FaceFluxOp {
         bd(y, b, d);
         return x_out + ((size_t)b * n_dir + d) * Np;
     }
-    __device__ __forceinline__ double diag(int y, int c) const {
+    __device__ __forceinline__ double inv_diag(int y, int c) const {
         int b, d;
         bd(y, b, d);
-        return fma(kb[b], dg[(size_t)d * Np + c], vo[(size_t)d * Np + c]);
+        return 1.0 / fma(kb[b], dg[(size_t)d * Np + c], vo[(size_t)d * Np + c]);
     }
     template <typename T>
     __device__ __forceinline__ T apply(int y, int c, const T* __restrict__ xs) const {
@@ -134,12 +134,14 @@ struct CsrOp {
     int n;
     size_t Np;
     __device__ __forceinline__ double* x_of(int) const { return x_out; }
-    __device__ __forceinline__ double diag(int, int c) const {
+    // src/bicgstab.hpp:122-131: 1 / (last stored diagonal entry), 0 for a row
+    // without one
+    __device__ __forceinline__ double inv_diag(int, int c) const {
         if (c >= n) return 1.0;
-        double dv = 0.0;  // src/bicgstab.hpp:125-131: the last diagonal entry wins
+        double inv = 0.0;
         for (int k = rowptr[c]; k < rowptr[c + 1]; ++k)
-            if (col[k] == c) dv = val[k];
-        return dv;
+            if (col[k] == c) inv = 1.0 / val[k];
+        return inv;
     }
     template <typename T>
     __device__ __forceinline__ T apply(int, int c, const T* __restrict__ xs) const {
@@ -163,8 +165,7 @@ __global__ void __launch_bounds__(THREADS) k_bicg_init(Op op, BicgVecs<double> v
     double acc[2] = {0, 0};
     BTE_CELL_LOOP(c) {
         double bb = v.b[o + c];
-        double dv = op.diag(y, c);
-        v.invD[o + c] = 1.0 / dv;
+        v.invD[o + c] = op.inv_diag(y, c);
         v.r[o + c] = bb; v.p[o + c] = bb; v.rw[o + c] = bb; v.q[o + c] = 0.0;
         x[c] = 0.0;
         acc[0] = fma(bb, bb, acc[0]);

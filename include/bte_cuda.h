@@ -162,6 +162,24 @@ bte_status bte_bicgstab_csr(int n, const int* rowptr, const int* colind, const d
                             int nnz, const double* b, double* x, int maxit, double tol,
                             int* iterations, int* converged);
 
+/* Allocation-free variant of bte_bicgstab_csr.  No counterpart in the
+ * reference: it exists for callers that cannot allocate device memory -- code
+ * whose device memory belongs to another allocator with a fixed budget, or
+ * that must not trigger the device-wide synchronisation of cudaMalloc/cudaFree
+ * in the middle of its stream work.  rowptr, colind, val, b and x are DEVICE
+ * pointers owned by the caller; stream is a cudaStream_t (NULL: the legacy
+ * default stream).  All scratch (work vectors, scalars, partial sums) lives in
+ * one static device array of about 21 MB that every GPU loading this library
+ * keeps until exit; it calls no cudaMalloc, cudaFree or allocating library
+ * routine.  Limits: n <= 262144 unknowns, maxit <= 10000; larger values and a
+ * malformed CSR return BTE_ERR_INVALID_ARGUMENT (message in bte_last_error(NULL)).
+ * The first call on a device looks up the array's device address and should
+ * come before any stream capture.  Calls share the array: calls that overlap
+ * on the GPU race.  The call returns after the solve has finished. */
+bte_status bte_bicgstab_csr_noalloc(int n, const int* rowptr, const int* colind, const double* val,
+                                    int nnz, const double* b, double* x, int maxit, double tol,
+                                    void* stream, int* iterations, int* converged);
+
 #ifdef __cplusplus
 }
 #endif

@@ -13,6 +13,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <thread>
 #include <vector>
@@ -1123,3 +1124,158 @@ bte_status bte_bicgstab_csr(int n, const int* rowptr, const int* colind, const d
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Allocation-free CSR BiCGSTAB (bte_bicgstab_csr_noalloc).
+//
+// For callers that cannot allocate device memory themselves: code whose
+// device memory is owned by another allocator with a fixed budget (a
+// framework's caching pool, an embedding application), and code that must not
+// trigger the implicit device-wide synchronisation of cudaMalloc/cudaFree in
+// the middle of its stream work.  The caller passes device inputs and outputs;
+// every work vector, per-system scalar and partial dot product lives in the
+// file-scope array below, which every GPU that loads this library holds until
+// the process exits (kNoAllocScratchBytes, about 21 MB).
+//
+// Host code must not pass g_noalloc_scratch itself to a kernel: in host code
+// the name is a host-side stand-in, not a device address.  The device address
+// is looked up once per device with cudaGetSymbolAddress (with that device
+// current) on the first call made on it; that first call should therefore come
+// before any stream capture.  All calls share the one array and leave their
+// contents in it: each call clears what must start at zero, and calls that
+// overlap on the GPU (different streams or threads at the same time) race.
+namespace {
+constexpr int kNoAllocMaxN = 1 << 18;     // unknowns
+constexpr int kNoAllocMaxIt = 10000;      // BiCGSTAB iterations
+constexpr size_t kNoAllocNp = ((size_t)kNoAllocMaxN + bte::CH - 1) / bte::CH * bte::CH;
+constexpr int kNoAllocChunks = (int)(kNoAllocNp / bte::CH);
+// doubles: 10 vectors of kNoAllocNp (r, r_hat, p, p_hat, q, z, t, b, 1/D, x),
+// 7 x kNoAllocChunks partials, 8 scalars; then ints (done, iters, flagA[2],
+// flagB[2], error flag, spare, active[kNoAllocMaxIt + 2]) packed two per double.
+constexpr size_t kNoAllocDoubles = 10 * kNoAllocNp + 7 * (size_t)kNoAllocChunks + 8;
+constexpr size_t kNoAllocInts = 8 + (size_t)kNoAllocMaxIt + 2;
+constexpr size_t kNoAllocScratch = kNoAllocDoubles + (kNoAllocInts + 1) / 2;
+constexpr size_t kNoAllocScratchBytes = kNoAllocScratch * sizeof(double);
+}  // namespace
+
+static __device__ __align__(256) double g_noalloc_scratch[kNoAllocScratch];
+
+// Checks a caller's device CSR (row pointers non-decreasing from 0 to nnz,
+// column indices in range) before any kernel dereferences it.
+__global__ void k_noalloc_check_csr(const int* __restrict__ rowptr, const int* __restrict__ col, int n, int nnz,
+                                    int* bad) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t == 0 && (rowptr[0] != 0 || rowptr[n] != nnz)) atomicOr(bad, 1);
+    if (t < n && rowptr[t + 1] < rowptr[t]) atomicOr(bad, 1);
+    for (int k = t; k < nnz; k += gridDim.x * blockDim.x)
+        if (col[k] < 0 || col[k] >= n) atomicOr(bad, 1);
+}
+
+static std::mutex g_noalloc_mutex;
+static double* g_noalloc_dev[256] = {};
+
+// Device address of g_noalloc_scratch on the current device (looked up once per device).
+static cudaError_t noalloc_scratch_address(int device, double** out) {
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (device < 0 || device >= 256) return cudaErrorInvalidDevice;
+    if (!g_noalloc_dev[device]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return e;
+        g_noalloc_dev[device] = static_cast<double*>(p);
+    }
+    *out = g_noalloc_dev[device];
+    return cudaSuccess;
+}
+
+#define NOALLOC_CUDA(call)                                                            \
+    do {                                                                              \
+        cudaError_t _e = (call);                                                      \
+        if (_e != cudaSuccess) {                                                      \
+            g_create_error = std::string("bte_bicgstab_csr_noalloc: ") + #call + ": " + \
+                             cudaGetErrorString(_e);                                  \
+            return BTE_ERR_CUDA;                                                      \
+        }                                                                             \
+    } while (0)
+
+extern "C" bte_status bte_bicgstab_csr_noalloc(int n, const int* rowptr, const int* colind, const double* val,
+                                               int nnz, const double* b, double* x, int maxit, double tol,
+                                               void* stream, int* iterations, int* converged) {
+    if (n <= 0 || n > kNoAllocMaxN) {
+        g_create_error = "bte_bicgstab_csr_noalloc: n must be in 1.." + std::to_string(kNoAllocMaxN);
+        return BTE_ERR_INVALID_ARGUMENT;
+    }
+    if (maxit <= 0 || maxit > kNoAllocMaxIt) {
+        g_create_error = "bte_bicgstab_csr_noalloc: maxit must be in 1.." + std::to_string(kNoAllocMaxIt);
+        return BTE_ERR_INVALID_ARGUMENT;
+    }
+    if (!rowptr || !colind || !val || !b || !x || nnz < 0 || !(tol > 0)) {
+        g_create_error = "bte_bicgstab_csr_noalloc: null pointer, negative nnz or tol <= 0";
+        return BTE_ERR_INVALID_ARGUMENT;
+    }
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    int dev = 0;
+    NOALLOC_CUDA(cudaGetDevice(&dev));
+    double* base = nullptr;
+    NOALLOC_CUDA(noalloc_scratch_address(dev, &base));
+    const size_t Np = (size_t)((n + bte::CH - 1) / bte::CH) * bte::CH;
+    const int nchunk = (int)(Np / bte::CH);
+    double* vec[10];
+    for (int k = 0; k < 10; ++k) vec[k] = base + (size_t)k * kNoAllocNp;
+    double* part = base + 10 * kNoAllocNp;
+    double* sc = part + 7 * (size_t)kNoAllocChunks;  // rho[2], alpha, omega, nrmr, nrm0
+    int* iv = reinterpret_cast<int*>(base + kNoAllocDoubles);
+    int* done = iv;
+    int* iters = iv + 1;
+    int* flagA = iv + 2;
+    int* flagB = iv + 4;
+    int* bad = iv + 6;
+    int* active = iv + 8;
+    // what must start at zero: the error flag, the per-iteration counters and
+    // the right-hand side padding (the kernels rewrite everything else)
+    NOALLOC_CUDA(cudaMemsetAsync(iv, 0, sizeof(int) * (8 + (size_t)maxit + 2), st));
+    NOALLOC_CUDA(cudaMemsetAsync(vec[7], 0, sizeof(double) * Np, st));
+    k_noalloc_check_csr<<<(n + 255) / 256, 256, 0, st>>>(rowptr, colind, n, nnz, bad);
+    NOALLOC_CUDA(cudaGetLastError());
+    int h_bad = 0;
+    NOALLOC_CUDA(cudaMemcpyAsync(&h_bad, bad, sizeof(int), cudaMemcpyDeviceToHost, st));
+    NOALLOC_CUDA(cudaStreamSynchronize(st));
+    if (h_bad) {
+        g_create_error = "bte_bicgstab_csr_noalloc: malformed CSR (row pointers or column indices)";
+        return BTE_ERR_INVALID_ARGUMENT;
+    }
+    NOALLOC_CUDA(cudaMemcpyAsync(vec[7], b, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+    bte::CsrOp op{rowptr, colind, val, vec[9], n, Np};
+    bte::BicgState bs{done, iters, flagA, flagB, sc, sc + 2, sc + 3, sc + 4, sc + 5, part, active, 1, nchunk, tol,
+                      maxit};
+    bte::BicgVecs<double> v{vec[0], vec[1], vec[2], vec[3], vec[4], vec[5], vec[6], vec[7], vec[8], Np};
+    dim3 grid(nchunk, 1);
+    bte::k_bicg_init<<<grid, bte::THREADS, 0, st>>>(op, v, bs);
+    bte::k_bicg_init_scalars<<<1, 32, 0, st>>>(bs);
+    NOALLOC_CUDA(cudaGetLastError());
+    int i = 1;
+    for (;;) {
+        int last = i;
+        for (int g = 0; g < kGroup && i <= maxit + 1; ++g, ++i) {
+            bte::k_bicg_p<<<grid, bte::THREADS, 0, st>>>(op, v, bs, i);
+            last = i;
+            if (i > maxit) break;
+            bte::k_bicg_spmv1<<<grid, bte::THREADS, 0, st>>>(op, v, bs, i);
+            bte::k_bicg_s<<<grid, bte::THREADS, 0, st>>>(op, v, bs, i);
+            bte::k_bicg_spmv2<<<grid, bte::THREADS, 0, st>>>(op, v, bs, i);
+            bte::k_bicg_x<<<grid, bte::THREADS, 0, st>>>(op, v, bs, i);
+        }
+        NOALLOC_CUDA(cudaGetLastError());
+        int h_active = 0;
+        NOALLOC_CUDA(cudaMemcpyAsync(&h_active, active + last, sizeof(int), cudaMemcpyDeviceToHost, st));
+        NOALLOC_CUDA(cudaStreamSynchronize(st));
+        if (h_active == 0 || last > maxit || i > maxit + 1) break;
+    }
+    NOALLOC_CUDA(cudaMemcpyAsync(x, vec[9], sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+    int h_state[2] = {0, 0};
+    NOALLOC_CUDA(cudaMemcpyAsync(h_state, done, 2 * sizeof(int), cudaMemcpyDeviceToHost, st));
+    NOALLOC_CUDA(cudaStreamSynchronize(st));
+    if (iterations) *iterations = h_state[1];
+    if (converged) *converged = (h_state[0] == 1 || h_state[0] == 2) ? 1 : 0;
+    return BTE_OK;
+}

@@ -629,11 +629,12 @@ static bte_status build_sweep_plan(bte_ctx* ctx) {
                 level_order(n, F, &mask[(size_t)d * n], ctx->nbr.data(), perm[d], lvl[d], lag[d]);
         });
     for (auto& th : pool) th.join();
-    std::vector<int> h_perm((size_t)ND * n), h_lag((size_t)ND * F * n), h_lvl, h_off(ND + 1, 0);
+    std::vector<int> h_perm((size_t)ND * n), h_pos((size_t)ND * n), h_lag((size_t)ND * F * n), h_lvl, h_off(ND + 1, 0);
     int lagged_dirs = 0;
     long long levels = 0;
     for (int d = 0; d < ND; ++d) {
         std::copy(perm[d].begin(), perm[d].end(), h_perm.begin() + (size_t)d * n);
+        for (int j = 0; j < n; ++j) h_pos[(size_t)d * n + perm[d][j]] = j;
         std::copy(lag[d].begin(), lag[d].end(), h_lag.begin() + (size_t)d * F * n);
         h_off[d] = (int)h_lvl.size();
         h_lvl.insert(h_lvl.end(), lvl[d].begin(), lvl[d].end());
@@ -643,8 +644,9 @@ static bte_status build_sweep_plan(bte_ctx* ctx) {
         lagged_dirs += any;
     }
     h_off[ND] = (int)h_lvl.size();
-    DevBuf d_perm, d_lag;
+    DevBuf d_perm, d_pos, d_lag;
     BTE_CUDA(upload(d_perm, h_perm, st));
+    BTE_CUDA(upload(d_pos, h_pos, st));
     BTE_CUDA(upload(d_lag, h_lag, st));
     BTE_CUDA(upload(ctx->p_lvl, h_lvl, st));
     BTE_CUDA(upload(ctx->p_lvl_off, h_off, st));
@@ -654,7 +656,7 @@ static bte_status build_sweep_plan(bte_ctx* ctx) {
     BTE_CUDA(ctx->p_nb.alloc(sizeof(int) * ND * F * n));
     BTE_CUDA(ctx->p_fc.alloc(sizeof(double) * ND * F * n));
     bte::k_sweep_layout<<<dim3((n + 255) / 256, ND), 256, 0, st>>>(
-        d_perm.as<int>(), d_lag.as<int>(), ctx->d_dg.as<double>(), ctx->d_vo.as<double>(), ctx->d_fc.as<double>(),
+        d_perm.as<int>(), d_pos.as<int>(), d_lag.as<int>(), ctx->d_dg.as<double>(), ctx->d_vo.as<double>(), ctx->d_fc.as<double>(),
         ctx->d_nbr.as<int>(), F, n, Np, ND, ctx->p_cell.as<int>(), ctx->p_dg.as<double>(), ctx->p_vo.as<double>(),
         ctx->p_nb.as<int>(), ctx->p_fc.as<double>());
     BTE_LAUNCHED();
@@ -755,6 +757,14 @@ static bte_status solve_batch_plain(bte_ctx* ctx, int b0, int nbb, const bte_opt
     return BTE_OK;
 }
 
+// Shared-memory ring of the sweep: W (a power of two) positions per band, 32 KB per block.
+static int sweep_ring(int G) {
+    int w = 4096;
+    while (w > 256 && w * std::max(G, 1) > 4096) w >>= 1;
+    return w;
+}
+static size_t sweep_smem(int G) { return sizeof(double) * (size_t)G * sweep_ring(G); }
+
 // Solve all systems of one batch by upwind sweeps (exact in one sweep when no
 // edge is lagged; otherwise Gauss-Seidel sweeps until ||R - A x|| <= inner_tol ||R||).
 static bte_status solve_batch_sweep(bte_ctx* ctx, int b0, int nbb, const bte_options& o, bte_report& rep) {
@@ -778,7 +788,7 @@ static bte_status solve_batch_sweep(bte_ctx* ctx, int b0, int nbb, const bte_opt
     // launch-shape autotuning on the first sweep of this plan (each candidate
     // computes the same x from the same inputs)
     if (!ctx->sweep_tuned) {
-        static const int cand[][2] = {{1, 128}, {2, 128}, {2, 256}, {4, 256}, {8, 256}, {8, 512}, {16, 512}};
+        static const int cand[][2] = {{1, 64}, {1, 128}, {2, 64}, {2, 128}, {2, 256}, {4, 128}, {4, 256}, {8, 256}};
         const int ncand = (int)(sizeof(cand) / sizeof(cand[0]));
         cudaEvent_t e0, e1;
         BTE_CUDA(cudaEventCreate(&e0));
@@ -787,9 +797,9 @@ static bte_status solve_batch_sweep(bte_ctx* ctx, int b0, int nbb, const bte_opt
         for (int k = 0; k < ncand; ++k) {
             const int Gk = std::max(1, std::min(cand[k][0], nbb));
             BTE_CUDA(cudaEventRecord(e0, st));
-            bte::k_sweep<<<dim3((nbb + Gk - 1) / Gk, ctx->n_dir), cand[k][1], 0, st>>>(
+            bte::k_sweep<<<dim3((nbb + Gk - 1) / Gk, ctx->n_dir), cand[k][1], sweep_smem(Gk), st>>>(
                 sp, ctx->d_kb.as<double>(), ctx->p_invd.as<double>(), ctx->w_b.as<double>(), ctx->e_curr,
-                ctx->e_prev, 1, Gk, nbb, b0, ctx->n_dir, ctx->Np);
+                ctx->e_prev, 1, Gk, sweep_ring(Gk), nbb, b0, ctx->n_dir, ctx->Np);
             BTE_LAUNCHED();
             BTE_CUDA(cudaEventRecord(e1, st));
             BTE_CUDA(cudaEventSynchronize(e1));
@@ -810,9 +820,9 @@ static bte_status solve_batch_sweep(bte_ctx* ctx, int b0, int nbb, const bte_opt
     int sweeps = 0;
     for (;;) {
         BTE_LAUNCH(KK_SWEEP, -1, sweep_bytes, 0,
-                   bte::k_sweep<<<sgrid, ctx->sweep_threads, 0, st>>>(
+                   bte::k_sweep<<<sgrid, ctx->sweep_threads, sweep_smem(G), st>>>(
                        sp, ctx->d_kb.as<double>(), ctx->p_invd.as<double>(), ctx->w_b.as<double>(), ctx->e_curr,
-                       ctx->e_prev, sweeps == 0, G, nbb, b0, ctx->n_dir, ctx->Np));
+                       ctx->e_prev, sweeps == 0, G, sweep_ring(G), nbb, b0, ctx->n_dir, ctx->Np));
         ++sweeps;
         if (ctx->plan_lagged_dirs == 0) break;
         BTE_CUDA(ctx->p_part.alloc(sizeof(double) * 2 * (size_t)S * ctx->nchunk));

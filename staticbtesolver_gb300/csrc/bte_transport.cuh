@@ -168,8 +168,9 @@ __global__ void __launch_bounds__(THREADS) k_reduce(const double* __restrict__ e
         const double* ec = e_curr + (size_t)b * n_dir * Np + c;
         const double* ep = e_prev + (size_t)b * n_dir * Np + c;
         double e0 = 0.0;
+#pragma unroll 8
         for (int d = 0; d < n_dir; ++d) {
-            const double a = ec[(size_t)d * Np], p = ep[(size_t)d * Np];
+            const double a = __ldcs(ec + (size_t)d * Np), p = __ldcs(ep + (size_t)d * Np);
             e0 += a * omega[d];
             const double df = a - p;
             m[0] = fma(df, df, m[0]);
@@ -261,9 +262,10 @@ namespace bte {
 // residual test passes.
 //
 // Sweep-ordered arrays, direction-major, position j in level order:
-//   sw_cell[d][j], sw_dg[d][j], sw_vo[d][j], sw_nb[d][f][j] (upstream cell,
-//   -1 none, -2-cell for a lagged edge), sw_fc[d][f][j]; levels
-//   lvl[lvl_off[d] .. lvl_off[d+1]] are start positions (the last entry is n).
+//   sw_cell[d][j], sw_dg[d][j], sw_vo[d][j], sw_fc[d][f][j], and sw_nb[d][f][j]
+//   = the upstream cell's POSITION in this direction's order (-1 none,
+//   -2-position for a lagged edge); levels lvl[lvl_off[d] .. lvl_off[d+1]] are
+//   start positions (the last entry is n).
 struct SweepPlan {
     const int* cell;
     const double* dg;
@@ -319,16 +321,23 @@ __device__ __forceinline__ void sweep_load(const SweepPlan& sp, const double* __
 // One block sweeps direction blockIdx.y for bands b0 + blockIdx.x * G .. + G - 1.
 // x and x_old are e_curr / e_prev ([band][n_dir][Np]).  Each thread's first
 // item of the next two levels is loaded ahead (everything but the upstream
-// values), so after a level barrier only the x[u] reads are on the critical path.
+// values), and the block keeps its last W solved positions (for its G bands)
+// in a shared-memory ring, so after a level barrier the upstream values come
+// from shared memory.  A position p is still in the ring during the level
+// [j0, j1) whenever p >= j1 - W: no position written in this level maps to
+// its slot.  W is a power of two.  Older and lagged upstream values are read
+// from global memory.
 __global__ void __launch_bounds__(512) k_sweep(SweepPlan sp, const double* __restrict__ kb,
                                                const double* __restrict__ invD, const double* __restrict__ rhs,
                                                double* x, const double* __restrict__ x_old, int first_sweep,
-                                               int G, int nbb, int b0, int n_dir, size_t Np) {
+                                               int G, int W, int nbb, int b0, int n_dir, size_t Np) {
+    extern __shared__ double ring[];  // [G][W]
     const int d = blockIdx.y;
     const int g0 = blockIdx.x * G;
     const int gn = min(G, nbb - g0);
     if (gn <= 0) return;
     const int L0 = sp.lvl_off[d], L1 = sp.lvl_off[d + 1] - 1;  // levels L0 .. L1-1
+    const int* cell_d = sp.cell + (size_t)d * sp.n;
     SweepItem p1, p2;  // this thread's first item of levels l and l+1
     bool h1 = false, h2 = false;
     auto pre = [&](int l, SweepItem& dst) -> bool {
@@ -343,21 +352,31 @@ __global__ void __launch_bounds__(512) k_sweep(SweepPlan sp, const double* __res
     for (int l = L0; l < L1; ++l) {
         const int j0 = sp.lvl[l], j1 = sp.lvl[l + 1];
         const int items = (j1 - j0) * gn;
+        const int keep = j1 - W;  // oldest position still readable from the ring
         for (int it = threadIdx.x; it < items; it += blockDim.x) {
             SweepItem cur;
+            const int j = j0 + it / gn;
+            const int bl = it % gn;
             if (it == threadIdx.x && h1) cur = p1;
-            else sweep_load(sp, invD, rhs, d, j0 + it / gn, g0 + it % gn, b0, nbb, n_dir, Np, cur);
+            else sweep_load(sp, invD, rhs, d, j, g0 + bl, b0, nbb, n_dir, Np, cur);
             double* xb = x + ((size_t)cur.b * n_dir + d) * Np;
-            const double* xo = x_old + ((size_t)cur.b * n_dir + d) * Np;
+            double* rg = ring + (size_t)bl * W;
             double off = 0.0;
 #pragma unroll
             for (int f = 0; f < 4; ++f) {
                 const int u = cur.u[f];
                 if (u == -1) continue;
-                const double xu = u >= 0 ? xb[u] : (first_sweep ? xo[-u - 2] : xb[-u - 2]);
+                double xu;
+                if (u >= 0) xu = u >= keep ? rg[u & (W - 1)] : xb[cell_d[u]];
+                else {  // lagged (u = -2 - position): previous sweep's value (or the previous outer iterate)
+                    const int cu = cell_d[-u - 2];
+                    xu = first_sweep ? x_old[((size_t)cur.b * n_dir + d) * Np + cu] : xb[cu];
+                }
                 off = fma(cur.cf[f], xu, off);
             }
-            xb[cur.c] = fma(-kb[cur.b], off, cur.r) * cur.invd;
+            const double v = fma(-kb[cur.b], off, cur.r) * cur.invd;
+            xb[cur.c] = v;
+            rg[j & (W - 1)] = v;
         }
         p1 = p2;
         h1 = h2;
@@ -419,7 +438,8 @@ __global__ void k_inflow_mask(const double* __restrict__ fc, int F, int n, size_
 }
 
 // Gather the per-direction geometry into level order.
-__global__ void k_sweep_layout(const int* __restrict__ perm, const int* __restrict__ lagged,  // [n_dir][F][n] 0/1
+__global__ void k_sweep_layout(const int* __restrict__ perm, const int* __restrict__ pos,  // pos [n_dir][n]: cell -> position
+                               const int* __restrict__ lagged,  // [n_dir][F][n] 0/1
                                const double* __restrict__ dg, const double* __restrict__ vo,
                                const double* __restrict__ fc, const int* __restrict__ nbr,  // nbr [n][F]
                                int F, int n, size_t Np, int n_dir, int* cell, double* sdg, double* svo, int* snb,
@@ -438,8 +458,8 @@ __global__ void k_sweep_layout(const int* __restrict__ perm, const int* __restri
         sfc[q] = v;
         if (v == 0.0) snb[q] = -1;
         else {
-            const int u = nbr[(size_t)c * F + f];
-            snb[q] = lagged[((size_t)d * F + f) * n + c] ? -2 - u : u;
+            const int pu = pos[(size_t)d * n + nbr[(size_t)c * F + f]];
+            snb[q] = lagged[((size_t)d * F + f) * n + c] ? -2 - pu : pu;
         }
     }
 }

@@ -60,7 +60,7 @@ def parse_args():
     ap.add_argument("--workload", default="square20k")
     ap.add_argument("--form", default="sweep", choices=["plain", "mixed", "sweep"])
     ap.add_argument("--plain-iters", type=int, default=3,
-                    help="outer iterations of the plain FP64 BiCGSTAB form timed for the comparison")
+                    help="outer iterations of the plain FP64 and mixed BiCGSTAB forms timed for the comparison")
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-profile", action="store_true", help="skip the profiled solve (roofline)")
@@ -273,22 +273,26 @@ def run_ours(args, rank, world, local):
         e2e = max_over_ranks(statistics.mean(e2e_t), world) if e2e_t else None
         ctx2.close()
 
-        # plain FP64 form (the reference GPU algorithm, batched): a bounded number
-        # of outer iterations, scaled by the outer-iteration count of the solve
-        plain = None
-        if form != S.FORM_PLAIN and args.plain_iters > 0:
-            pkw = dict(solve_kw, form=S.FORM_PLAIN, max_iter=args.plain_iters)
+        # plain FP64 form (the reference GPU algorithm, batched) and the mixed
+        # FP32/FP64 form: a bounded number of outer iterations each, scaled by
+        # the outer-iteration count of the solve (the mixed form's warm start
+        # helps more in later iterations, so its scaled time is an upper bound)
+        def compare(fm):
+            pkw = dict(solve_kw, form=fm, max_iter=args.plain_iters)
             ctx.solve(**pkw)  # warm
             st_p, rep_p = ctx.solve(**pkw)
             per_outer = rep_p.ms_total / 1e3 / rep_p.n_iter
             ctx.solve(profile=True, **pkw)
             pstats = ctx.kernel_stats()
-            plain = {"s_per_outer_iteration": per_outer, "outer_iterations_timed": rep_p.n_iter,
-                     "s_extrapolated": per_outer * last["n_iter"],
-                     "inner_iterations_per_system": rep_p.inner_iterations / max(rep_p.inner_solves, 1),
-                     "kernels": {k: {"launches": v["launches"], "ms": round(v["ms"], 3),
-                                     "GB/s": round(v["bytes"] / (v["ms"] / 1e3) / 1e9, 1) if v["ms"] > 0 else None}
-                                 for k, v in pstats.items() if v["launches"]}}
+            return {"s_per_outer_iteration": per_outer, "outer_iterations_timed": rep_p.n_iter,
+                    "s_extrapolated": per_outer * last["n_iter"],
+                    "inner_iterations_per_system": rep_p.inner_iterations / max(rep_p.inner_solves, 1),
+                    "kernels": {k: {"launches": v["launches"], "ms": round(v["ms"], 3),
+                                    "GB/s": round(v["bytes"] / (v["ms"] / 1e3) / 1e9, 1) if v["ms"] > 0 else None}
+                                for k, v in pstats.items() if v["launches"]}}
+
+        plain = compare(S.FORM_PLAIN) if form != S.FORM_PLAIN and args.plain_iters > 0 else None
+        mixed = compare(S.FORM_MIXED) if form != S.FORM_MIXED and args.plain_iters > 0 else None
 
         # profiled solve (outside the timed region) for the per-kernel roofline
         if args.no_profile:
@@ -334,6 +338,7 @@ def run_ours(args, rank, world, local):
                        "replicas": world, "q_left": float(q[0]), "q_right": float(q[2]),
                        "T_min": float(T.min()), "T_max": float(T.max()), "kernels": per_kernel,
                        "plain_fp64_form": plain,
+                       "mixed_fp32_fp64_form": mixed,
                        "sweep_shape": {"bands_per_block": last["sweep_group"], "threads": last["sweep_threads"]},
                        "speedup_vs_plain_fp64": (plain["s_extrapolated"] / t_step) if plain else None},
             "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": round(achieved, 1), "peak": peak,

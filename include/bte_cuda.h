@@ -41,10 +41,13 @@ typedef enum bte_form {
      * the reference GPU inner solve (src/bicgstab.hpp:138-300), all systems of
      * an outer iteration batched into one launch per BiCGSTAB phase. */
     BTE_FORM_PLAIN = 0,
-    /* FP32 BiCGSTAB inside FP64 iterative refinement: the FP64 residual
-     * b - A x is recomputed after every FP32 cycle and the solve stops when
-     * ||b - A x|| <= inner_tol * ||b||, the reference's criterion for x0 = 0.
-     * The inner iterate starts from the previous outer iterate. */
+    /* FP32 BiCGSTAB inside FP64 iterative refinement: x starts from the
+     * previous outer iterate; each cycle computes the FP64 residual b - A x,
+     * retires the systems with ||b - A x|| <= inner_tol * ||b|| (the
+     * reference's criterion for x0 = 0), solves A dx = r for the others with
+     * right-Jacobi BiCGSTAB in FP32 (relative tolerance 1e-4, on geometry
+     * scaled per direction by 1 / mean(V Omega_d)) and adds dx in FP64; at
+     * most 30 cycles. */
     BTE_FORM_MIXED = 1,
     /* FP64 upwind sweep: each system is lower triangular in the topological
      * order of its direction's upwind graph, so one level-scheduled forward

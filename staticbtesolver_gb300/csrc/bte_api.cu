@@ -98,6 +98,10 @@ struct bte_ctx {
     double* h_pinned = nullptr;  // [4]
     int* h_pinned_i = nullptr;   // [4]
     std::vector<int> h_done, h_iters;
+    // mixed form: scaled FP32 geometry and FP32 work vectors
+    bool mixed_ready = false;
+    DevBuf d_dg32, d_vo32, d_fc32, d_kb32, d_kappa;
+    DevBuf x_r, x_rw, x_p, x_ph, x_q, x_z, x_t, x_b, x_invD, x_dx, m_part, m_skip, m_active;
     // upwind sweep plan (form BTE_FORM_SWEEP)
     bool plan_ready = false;
     int plan_lagged_dirs = 0;
@@ -551,7 +555,40 @@ static bte_status setup(bte_ctx* ctx, int batch_systems) {
     ctx->h_done.resize(S);
     ctx->h_iters.resize(S);
     ctx->plan_ready = false;
+    ctx->mixed_ready = false;
     ctx->dirty = false;
+    return BTE_OK;
+}
+
+// FP32 geometry for the mixed form, scaled per direction by 1 / mean(V Omega_d).
+static bte_status setup_mixed(bte_ctx* ctx) {
+    const int n = ctx->n, F = ctx->F, ND = ctx->n_dir, NB = ctx->n_band;
+    const size_t Np = ctx->Np;
+    cudaStream_t st = ctx->stream;
+    double vmean = 0;
+    for (double v : ctx->volume) vmean += v;
+    vmean /= n;
+    std::vector<double> kappa(ND);
+    for (int d = 0; d < ND; ++d) kappa[d] = 1.0 / (ctx->dim > 1 ? vmean * ctx->omega[d] : vmean);
+    std::vector<float> kb32(NB);
+    for (int b = 0; b < NB; ++b) kb32[b] = (float)(ctx->vg[b] * ctx->tau[b]);
+    BTE_CUDA(upload(ctx->d_kappa, kappa, st));
+    BTE_CUDA(upload(ctx->d_kb32, kb32, st));
+    BTE_CUDA(ctx->d_dg32.alloc(sizeof(float) * ND * Np));
+    BTE_CUDA(ctx->d_vo32.alloc(sizeof(float) * ND * Np));
+    BTE_CUDA(ctx->d_fc32.alloc(sizeof(float) * ND * F * Np));
+    bte::k_geometry32<<<dim3((unsigned)((Np + 255) / 256), ND), 256, 0, st>>>(
+        ctx->d_dg.as<double>(), ctx->d_vo.as<double>(), ctx->d_fc.as<double>(), ctx->d_kappa.as<double>(), n, F, Np,
+        ctx->d_dg32.as<float>(), ctx->d_vo32.as<float>(), ctx->d_fc32.as<float>());
+    BTE_LAUNCHED();
+    const size_t S = (size_t)ctx->nbb * ND;
+    for (DevBuf* b : {&ctx->x_r, &ctx->x_rw, &ctx->x_p, &ctx->x_ph, &ctx->x_q, &ctx->x_z, &ctx->x_t, &ctx->x_b,
+                      &ctx->x_invD, &ctx->x_dx})
+        BTE_CUDA(b->alloc(sizeof(float) * S * Np));
+    BTE_CUDA(ctx->m_part.alloc(sizeof(double) * 2 * S * ctx->nchunk));
+    BTE_CUDA(ctx->m_skip.alloc(sizeof(int) * S));
+    BTE_CUDA(ctx->m_active.alloc(sizeof(int)));
+    ctx->mixed_ready = true;
     return BTE_OK;
 }
 
@@ -721,7 +758,7 @@ static bte_status solve_batch_plain(bte_ctx* ctx, int b0, int nbb, const bte_opt
                             ctx->w_ph.as<double>(), ctx->w_q.as<double>(), ctx->w_z.as<double>(),
                             ctx->w_t.as<double>(), ctx->w_b.as<double>(), ctx->w_invD.as<double>(), ctx->Np};
     BTE_LAUNCH(KK_INIT, -1, S * N * 7 * w + geo / 2, 0, bte::k_bicg_init<<<grid, bte::THREADS, 0, st>>>(op, v, bs));
-    BTE_LAUNCH(KK_INIT, -1, 0, 0, bte::k_bicg_init_scalars<<<(S + 127) / 128, 128, 0, st>>>(bs));
+    BTE_LAUNCH(KK_INIT, -1, 0, 0, bte::k_bicg_init_scalars<<<(S + 127) / 128, 128, 0, st>>>(bs, nullptr));
     int i = 1;
     for (;;) {
         int last = i;
@@ -752,6 +789,106 @@ static bte_status solve_batch_plain(bte_ctx* ctx, int b0, int nbb, const bte_opt
     for (int y = 0; y < S; ++y) {
         rep.inner_iterations += ctx->h_iters[y];
         if (ctx->h_done[y] == 3 || ctx->h_done[y] == 0) ++rep.inner_unconverged;
+    }
+    rep.inner_solves += S;
+    return BTE_OK;
+}
+
+// Mixed form for one batch: x starts from the previous outer iterate; each
+// refinement cycle computes the FP64 residual, stops the systems that meet
+// ||b - A x|| <= inner_tol ||b||, solves A dx = r for the others with FP32
+// BiCGSTAB (relative tolerance 1e-4) and adds dx in FP64.
+static bte_status solve_batch_mixed(bte_ctx* ctx, int b0, int nbb, const bte_options& o, bte_report& rep) {
+    cudaStream_t st = ctx->stream;
+    const int S = nbb * ctx->n_dir;
+    const double N = ctx->n;
+    bte::FaceFluxOp op{ctx->d_dg.as<double>(), ctx->d_vo.as<double>(), ctx->d_fc.as<double>(),
+                       ctx->d_nb.as<int>(), ctx->d_kb.as<double>(), ctx->e_curr, ctx->F, nbb, b0,
+                       ctx->n_dir, ctx->Np};
+    bte::FaceFluxOp32 op32{ctx->d_dg32.as<float>(), ctx->d_vo32.as<float>(), ctx->d_fc32.as<float>(),
+                           ctx->d_nb.as<int>(), ctx->d_kb32.as<float>(), ctx->x_dx.as<float>(), ctx->F, nbb, b0,
+                           ctx->n_dir, ctx->Np};
+    bte::Boundary bd{ctx->d_bptr.as<int>(), ctx->d_bf_cell.as<int>(), ctx->d_bf_kind.as<int>(),
+                     ctx->d_bf_bc.as<int>(), ctx->d_bf_diff.as<int>(), ctx->d_cin.as<double>(),
+                     ctx->d_eiso.as<double>(), ctx->d_mirror.as<int>(), ctx->d_ediff.as<double>(),
+                     ctx->nbf, std::max(ctx->n_bc, 1)};
+    const double geo = N * ((ctx->F + 2) * 8.0 + ctx->F * 4.0) * std::min(S, ctx->n_dir);
+    const double geo32 = N * ((ctx->F + 2) * 4.0 + ctx->F * 4.0) * std::min(S, ctx->n_dir);
+    dim3 grid(ctx->nchunk, S);
+    BTE_LAUNCH(KK_RHS, -1, S * N * 16.0 + geo / 2, 0,
+               bte::k_rhs<<<grid, bte::THREADS, 0, st>>>(op, bd, ctx->d_ebar.as<double>(), ctx->e_prev,
+                                                         ctx->w_b.as<double>(), ctx->n));
+    BTE_LAUNCH(KK_INIT, -1, S * N * 16.0, 0, bte::k_mixed_start<<<grid, bte::THREADS, 0, st>>>(op, ctx->e_prev));
+    const int maxit = o.inner_maxit;
+    if (ctx->active_cap < maxit + 2) {
+        BTE_CUDA(ctx->s_active.alloc(sizeof(int) * (maxit + 2)));
+        ctx->active_cap = maxit + 2;
+    }
+    bte::BicgState bs{ctx->s_done.as<int>(), ctx->s_iters.as<int>(), ctx->s_flagA.as<int>(), ctx->s_flagB.as<int>(),
+                      ctx->s_rho.as<double>(), ctx->s_alpha.as<double>(), ctx->s_omega.as<double>(),
+                      ctx->s_nrmr.as<double>(), ctx->s_nrm0.as<double>(), ctx->s_part.as<double>(),
+                      ctx->s_active.as<int>(), S, ctx->nchunk, 1e-4, maxit};
+    bte::BicgVecs<float> v{ctx->x_r.as<float>(), ctx->x_rw.as<float>(), ctx->x_p.as<float>(),
+                           ctx->x_ph.as<float>(), ctx->x_q.as<float>(), ctx->x_z.as<float>(),
+                           ctx->x_t.as<float>(), ctx->x_b.as<float>(), ctx->x_invD.as<float>(), ctx->Np};
+    const double w = 4.0;
+    const int max_cycles = 30;
+    int cycle = 0;
+    for (; cycle < max_cycles; ++cycle) {
+        BTE_CUDA(cudaMemsetAsync(ctx->m_active.p, 0, sizeof(int), st));
+        BTE_LAUNCH(KK_SWEEP_RES, -1, S * N * (8.0 * 2 + 4.0) + geo, 0,
+                   bte::k_mixed_residual<<<grid, bte::THREADS, 0, st>>>(op, ctx->w_b.as<double>(),
+                                                                        ctx->d_kappa.as<double>(), ctx->x_b.as<float>(),
+                                                                        ctx->m_part.as<double>(), ctx->nchunk, ctx->n));
+        bte::k_mixed_check<<<(S + 127) / 128, 128, 0, st>>>(ctx->m_part.as<double>(), S, ctx->nchunk, o.inner_tol,
+                                                             ctx->m_skip.as<int>(), ctx->m_active.as<int>());
+        BTE_LAUNCHED();
+        BTE_CUDA(cudaMemcpyAsync(ctx->h_pinned_i + 1, ctx->m_active.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+        BTE_CUDA(cudaStreamSynchronize(st));
+        if (ctx->h_pinned_i[1] == 0) break;
+        BTE_CUDA(cudaMemsetAsync(ctx->s_active.p, 0, sizeof(int) * (maxit + 2), st));
+        BTE_LAUNCH(KK_INIT, -1, S * N * 7 * w + geo32 / 2, 0,
+                   bte::k_bicg_init<<<grid, bte::THREADS, 0, st>>>(op32, v, bs));
+        BTE_LAUNCH(KK_INIT, -1, 0, 0,
+                   bte::k_bicg_init_scalars<<<(S + 127) / 128, 128, 0, st>>>(bs, ctx->m_skip.as<int>()));
+        int i = 1;
+        for (;;) {
+            int last = i;
+            for (int g = 0; g < kGroup && i <= maxit + 1; ++g, ++i) {
+                BTE_LAUNCH(KK_P, i, 0, N * 6 * w, bte::k_bicg_p<<<grid, bte::THREADS, 0, st>>>(op32, v, bs, i));
+                last = i;
+                if (i > maxit) break;
+                BTE_LAUNCH(KK_SPMV1, i, geo32, N * 3 * w,
+                           bte::k_bicg_spmv1<<<grid, bte::THREADS, 0, st>>>(op32, v, bs, i));
+                BTE_LAUNCH(KK_S, i, 0, N * 5 * w, bte::k_bicg_s<<<grid, bte::THREADS, 0, st>>>(op32, v, bs, i));
+                BTE_LAUNCH(KK_SPMV2, i, geo32, N * 3 * w,
+                           bte::k_bicg_spmv2<<<grid, bte::THREADS, 0, st>>>(op32, v, bs, i));
+                BTE_LAUNCH(KK_X, i, 0, N * 8 * w, bte::k_bicg_x<<<grid, bte::THREADS, 0, st>>>(op32, v, bs, i));
+            }
+            BTE_CUDA(cudaMemcpyAsync(ctx->h_pinned_i, ctx->s_active.as<int>() + last, sizeof(int),
+                                     cudaMemcpyDeviceToHost, st));
+            BTE_CUDA(cudaStreamSynchronize(st));
+            if (ctx->h_pinned_i[0] == 0 || last > maxit || i > maxit + 1) break;
+        }
+        if (ctx->profile) {
+            ctx->h_active.resize(maxit + 2);
+            BTE_CUDA(cudaMemcpyAsync(ctx->h_active.data(), ctx->s_active.p, sizeof(int) * (maxit + 2),
+                                     cudaMemcpyDeviceToHost, st));
+            BTE_CUDA(cudaStreamSynchronize(st));
+            prof_resolve(ctx, ctx->h_active.data(), maxit + 2);
+        }
+        BTE_LAUNCH(KK_X, -1, S * N * (8.0 * 2 + 4.0), 0,
+                   bte::k_mixed_update<<<grid, bte::THREADS, 0, st>>>(op, ctx->x_dx.as<float>(),
+                                                                      ctx->m_skip.as<int>()));
+        BTE_CUDA(cudaMemcpyAsync(ctx->h_iters.data(), ctx->s_iters.p, sizeof(int) * S, cudaMemcpyDeviceToHost, st));
+        BTE_CUDA(cudaStreamSynchronize(st));
+        for (int y = 0; y < S; ++y) rep.inner_iterations += ctx->h_iters[y];
+        ++rep.refinements;
+    }
+    if (cycle == max_cycles) rep.inner_unconverged += ctx->h_pinned_i[1];
+    if (ctx->profile) {
+        BTE_CUDA(cudaStreamSynchronize(st));
+        prof_resolve(ctx, nullptr, 0);
     }
     rep.inner_solves += S;
     return BTE_OK;
@@ -860,8 +997,8 @@ extern "C" bte_status bte_solve(bte_ctx* ctx, const bte_options* opts, bte_repor
     else bte_default_options(&o);
     if (o.max_iter < 0 || o.inner_maxit <= 0 || !(o.inner_tol > 0))
         return fail(ctx, BTE_ERR_INVALID_ARGUMENT, "bte_solve: bad options");
-    if (o.form != BTE_FORM_PLAIN && o.form != BTE_FORM_SWEEP)
-        return fail(ctx, BTE_ERR_INVALID_ARGUMENT, "bte_solve: form not available in this build");
+    if (o.form != BTE_FORM_PLAIN && o.form != BTE_FORM_SWEEP && o.form != BTE_FORM_MIXED)
+        return fail(ctx, BTE_ERR_INVALID_ARGUMENT, "bte_solve: unknown form");
     if (ctx->dim == 1 && ctx->F != 2) return fail(ctx, BTE_ERR_INVALID_ARGUMENT, "1D mesh needs 2 faces");
     BTE_CUDA(cudaSetDevice(ctx->device));
     bte_report rep;
@@ -880,6 +1017,10 @@ extern "C" bte_status bte_solve(bte_ctx* ctx, const bte_options* opts, bte_repor
     }
     if (o.form == BTE_FORM_SWEEP && !ctx->plan_ready) {
         bte_status s = build_sweep_plan(ctx);
+        if (s != BTE_OK) return s;
+    }
+    if (o.form == BTE_FORM_MIXED && !ctx->mixed_ready) {
+        bte_status s = setup_mixed(ctx);
         if (s != BTE_OK) return s;
     }
     cudaStream_t st = ctx->stream;
@@ -910,8 +1051,9 @@ extern "C" bte_status bte_solve(bte_ctx* ctx, const bte_options* opts, bte_repor
         BTE_CUDA(cudaEventRecord(ev[1], st));
         for (int b0 = 0; b0 < NB; b0 += ctx->nbb) {
             const int nbb = std::min(ctx->nbb, NB - b0);
-            bte_status s = o.form == BTE_FORM_SWEEP ? solve_batch_sweep(ctx, b0, nbb, o, rep)
-                                                    : solve_batch_plain(ctx, b0, nbb, o, rep);
+            bte_status s = o.form == BTE_FORM_SWEEP   ? solve_batch_sweep(ctx, b0, nbb, o, rep)
+                           : o.form == BTE_FORM_MIXED ? solve_batch_mixed(ctx, b0, nbb, o, rep)
+                                                      : solve_batch_plain(ctx, b0, nbb, o, rep);
             if (s != BTE_OK) return s;
         }
         BTE_CUDA(cudaEventRecord(ev[2], st));
@@ -1099,7 +1241,7 @@ bte_status bte_bicgstab_csr(int n, const int* rowptr, const int* colind, const d
     dim3 grid(nchunk, 1);
     bte::k_bicg_init<<<grid, bte::THREADS, 0, st>>>(op, v, bs);
     BTE_LAUNCHED();
-    bte::k_bicg_init_scalars<<<1, 32, 0, st>>>(bs);
+    bte::k_bicg_init_scalars<<<1, 32, 0, st>>>(bs, nullptr);
     BTE_LAUNCHED();
     int i = 1;
     for (;;) {
@@ -1261,7 +1403,7 @@ extern "C" bte_status bte_bicgstab_csr_noalloc(int n, const int* rowptr, const i
     bte::BicgVecs<double> v{vec[0], vec[1], vec[2], vec[3], vec[4], vec[5], vec[6], vec[7], vec[8], Np};
     dim3 grid(nchunk, 1);
     bte::k_bicg_init<<<grid, bte::THREADS, 0, st>>>(op, v, bs);
-    bte::k_bicg_init_scalars<<<1, 32, 0, st>>>(bs);
+    bte::k_bicg_init_scalars<<<1, 32, 0, st>>>(bs, nullptr);
     NOALLOC_CUDA(cudaGetLastError());
     int i = 1;
     for (;;) {

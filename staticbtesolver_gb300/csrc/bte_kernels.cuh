@@ -155,22 +155,58 @@ struct CsrOp {
 #define BTE_CELL_LOOP(c)                                                     \
     for (int _k = 0, c = blockIdx.x * CH + threadIdx.x; _k < CPT; ++_k, c += THREADS)
 
+// FP32 counterpart of FaceFluxOp for the mixed form: per-direction geometry
+// stored in FP32 and pre-scaled by kappa_d = 1 / mean(V Omega_d), so the
+// scaled operator's entries are O(1..1e3) and no FP32 product under- or
+// overflows.  The unknown is the batch-local correction dx[y][Np].
+struct FaceFluxOp32 {
+    const float* dg;
+    const float* vo;
+    const float* fc;
+    const int* nb;
+    const float* kb;
+    float* dx;
+    int F, nbb, b0, n_dir;
+    size_t Np;
+    __device__ __forceinline__ void bd(int y, int& b, int& d) const {
+        d = y / nbb;
+        b = b0 + y % nbb;
+    }
+    __device__ __forceinline__ float* x_of(int y) const { return dx + (size_t)y * Np; }
+    __device__ __forceinline__ float inv_diag(int y, int c) const {
+        int b, d;
+        bd(y, b, d);
+        return 1.0f / fmaf(kb[b], dg[(size_t)d * Np + c], vo[(size_t)d * Np + c]);
+    }
+    template <typename T>
+    __device__ __forceinline__ T apply(int y, int c, const T* __restrict__ xs) const {
+        int b, d;
+        bd(y, b, d);
+        const float k = kb[b];
+        const size_t dc = (size_t)d * Np + c;
+        const float acc = fmaf(k, dg[dc], vo[dc]) * (float)xs[c];
+        float off = 0.0f;
+        for (int f = 0; f < F; ++f) off = fmaf(fc[((size_t)d * F + f) * Np + c], (float)xs[nb[(size_t)f * Np + c]], off);
+        return (T)fmaf(k, off, acc);
+    }
+};
+
 // K0: x = 0, r = p = r_hat = b, q = 0, invD; partial ||b||^2 (src/bicgstab.hpp:146-162).
-template <typename Op>
-__global__ void __launch_bounds__(THREADS) k_bicg_init(Op op, BicgVecs<double> v, BicgState st) {
+template <typename Op, typename T>
+__global__ void __launch_bounds__(THREADS) k_bicg_init(Op op, BicgVecs<T> v, BicgState st) {
     __shared__ double sm[2][NWARP];
     const int y = blockIdx.y;
     const size_t o = (size_t)y * v.Np;
-    double* x = op.x_of(y);
-    double acc[2] = {0, 0};
+    T* x = op.x_of(y);
+    T acc_t = 0;
     BTE_CELL_LOOP(c) {
-        double bb = v.b[o + c];
-        v.invD[o + c] = op.inv_diag(y, c);
-        v.r[o + c] = bb; v.p[o + c] = bb; v.rw[o + c] = bb; v.q[o + c] = 0.0;
-        x[c] = 0.0;
-        acc[0] = fma(bb, bb, acc[0]);
+        const T bb = v.b[o + c];
+        v.invD[o + c] = (T)op.inv_diag(y, c);
+        v.r[o + c] = bb; v.p[o + c] = bb; v.rw[o + c] = bb; v.q[o + c] = 0;
+        x[c] = 0;
+        acc_t = fma(bb, bb, acc_t);
     }
-    acc[1] = acc[0];
+    double acc[2] = {(double)acc_t, (double)acc_t};
     block_sum<2>(acc, sm);
     if (threadIdx.x == 0) {
         st.P(PK_RR0, y)[blockIdx.x] = acc[0];
@@ -178,8 +214,9 @@ __global__ void __launch_bounds__(THREADS) k_bicg_init(Op op, BicgVecs<double> v
     }
 }
 
-// One thread per system: scalars after K0.
-__global__ void k_bicg_init_scalars(BicgState st) {
+// One thread per system: scalars after K0.  skip[y] != 0 (optional) marks a
+// system that needs no solve this time (done = 4).
+__global__ void k_bicg_init_scalars(BicgState st, const int* skip) {
     int y = blockIdx.x * blockDim.x + threadIdx.x;
     if (y >= st.S) return;
     double n0 = sqrt(sum_parts(st.P(PK_RR0, y), st.nchunk));
@@ -187,36 +224,37 @@ __global__ void k_bicg_init_scalars(BicgState st) {
     st.nrmr[y] = n0;
     st.rho[y] = 1.0; st.rho[st.S + y] = 1.0;
     st.alpha[y] = 1.0; st.omega[y] = 1.0;
-    st.done[y] = 0; st.iters[y] = 0;
+    st.done[y] = (skip && skip[y]) ? 4 : 0;
+    st.iters[y] = 0;
     st.flagA[y] = st.flagA[st.S + y] = 0;
     st.flagB[y] = st.flagB[st.S + y] = 0;
 }
 
 // Breakdown restart on this block's chunk (src/bicgstab.hpp:170-179, :224-234):
 // x = q = p = 0, r = b, r_hat = 6.8 b + 0.6; partial r_hat.r for the next rho.
-template <typename Op>
-__device__ __forceinline__ void bicg_restart_chunk(const Op& op, const BicgVecs<double>& v,
-                                                   const BicgState& st, int y, int par,
-                                                   double (*sm)[NWARP]) {
+template <typename Op, typename T>
+__device__ __forceinline__ void bicg_restart_chunk(const Op& op, const BicgVecs<T>& v, const BicgState& st, int y,
+                                                   int par, double (*sm)[NWARP]) {
     const size_t o = (size_t)y * v.Np;
-    double* x = op.x_of(y);
-    double acc[1] = {0};
+    T* x = op.x_of(y);
+    T acc_t = 0;
     BTE_CELL_LOOP(c) {
         // Padded cells get r_hat = 0.6 but keep r = p = q = 0, so they add
         // nothing to any dot product.
-        double bb = v.b[o + c];
-        double rh = bb * 6.8 + 0.6;
-        x[c] = 0.0; v.q[o + c] = 0.0; v.p[o + c] = 0.0; v.r[o + c] = bb;
+        const T bb = v.b[o + c];
+        const T rh = bb * (T)6.8 + (T)0.6;
+        x[c] = 0; v.q[o + c] = 0; v.p[o + c] = 0; v.r[o + c] = bb;
         v.rw[o + c] = rh;
-        acc[0] = fma(rh, bb, acc[0]);
+        acc_t = fma(rh, bb, acc_t);
     }
+    double acc[1] = {(double)acc_t};
     block_sum<1>(acc, sm);
     if (threadIdx.x == 0) st.P(par ? PK_RWR1 : PK_RWR0, y)[blockIdx.x] = acc[0];
 }
 
 // K1 (iteration i): convergence bookkeeping, rho, beta; p = r + beta (p - omega q); ph = M p.
-template <typename Op>
-__global__ void __launch_bounds__(THREADS) k_bicg_p(Op op, BicgVecs<double> v, BicgState st, int i) {
+template <typename Op, typename T>
+__global__ void __launch_bounds__(THREADS) k_bicg_p(Op op, BicgVecs<T> v, BicgState st, int i) {
     __shared__ double sm[2][NWARP];
     const int y = blockIdx.y;
     if (st.done[y]) return;
@@ -252,7 +290,7 @@ __global__ void __launch_bounds__(THREADS) k_bicg_p(Op op, BicgVecs<double> v, B
         return;
     }
     const double beta = (rho_new / st.rho[pp * st.S + y]) * (st.alpha[y] / st.omega[y]);
-    const double om = st.omega[y];
+    const T om = (T)st.omega[y], bt = (T)beta;
     if (lead) {
         st.rho[par * st.S + y] = rho_new;
         st.flagA[par * st.S + y] = 0; st.flagB[par * st.S + y] = 0;
@@ -260,35 +298,36 @@ __global__ void __launch_bounds__(THREADS) k_bicg_p(Op op, BicgVecs<double> v, B
     const size_t o = (size_t)y * v.Np;
     BTE_CELL_LOOP(c) {
         // cublasDaxpy(-omega, q, p); cublasDscal(beta, p); cublasDaxpy(1, r, p)
-        double pv = fma(-om, v.q[o + c], v.p[o + c]);
-        pv = fma(beta, pv, v.r[o + c]);
+        T pv = fma(-om, v.q[o + c], v.p[o + c]);
+        pv = fma(bt, pv, v.r[o + c]);
         v.p[o + c] = pv;
         v.ph[o + c] = v.invD[o + c] * pv;
     }
 }
 
 // K2: q = A ph; partial r_hat . q
-template <typename Op>
-__global__ void __launch_bounds__(THREADS) k_bicg_spmv1(Op op, BicgVecs<double> v, BicgState st, int i) {
+template <typename Op, typename T>
+__global__ void __launch_bounds__(THREADS) k_bicg_spmv1(Op op, BicgVecs<T> v, BicgState st, int i) {
     __shared__ double sm[1][NWARP];
     const int y = blockIdx.y;
     const int par = i & 1;
     if (st.done[y] | st.flagA[par * st.S + y]) return;
     const size_t o = (size_t)y * v.Np;
-    const double* ph = v.ph + o;
-    double acc[1] = {0};
+    const T* ph = v.ph + o;
+    T acc_t = 0;
     BTE_CELL_LOOP(c) {
-        double qv = op.template apply<double>(y, c, ph);
+        const T qv = op.template apply<T>(y, c, ph);
         v.q[o + c] = qv;
-        acc[0] = fma(v.rw[o + c], qv, acc[0]);
+        acc_t = fma(v.rw[o + c], qv, acc_t);
     }
+    double acc[1] = {(double)acc_t};
     block_sum<1>(acc, sm);
     if (threadIdx.x == 0) st.P(PK_RWQ, y)[blockIdx.x] = acc[0];
 }
 
 // K3: alpha; s = r - alpha q (in place in r); z = M s
-template <typename Op>
-__global__ void __launch_bounds__(THREADS) k_bicg_s(Op op, BicgVecs<double> v, BicgState st, int i) {
+template <typename Op, typename T>
+__global__ void __launch_bounds__(THREADS) k_bicg_s(Op op, BicgVecs<T> v, BicgState st, int i) {
     __shared__ double sm[1][NWARP];
     const int y = blockIdx.y;
     const int par = i & 1;
@@ -305,30 +344,32 @@ __global__ void __launch_bounds__(THREADS) k_bicg_s(Op op, BicgVecs<double> v, B
     }
     const double alpha = st.rho[par * st.S + y] / temp;
     if (lead) st.alpha[y] = alpha;
+    const T al = (T)alpha;
     const size_t o = (size_t)y * v.Np;
     BTE_CELL_LOOP(c) {
-        double s = fma(-alpha, v.q[o + c], v.r[o + c]);
+        const T s = fma(-al, v.q[o + c], v.r[o + c]);
         v.r[o + c] = s;
         v.z[o + c] = v.invD[o + c] * s;
     }
 }
 
 // K4: t = A z; partials t.s, t.t
-template <typename Op>
-__global__ void __launch_bounds__(THREADS) k_bicg_spmv2(Op op, BicgVecs<double> v, BicgState st, int i) {
+template <typename Op, typename T>
+__global__ void __launch_bounds__(THREADS) k_bicg_spmv2(Op op, BicgVecs<T> v, BicgState st, int i) {
     __shared__ double sm[2][NWARP];
     const int y = blockIdx.y;
     const int par = i & 1;
     if (st.done[y] | st.flagA[par * st.S + y] | st.flagB[par * st.S + y]) return;
     const size_t o = (size_t)y * v.Np;
-    const double* z = v.z + o;
-    double acc[2] = {0, 0};
+    const T* z = v.z + o;
+    T a0 = 0, a1 = 0;
     BTE_CELL_LOOP(c) {
-        double tv = op.template apply<double>(y, c, z);
+        const T tv = op.template apply<T>(y, c, z);
         v.t[o + c] = tv;
-        acc[0] = fma(tv, v.r[o + c], acc[0]);
-        acc[1] = fma(tv, tv, acc[1]);
+        a0 = fma(tv, v.r[o + c], a0);
+        a1 = fma(tv, tv, a1);
     }
+    double acc[2] = {(double)a0, (double)a1};
     block_sum<2>(acc, sm);
     if (threadIdx.x == 0) {
         st.P(PK_TS, y)[blockIdx.x] = acc[0];
@@ -337,8 +378,8 @@ __global__ void __launch_bounds__(THREADS) k_bicg_spmv2(Op op, BicgVecs<double> 
 }
 
 // K5: omega; x += alpha ph; x += omega z; r = s - omega t; partials r.r, r_hat.r
-template <typename Op>
-__global__ void __launch_bounds__(THREADS) k_bicg_x(Op op, BicgVecs<double> v, BicgState st, int i) {
+template <typename Op, typename T>
+__global__ void __launch_bounds__(THREADS) k_bicg_x(Op op, BicgVecs<T> v, BicgState st, int i) {
     __shared__ double sm[2][NWARP];
     const int y = blockIdx.y;
     const int par = i & 1;
@@ -347,18 +388,20 @@ __global__ void __launch_bounds__(THREADS) k_bicg_x(Op op, BicgVecs<double> v, B
     const double omega = sum_parts(st.P(PK_TS, y), st.nchunk) / sum_parts(st.P(PK_TT, y), st.nchunk);
     const double alpha = st.alpha[y];
     if (lead) st.omega[y] = omega;
+    const T al = (T)alpha, om = (T)omega;
     const size_t o = (size_t)y * v.Np;
-    double* x = op.x_of(y);
-    double acc[2] = {0, 0};
+    T* x = op.x_of(y);
+    T a0 = 0, a1 = 0;
     BTE_CELL_LOOP(c) {
-        double xv = fma(alpha, v.ph[o + c], x[c]);
-        xv = fma(omega, v.z[o + c], xv);
+        T xv = fma(al, v.ph[o + c], x[c]);
+        xv = fma(om, v.z[o + c], xv);
         x[c] = xv;
-        double r = fma(-omega, v.t[o + c], v.r[o + c]);
+        const T r = fma(-om, v.t[o + c], v.r[o + c]);
         v.r[o + c] = r;
-        acc[0] = fma(r, r, acc[0]);
-        acc[1] = fma(v.rw[o + c], r, acc[1]);
+        a0 = fma(r, r, a0);
+        a1 = fma(v.rw[o + c], r, a1);
     }
+    double acc[2] = {(double)a0, (double)a1};
     block_sum<2>(acc, sm);
     if (threadIdx.x == 0) {
         st.P(par ? PK_RR1 : PK_RR0, y)[blockIdx.x] = acc[0];

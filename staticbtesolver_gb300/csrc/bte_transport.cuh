@@ -465,3 +465,89 @@ __global__ void k_sweep_layout(const int* __restrict__ perm, const int* __restri
 }
 
 }  // namespace bte
+
+namespace bte {
+
+// ---------------------------------------------------------------------------
+// Mixed form: FP32 BiCGSTAB corrections inside FP64 iterative refinement.
+
+// FP32 copy of the per-direction geometry scaled by kappa[d].
+__global__ void k_geometry32(const double* __restrict__ dg, const double* __restrict__ vo,
+                             const double* __restrict__ fc, const double* __restrict__ kappa, int n, int F,
+                             size_t Np, float* dg32, float* vo32, float* fc32) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    const int d = blockIdx.y;
+    if (c >= Np) return;
+    const size_t dc = (size_t)d * Np + c;
+    const double k = kappa[d];
+    dg32[dc] = (float)(dg[dc] * k);
+    vo32[dc] = c < n ? (float)(vo[dc] * k) : 1.0f;
+    for (int f = 0; f < F; ++f) {
+        const size_t q = ((size_t)d * F + f) * Np + c;
+        fc32[q] = (float)(fc[q] * k);
+    }
+}
+
+// Warm start: x (e_curr) = previous outer iterate (e_prev) for every system of the batch.
+__global__ void __launch_bounds__(THREADS) k_mixed_start(FaceFluxOp op, const double* __restrict__ e_prev) {
+    const int y = blockIdx.y;
+    int b, d;
+    op.bd(y, b, d);
+    const size_t off = ((size_t)b * op.n_dir + d) * op.Np;
+    BTE_CELL_LOOP(c) { op.x_out[off + c] = e_prev[off + c]; }
+}
+
+// FP64 residual r = b - A x of every system; r32 = kappa_d r for the FP32
+// correction solve; partials of ||r||^2 and ||b||^2 per (system, chunk).
+__global__ void __launch_bounds__(THREADS) k_mixed_residual(FaceFluxOp op, const double* __restrict__ rhs,
+                                                            const double* __restrict__ kappa, float* r32,
+                                                            double* part, int nchunk, int n) {
+    __shared__ double sm[2][NWARP];
+    const int y = blockIdx.y;
+    int b, d;
+    op.bd(y, b, d);
+    const size_t o = (size_t)y * op.Np;
+    const double* xs = op.x_of(y);
+    const double k = kappa[d];
+    double acc[2] = {0, 0};
+    BTE_CELL_LOOP(c) {
+        double r = 0.0;
+        if (c < n) {
+            r = rhs[o + c] - op.template apply<double>(y, c, xs);
+            acc[0] = fma(r, r, acc[0]);
+            acc[1] = fma(rhs[o + c], rhs[o + c], acc[1]);
+        }
+        r32[o + c] = (float)(k * r);
+    }
+    block_sum<2>(acc, sm);
+    if (threadIdx.x == 0) {
+        part[((size_t)y * nchunk + blockIdx.x) * 2] = acc[0];
+        part[((size_t)y * nchunk + blockIdx.x) * 2 + 1] = acc[1];
+    }
+}
+
+// skip[y] = 1 when ||b - A x|| <= tol ||b|| (the reference's criterion for x0 = 0).
+__global__ void k_mixed_check(const double* part, int S, int nchunk, double tol, int* skip, int* n_active) {
+    const int y = blockIdx.x * blockDim.x + threadIdx.x;
+    if (y >= S) return;
+    double rr = 0, bb = 0;
+    for (int i = 0; i < nchunk; ++i) {
+        rr += part[((size_t)y * nchunk + i) * 2];
+        bb += part[((size_t)y * nchunk + i) * 2 + 1];
+    }
+    const int ok = rr <= tol * tol * bb;
+    skip[y] = ok;
+    if (!ok) atomicAdd(n_active, 1);
+}
+
+// x += dx for the systems that were corrected.
+__global__ void __launch_bounds__(THREADS) k_mixed_update(FaceFluxOp op, const float* __restrict__ dx,
+                                                          const int* __restrict__ skip) {
+    const int y = blockIdx.y;
+    if (skip[y]) return;
+    double* x = op.x_of(y);
+    const size_t o = (size_t)y * op.Np;
+    BTE_CELL_LOOP(c) { x[c] += (double)dx[o + c]; }
+}
+
+}  // namespace bte

@@ -74,6 +74,10 @@ typedef struct bte_options {
     void* user;
     int profile;          /* nonzero: time every inner-solve kernel with CUDA events
                              (bte_get_kernel_stats); adds event records between launches */
+    int accel;            /* outer-iteration extrapolation: 0 none (the reference), 1 learned
+                             (the MLP set by bte_set_mlp), 2 Aitken per cell (non-learned) */
+    int accel_every;      /* outer iterations between extrapolations (>= 4) */
+    int keep_history;     /* nonzero: keep T after every outer iteration (bte_get_history) */
 } bte_options;
 
 /* Per-kernel totals of the last profiled bte_solve. */
@@ -99,6 +103,7 @@ typedef struct bte_report {
     long long kernel_launches; /* kernels this library launched during the solve */
     int sweep_group;           /* sweep form: bands per block and threads per block */
     int sweep_threads;         /* chosen by timing candidate shapes on a plan's first sweep */
+    int accel_steps;           /* outer-iteration extrapolations applied */
 } bte_report;
 
 /* Fill opts with the reference's defaults (max_iter 10000 as BTEcmd's -I default,
@@ -153,6 +158,38 @@ bte_status bte_get_heat_flux(bte_ctx* ctx, double* q_bc, double* q_bc_band);
 bte_status bte_get_energy(bte_ctx* ctx, double* e);
 /* Margins of the outer iterations run, up to cap values; returns how many via *n. */
 bte_status bte_get_margins(bte_ctx* ctx, double* margins, int cap, int* n);
+
+/* Learned outer-iteration acceleration (no counterpart in the reference; the
+ * plain source iteration still runs to the same margin, so the accelerator
+ * changes how fast the fixed point is reached, not which one).  Every
+ * accel_every outer iterations a per-cell MLP (8 -> 128 -> 128 -> 128 -> 1,
+ * BF16 weights, FP32 accumulation on the tensor cores) maps the cell's last
+ * four temperatures and its geometry to an extrapolated equilibrium
+ * temperature; T and the equilibrium energy density are reset to it.  If the
+ * margin accel_every-1 iterations after a jump is not below the margin at the
+ * jump, extrapolation stops for the rest of the solve.
+ * Features per cell (d_i = T_{k-i+1} - T_{k-i}, s = |d1| + |d2| + |d3|):
+ *   d1/s, d2/s, d3/s, (T_k - T_ref)/max|T_bc - T_ref|, x and y of the centroid
+ *   scaled to [0, 1] over the mesh, log(V / mean V), log10(Kn), Kn =
+ *   (sum_b Lr_b v_b tau_b / sum_b Lr_b) / V^(1/dim); output (T* - T_k) / s,
+ *   clipped to [-64, 64].  Parameters: FP32, bte_mlp_param_count() values,
+ *   W1[8][128] b1 W2[128][128] b2 W3[128][128] b3 W4[128][1] b4. */
+int bte_mlp_param_count(void);
+bte_status bte_set_mlp(bte_ctx* ctx, const float* params);
+/* Cell centroids [n_cell][3] (used only for the accelerator's features). */
+bte_status bte_set_centroids(bte_ctx* ctx, const double* centroid);
+/* T after every outer iteration of the last solve run with keep_history, row-major
+ * [iteration][n_cell], up to cap_iters rows; *n_iters = rows available. */
+bte_status bte_get_history(bte_ctx* ctx, double* T, int cap_iters, int* n_iters);
+/* MLP on the current device, host buffers: X [M][8] FP32 features. */
+bte_status bte_mlp_predict(const float* X, int M, const float* params, float* y);
+/* Full-batch loss 0.5 mean (y - Y)^2 and its gradient w.r.t. the parameters. */
+bte_status bte_mlp_gradient(const float* X, const float* Y, int M, const float* params, float* grad,
+                            double* loss);
+/* Adam training on the GPU: steps minibatches of batch rows drawn with seed;
+ * params in/out (FP32); loss_hist[steps] (may be NULL). */
+bte_status bte_mlp_train(const float* X, const float* Y, int M, int steps, int batch, float lr,
+                         unsigned seed, float* params, float* loss_hist);
 
 /* Kernel statistics of the last solve run with opts->profile set; *n = entries. */
 bte_status bte_get_kernel_stats(bte_ctx* ctx, bte_kernel_stat* stats, int cap, int* n);

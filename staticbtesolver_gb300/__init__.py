@@ -47,7 +47,8 @@ class BteError(RuntimeError):
 class Options(C.Structure):
     _fields_ = [("max_iter", C.c_int), ("tol", C.c_double), ("form", C.c_int), ("inner_tol", C.c_double),
                 ("inner_maxit", C.c_int), ("batch_systems", C.c_int), ("on_iteration", ITER_CB),
-                ("user", C.c_void_p), ("profile", C.c_int)]
+                ("user", C.c_void_p), ("profile", C.c_int), ("accel", C.c_int), ("accel_every", C.c_int),
+                ("keep_history", C.c_int)]
 
 
 class KernelStat(C.Structure):
@@ -59,7 +60,8 @@ class Report(C.Structure):
                 ("inner_solves", C.c_longlong), ("inner_iterations", C.c_longlong),
                 ("inner_unconverged", C.c_longlong), ("refinements", C.c_longlong), ("ms_total", C.c_double),
                 ("ms_rhs", C.c_double), ("ms_inner", C.c_double), ("ms_reduce", C.c_double),
-                ("kernel_launches", C.c_longlong), ("sweep_group", C.c_int), ("sweep_threads", C.c_int)]
+                ("kernel_launches", C.c_longlong), ("sweep_group", C.c_int), ("sweep_threads", C.c_int),
+                ("accel_steps", C.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -103,6 +105,17 @@ def _load():
     L.bte_get_heat_flux.argtypes = [vp, _dp, C.c_void_p]
     L.bte_get_energy.argtypes = [vp, _dp]
     L.bte_get_margins.argtypes = [vp, C.c_void_p, C.c_int, C.POINTER(C.c_int)]
+    for fn in ("bte_set_mlp", "bte_set_centroids", "bte_get_history", "bte_mlp_predict", "bte_mlp_gradient",
+               "bte_mlp_train"):
+        getattr(L, fn).restype = C.c_int
+    L.bte_set_mlp.argtypes = [vp, C.c_void_p]
+    L.bte_set_centroids.argtypes = [vp, _dp]
+    L.bte_get_history.argtypes = [vp, C.c_void_p, C.c_int, C.POINTER(C.c_int)]
+    L.bte_mlp_predict.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
+    L.bte_mlp_gradient.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.POINTER(C.c_double)]
+    L.bte_mlp_train.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_float, C.c_uint, C.c_void_p,
+                                C.c_void_p]
+    L.bte_mlp_param_count.restype = C.c_int
     L.bte_get_kernel_stats.argtypes = [vp, C.c_void_p, C.c_int, C.POINTER(C.c_int)]
     L.bte_get_kernel_stats.restype = C.c_int
     L.bte_bicgstab_csr.argtypes = [C.c_int, _ip, _ip, _dp, C.c_int, _dp, _dp, C.c_int, C.c_double,
@@ -260,13 +273,29 @@ class Context:
         self._check(L.bte_set_bcs(self._h, n_bc, i32(c["index"]) if n_bc else np.zeros(1, np.int32),
                                   i32(c["type"]) if n_bc else np.zeros(1, np.int32),
                                   f64(c["T"]) if n_bc else np.zeros(1)), "bcs")
+        if "centroid" in a:
+            self._check(L.bte_set_centroids(self._h, f64(a["centroid"])), "centroids")
         self._dims = (a["n_cell"], a["n_dir"], len(b["vg"]), n_bc)
         return self
 
+    def set_mlp(self, params):
+        p = np.ascontiguousarray(params, np.float32)
+        self._check(_cuda.bte_set_mlp(self._h, p.ctypes.data_as(C.c_void_p)), "set_mlp")
+        return self
+
+    def history(self):
+        k = C.c_int(0)
+        _cuda.bte_get_history(self._h, None, 0, C.byref(k))
+        h = np.zeros((k.value, self._dims[0]))
+        _cuda.bte_get_history(self._h, h.ctypes.data_as(C.c_void_p), k.value, C.byref(k))
+        return h
+
     def solve(self, max_iter=1000, tol=1e-5, form=FORM_PLAIN, inner_tol=1e-9, inner_maxit=1000,
-              batch_systems=0, on_iteration=None, raise_on_not_converged=False, profile=False):
+              batch_systems=0, on_iteration=None, raise_on_not_converged=False, profile=False, accel=0,
+              accel_every=8, keep_history=False):
         o = default_options(max_iter=int(max_iter), tol=float(tol), form=int(form), inner_tol=float(inner_tol),
-                            inner_maxit=int(inner_maxit), batch_systems=int(batch_systems), profile=int(profile))
+                            inner_maxit=int(inner_maxit), batch_systems=int(batch_systems), profile=int(profile),
+                            accel=int(accel), accel_every=int(accel_every), keep_history=int(bool(keep_history)))
         cb = None
         if on_iteration is not None:
             cb = ITER_CB(lambda _u, it, m, ms: on_iteration(it, m, ms))

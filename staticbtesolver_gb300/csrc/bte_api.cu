@@ -21,6 +21,8 @@
 #include "../../include/bte_cuda.h"
 #include "bte_kernels.cuh"
 #include "bte_transport.cuh"
+#include "bte_mlp.cuh"
+#include <random>
 
 namespace {
 
@@ -98,6 +100,12 @@ struct bte_ctx {
     double* h_pinned = nullptr;  // [4]
     int* h_pinned_i = nullptr;   // [4]
     std::vector<int> h_done, h_iters;
+    // learned accelerator
+    std::vector<double> centroid;
+    bool has_mlp = false;
+    DevBuf d_params, d_wpack, d_centroid, d_ring, d_feat, d_scale, d_y;
+    std::vector<double> history;
+    int history_rows = 0;
     // mixed form: scaled FP32 geometry and FP32 work vectors
     bool mixed_ready = false;
     DevBuf d_dg32, d_vo32, d_fc32, d_kb32, d_kappa;
@@ -290,6 +298,7 @@ bte_status bte_set_geometry(bte_ctx* ctx, int dim, int n_cell, int n_face, const
     ctx->area.assign(area, area + nf);
     ctx->normal.assign(normal, normal + 3 * nf);
     ctx->volume.assign(volume, volume + n_cell);
+    ctx->centroid.clear();
     ctx->has_geom = true;
     ctx->dirty = true;
     ctx->solved = false;
@@ -1038,6 +1047,37 @@ extern "C" bte_status bte_solve(bte_ctx* ctx, const bte_options* opts, bte_repor
     struct EvGuard { cudaEvent_t* e; ~EvGuard() { for (int k = 0; k < 5; ++k) cudaEventDestroy(e[k]); } } guard{ev};
     bte_status result = BTE_ERR_NOT_CONVERGED;
     const int nred = (int)(Np / bte::THREADS);
+    // accelerator set-up
+    bool accel_on = o.accel != 0;
+    int accel_last = -1;
+    double accel_margin = 0.0;
+    bte::mlp::FeatureGeom fg{};
+    if (o.accel) {
+        if (o.accel_every < 4) return fail(ctx, BTE_ERR_INVALID_ARGUMENT, "bte_solve: accel_every must be >= 4");
+        if (o.accel == 1 && !ctx->has_mlp) return fail(ctx, BTE_ERR_STATE, "bte_solve: accel = 1 needs bte_set_mlp");
+        if ((int)ctx->centroid.size() != 3 * ctx->n)
+            return fail(ctx, BTE_ERR_STATE, "bte_solve: the accelerator needs bte_set_centroids");
+        BTE_CUDA(upload(ctx->d_centroid, ctx->centroid, st));
+        BTE_CUDA(ctx->d_ring.alloc(sizeof(double) * 4 * Np));
+        BTE_CUDA(ctx->d_feat.alloc(sizeof(__nv_bfloat16) * bte::mlp::IN_PAD * ctx->n));
+        BTE_CUDA(ctx->d_scale.alloc(sizeof(double) * ctx->n));
+        BTE_CUDA(ctx->d_y.alloc(sizeof(float) * ctx->n));
+        BTE_CUDA(cudaFuncSetAttribute(bte::mlp::k_forward, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)bte::mlp::FWD_SMEM));
+        double vmean = 0, xmin = 1e300, xmax = -1e300, ymin = 1e300, ymax = -1e300, lrs = 0, lrk = 0, dT = 0;
+        for (int c = 0; c < ctx->n; ++c) {
+            vmean += ctx->volume[c];
+            xmin = std::min(xmin, ctx->centroid[3 * c]); xmax = std::max(xmax, ctx->centroid[3 * c]);
+            ymin = std::min(ymin, ctx->centroid[3 * c + 1]); ymax = std::max(ymax, ctx->centroid[3 * c + 1]);
+        }
+        for (int b = 0; b < NB; ++b) { lrs += ctx->Lr[b]; lrk += ctx->Lr[b] * ctx->vg[b] * ctx->tau[b]; }
+        for (int i = 0; i < ctx->n_bc; ++i) dT = std::max(dT, std::fabs(ctx->bc_T[i] - ctx->T_ref));
+        fg = bte::mlp::FeatureGeom{ctx->d_centroid.as<double>(), ctx->d_volume.as<double>(), vmean / ctx->n, xmin,
+                                   xmax - xmin, ymin, ymax - ymin, lrk / lrs, 1.0 / ctx->dim, ctx->T_ref,
+                                   dT > 0 ? dT : 1.0};
+    }
+    ctx->history.clear();
+    ctx->history_rows = 0;
     for (int it = 0; it < o.max_iter; ++it) {
         std::swap(ctx->e_curr, ctx->e_prev);
         BTE_CUDA(cudaEventRecord(ev[0], st));
@@ -1073,27 +1113,48 @@ extern "C" bte_status bte_solve(bte_ctx* ctx, const bte_options* opts, bte_repor
         BTE_CUDA(cudaStreamSynchronize(st));
         if (ctx->profile) prof_resolve(ctx, nullptr, 0);
         const double m = ctx->h_pinned[0];
-        float t01 = 0, t12 = 0, t23 = 0;
-        cudaEventElapsedTime(&t01, ev[0], ev[1]);
-        cudaEventElapsedTime(&t12, ev[1], ev[2]);
-        cudaEventElapsedTime(&t23, ev[2], ev[3]);
-        rep.ms_rhs += t01;
-        rep.ms_inner += t12;
-        rep.ms_reduce += t23;
-        rep.ms_total += t01 + t12 + t23;
-        ctx->margins.push_back(m);
-        rep.n_iter = it + 1;
-        rep.final_margin = m;
-        if (o.on_iteration) o.on_iteration(o.user, it, m, (double)(t01 + t12 + t23));
-        if (!std::isfinite(m)) {
-            result = BTE_ERR_NUMERICAL;
-            ctx->err = "non-finite margin in outer iteration " + std::to_string(it);
-            break;
+        // the last four temperature fields (accelerator) and the history
+        if (o.accel) {
+            BTE_CUDA(cudaMemcpyAsync(ctx->d_ring.as<double>() + (size_t)(it % 4) * Np, ctx->d_T.p,
+                                     sizeof(double) * Np, cudaMemcpyDeviceToDevice, st));
+        }
+        if (o.keep_history) {
+            ctx->history.resize((size_t)(it + 1) * ctx->n);
+            BTE_CUDA(cudaMemcpyAsync(ctx->history.data() + (size_t)it * ctx->n, ctx->d_T.p, sizeof(double) * ctx->n,
+                                     cudaMemcpyDeviceToHost, st));
+            BTE_CUDA(cudaStreamSynchronize(st));
+            ctx->history_rows = it + 1;
         }
         if (m <= o.tol) {
             rep.converged = 1;
             result = BTE_OK;
             break;
+        }
+        // outer-iteration extrapolation (accel): stop for good when the margin
+        // accel_every-1 iterations after a jump is not below the margin at it
+        if (o.accel && accel_on && accel_last >= 0 && it == accel_last + o.accel_every - 1 && m >= accel_margin)
+            accel_on = false;
+        if (o.accel && accel_on && it >= 3 && (accel_last < 0 || it - accel_last >= o.accel_every)) {
+            const int n = ctx->n;
+            const int s0 = it % 4, s1 = (it + 3) % 4, s2 = (it + 2) % 4, s3 = (it + 1) % 4;
+            BTE_LAUNCH(KK_REDUCE, -1, 0, 0,
+                       bte::mlp::k_accel_features<<<(n + 255) / 256, 256, 0, st>>>(
+                           ctx->d_ring.as<double>(), s0, s1, s2, s3, Np, n, fg, ctx->d_feat.as<__nv_bfloat16>(),
+                           ctx->d_scale.as<double>()));
+            if (o.accel == 1) {
+                BTE_LAUNCH(KK_REDUCE, -1, 0, 0,
+                           bte::mlp::k_forward<<<std::max(1, std::min(1024, (n + 63) / 64)), 128, bte::mlp::FWD_SMEM, st>>>(
+                               ctx->d_feat.as<__nv_bfloat16>(), n, ctx->d_wpack.as<__nv_bfloat16>(),
+                               ctx->d_params.as<float>(), ctx->d_y.as<float>(), nullptr));
+            }
+            BTE_LAUNCH(KK_REDUCE, -1, 0, 0,
+                       bte::mlp::k_accel_apply<<<(n + 255) / 256, 256, 0, st>>>(
+                           ctx->d_ring.as<double>(), s0, s1, s2, Np, n, ctx->d_scale.as<double>(),
+                           ctx->d_y.as<float>(), o.accel == 1, ctx->d_Cb.as<double>(), NB, ctx->solid_angle,
+                           ctx->T_ref, ctx->d_T.as<double>(), ctx->d_ebar.as<double>()));
+            accel_last = it;
+            accel_margin = m;
+            ++rep.accel_steps;
         }
     }
     if (o.max_iter == 0) result = BTE_OK;
@@ -1431,3 +1492,254 @@ extern "C" bte_status bte_bicgstab_csr_noalloc(int n, const int* rowptr, const i
     if (converged) *converged = (h_state[0] == 1 || h_state[0] == 2) ? 1 : 0;
     return BTE_OK;
 }
+
+// ---------------------------------------------------------------------------
+// MLP of the learned accelerator: parameters, inference, gradient, training.
+
+namespace {
+
+// Device buffers of one MLP computation on M rows (batch).
+struct MlpWork {
+    DevBuf x, y, t, dy, act, dh, p1, p2, p3, part, params, wpack, wi, grad, m, v, idx, xall, yall;
+    int M = 0, nslices = 0;
+};
+constexpr int kRowsPerSlice = 256;
+
+#define MLP_CUDA(call)                                                                          \
+    do {                                                                                        \
+        cudaError_t _e = (call);                                                                \
+        if (_e != cudaSuccess) {                                                                \
+            g_create_error = std::string("mlp: ") + #call + ": " + cudaGetErrorString(_e);      \
+            return _e == cudaErrorMemoryAllocation ? BTE_ERR_OUT_OF_MEMORY : BTE_ERR_CUDA;      \
+        }                                                                                       \
+    } while (0)
+
+bte_status mlp_alloc(MlpWork& w, int M) {
+    using bf = __nv_bfloat16;
+    namespace ml = bte::mlp;
+    w.M = M;
+    w.nslices = (M + kRowsPerSlice - 1) / kRowsPerSlice;
+    MLP_CUDA(w.x.alloc(sizeof(bf) * (size_t)M * ml::IN_PAD));
+    MLP_CUDA(w.y.alloc(sizeof(float) * M));
+    MLP_CUDA(w.t.alloc(sizeof(float) * M));
+    MLP_CUDA(w.dy.alloc(sizeof(float) * M));
+    MLP_CUDA(w.act.alloc(sizeof(bf) * 3 * (size_t)M * ml::H));
+    MLP_CUDA(w.dh.alloc(sizeof(bf) * 3 * (size_t)M * ml::H));
+    MLP_CUDA(w.p1.alloc(sizeof(float) * (size_t)w.nslices * ml::IN_PAD * ml::H));
+    MLP_CUDA(w.p2.alloc(sizeof(float) * (size_t)w.nslices * ml::H * ml::H));
+    MLP_CUDA(w.p3.alloc(sizeof(float) * (size_t)w.nslices * ml::H * ml::H));
+    MLP_CUDA(w.part.alloc(sizeof(double) * 256));
+    MLP_CUDA(w.params.alloc(sizeof(float) * ml::NPARAM));
+    MLP_CUDA(w.wpack.alloc(sizeof(bf) * ml::PK_N));
+    MLP_CUDA(w.wi.alloc(sizeof(bf) * 2 * ml::H * ml::H));
+    MLP_CUDA(w.grad.alloc(sizeof(float) * ml::NPARAM));
+    MLP_CUDA(cudaFuncSetAttribute(ml::k_forward, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ml::FWD_SMEM));
+    MLP_CUDA(cudaFuncSetAttribute(ml::k_backward_data, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)ml::BWD_SMEM));
+    return BTE_OK;
+}
+
+int mlp_blocks(int M) { return std::max(1, std::min(1024, (M + 63) / 64)); }
+
+// Pack the FP32 parameters in w.params into the kernels' BF16 layouts.
+bte_status mlp_pack(MlpWork& w, cudaStream_t st) {
+    namespace ml = bte::mlp;
+    ml::k_pack<<<(ml::H * ml::H + 255) / 256, 256, 0, st>>>(w.params.as<float>(), w.wpack.as<__nv_bfloat16>());
+    ml::k_pack_in_major<<<(ml::H * ml::H + 255) / 256, 256, 0, st>>>(w.params.as<float>(), w.wi.as<__nv_bfloat16>());
+    MLP_CUDA(cudaGetLastError());
+    return BTE_OK;
+}
+
+// Loss and gradient of the rows already in w.x / w.t (M rows) into w.grad; loss to *loss.
+bte_status mlp_loss_grad(MlpWork& w, int M, cudaStream_t st, double* loss) {
+    namespace ml = bte::mlp;
+    using bf = __nv_bfloat16;
+    ml::k_forward<<<mlp_blocks(M), 128, ml::FWD_SMEM, st>>>(w.x.as<bf>(), M, w.wpack.as<bf>(), w.params.as<float>(),
+                                                          w.y.as<float>(), w.act.as<bf>());
+    const int lb = std::min(256, (M + 255) / 256);
+    ml::k_loss<<<lb, 256, 0, st>>>(w.y.as<float>(), w.t.as<float>(), M, w.dy.as<float>(), w.part.as<double>());
+    ml::k_backward_data<<<mlp_blocks(M), 128, ml::BWD_SMEM, st>>>(w.dy.as<float>(), M, w.act.as<bf>(),
+                                                                 w.wi.as<bf>(), w.params.as<float>(), w.dh.as<bf>());
+    const int ns = (M + kRowsPerSlice - 1) / kRowsPerSlice;
+    ml::k_weight_grad<ml::IN_PAD><<<ns, 256, 0, st>>>(w.x.as<bf>(), ml::IN_PAD, w.dh.as<bf>(), M, kRowsPerSlice,
+                                                       w.p1.as<float>());
+    ml::k_weight_grad<ml::H><<<ns, 256, 0, st>>>(w.act.as<bf>(), ml::H, w.dh.as<bf>() + (size_t)M * ml::H, M,
+                                                 kRowsPerSlice, w.p2.as<float>());
+    ml::k_weight_grad<ml::H><<<ns, 256, 0, st>>>(w.act.as<bf>() + (size_t)M * ml::H, ml::H,
+                                                 w.dh.as<bf>() + (size_t)2 * M * ml::H, M, kRowsPerSlice,
+                                                 w.p3.as<float>());
+    ml::k_grad_assemble<<<(ml::NPARAM + 255) / 256, 256, 0, st>>>(w.p1.as<float>(), w.p2.as<float>(),
+                                                                   w.p3.as<float>(), ns, w.act.as<bf>(),
+                                                                   w.dh.as<bf>(), w.dy.as<float>(), M,
+                                                                   w.grad.as<float>());
+    MLP_CUDA(cudaGetLastError());
+    if (loss) {
+        std::vector<double> part(lb);
+        MLP_CUDA(cudaMemcpyAsync(part.data(), w.part.p, sizeof(double) * lb, cudaMemcpyDeviceToHost, st));
+        MLP_CUDA(cudaStreamSynchronize(st));
+        double s = 0;
+        for (double v : part) s += v;
+        *loss = s;
+    }
+    return BTE_OK;
+}
+
+struct ScopedStream {
+    cudaStream_t s = nullptr;
+    ~ScopedStream() {
+        if (s) {
+            cudaStreamSynchronize(s);
+            cudaStreamDestroy(s);
+        }
+    }
+};
+
+}  // namespace
+
+extern "C" {
+
+int bte_mlp_param_count(void) { return bte::mlp::NPARAM; }
+
+bte_status bte_set_centroids(bte_ctx* ctx, const double* centroid) {
+    if (!ctx || !centroid) return BTE_ERR_INVALID_ARGUMENT;
+    if (!ctx->has_geom) return fail(ctx, BTE_ERR_STATE, "bte_set_centroids: set the geometry first");
+    ctx->centroid.assign(centroid, centroid + 3 * (size_t)ctx->n);
+    for (double v : ctx->centroid)
+        if (!std::isfinite(v)) return fail(ctx, BTE_ERR_INVALID_ARGUMENT, "bte_set_centroids: non-finite value");
+    return BTE_OK;
+}
+
+bte_status bte_set_mlp(bte_ctx* ctx, const float* params) {
+    if (!ctx || !params) return BTE_ERR_INVALID_ARGUMENT;
+    namespace ml = bte::mlp;
+    for (int i = 0; i < ml::NPARAM; ++i)
+        if (!std::isfinite(params[i])) return fail(ctx, BTE_ERR_INVALID_ARGUMENT, "bte_set_mlp: non-finite parameter");
+    BTE_CUDA(cudaSetDevice(ctx->device));
+    BTE_CUDA(ctx->d_params.alloc(sizeof(float) * ml::NPARAM));
+    BTE_CUDA(ctx->d_wpack.alloc(sizeof(__nv_bfloat16) * ml::PK_N));
+    BTE_CUDA(cudaMemcpyAsync(ctx->d_params.p, params, sizeof(float) * ml::NPARAM, cudaMemcpyHostToDevice, ctx->stream));
+    ml::k_pack<<<(ml::H * ml::H + 255) / 256, 256, 0, ctx->stream>>>(ctx->d_params.as<float>(),
+                                                                     ctx->d_wpack.as<__nv_bfloat16>());
+    BTE_LAUNCHED();
+    BTE_CUDA(cudaStreamSynchronize(ctx->stream));
+    ctx->has_mlp = true;
+    return BTE_OK;
+}
+
+bte_status bte_get_history(bte_ctx* ctx, double* T, int cap_iters, int* n_iters) {
+    if (!ctx) return BTE_ERR_INVALID_ARGUMENT;
+    if (n_iters) *n_iters = ctx->history_rows;
+    if (T && cap_iters > 0) {
+        const size_t rows = (size_t)std::min(cap_iters, ctx->history_rows);
+        std::memcpy(T, ctx->history.data(), sizeof(double) * rows * ctx->n);
+    }
+    return BTE_OK;
+}
+
+bte_status bte_mlp_predict(const float* X, int M, const float* params, float* y) {
+    namespace ml = bte::mlp;
+    if (!X || !params || !y || M <= 0) return BTE_ERR_INVALID_ARGUMENT;
+    ScopedStream ss;
+    MLP_CUDA(cudaStreamCreateWithFlags(&ss.s, cudaStreamNonBlocking));
+    MlpWork w;
+    bte_status rc = mlp_alloc(w, M);
+    if (rc) return rc;
+    DevBuf xf;
+    MLP_CUDA(xf.alloc(sizeof(float) * (size_t)M * ml::IN));
+    MLP_CUDA(cudaMemcpyAsync(xf.p, X, sizeof(float) * (size_t)M * ml::IN, cudaMemcpyHostToDevice, ss.s));
+    MLP_CUDA(cudaMemcpyAsync(w.params.p, params, sizeof(float) * ml::NPARAM, cudaMemcpyHostToDevice, ss.s));
+    ml::k_features_bf16<<<(M * ml::IN_PAD + 255) / 256, 256, 0, ss.s>>>(xf.as<float>(), M, w.x.as<__nv_bfloat16>());
+    rc = mlp_pack(w, ss.s);
+    if (rc) return rc;
+    ml::k_forward<<<mlp_blocks(M), 128, ml::FWD_SMEM, ss.s>>>(w.x.as<__nv_bfloat16>(), M, w.wpack.as<__nv_bfloat16>(),
+                                                            w.params.as<float>(), w.y.as<float>(), nullptr);
+    MLP_CUDA(cudaGetLastError());
+    MLP_CUDA(cudaMemcpyAsync(y, w.y.p, sizeof(float) * M, cudaMemcpyDeviceToHost, ss.s));
+    MLP_CUDA(cudaStreamSynchronize(ss.s));
+    return BTE_OK;
+}
+
+bte_status bte_mlp_gradient(const float* X, const float* Y, int M, const float* params, float* grad, double* loss) {
+    namespace ml = bte::mlp;
+    if (!X || !Y || !params || !grad || M <= 0) return BTE_ERR_INVALID_ARGUMENT;
+    ScopedStream ss;
+    MLP_CUDA(cudaStreamCreateWithFlags(&ss.s, cudaStreamNonBlocking));
+    MlpWork w;
+    bte_status rc = mlp_alloc(w, M);
+    if (rc) return rc;
+    DevBuf xf;
+    MLP_CUDA(xf.alloc(sizeof(float) * (size_t)M * ml::IN));
+    MLP_CUDA(cudaMemcpyAsync(xf.p, X, sizeof(float) * (size_t)M * ml::IN, cudaMemcpyHostToDevice, ss.s));
+    MLP_CUDA(cudaMemcpyAsync(w.t.p, Y, sizeof(float) * M, cudaMemcpyHostToDevice, ss.s));
+    MLP_CUDA(cudaMemcpyAsync(w.params.p, params, sizeof(float) * ml::NPARAM, cudaMemcpyHostToDevice, ss.s));
+    ml::k_features_bf16<<<(M * ml::IN_PAD + 255) / 256, 256, 0, ss.s>>>(xf.as<float>(), M, w.x.as<__nv_bfloat16>());
+    rc = mlp_pack(w, ss.s);
+    if (rc) return rc;
+    rc = mlp_loss_grad(w, M, ss.s, loss);
+    if (rc) return rc;
+    MLP_CUDA(cudaMemcpyAsync(grad, w.grad.p, sizeof(float) * ml::NPARAM, cudaMemcpyDeviceToHost, ss.s));
+    MLP_CUDA(cudaStreamSynchronize(ss.s));
+    return BTE_OK;
+}
+
+bte_status bte_mlp_train(const float* X, const float* Y, int M, int steps, int batch, float lr, unsigned seed,
+                         float* params, float* loss_hist) {
+    namespace ml = bte::mlp;
+    using bf = __nv_bfloat16;
+    if (!X || !Y || !params || M <= 0 || steps <= 0 || batch <= 0 || !(lr > 0)) return BTE_ERR_INVALID_ARGUMENT;
+    batch = std::min(batch, M);
+    ScopedStream ss;
+    MLP_CUDA(cudaStreamCreateWithFlags(&ss.s, cudaStreamNonBlocking));
+    cudaStream_t st = ss.s;
+    MlpWork w;
+    bte_status rc = mlp_alloc(w, batch);
+    if (rc) return rc;
+    DevBuf xf;
+    MLP_CUDA(xf.alloc(sizeof(float) * (size_t)M * ml::IN));
+    MLP_CUDA(w.xall.alloc(sizeof(bf) * (size_t)M * ml::IN_PAD));
+    MLP_CUDA(w.yall.alloc(sizeof(float) * M));
+    MLP_CUDA(w.idx.alloc(sizeof(int) * M));
+    MLP_CUDA(w.m.alloc(sizeof(float) * ml::NPARAM));
+    MLP_CUDA(w.v.alloc(sizeof(float) * ml::NPARAM));
+    MLP_CUDA(cudaMemsetAsync(w.m.p, 0, sizeof(float) * ml::NPARAM, st));
+    MLP_CUDA(cudaMemsetAsync(w.v.p, 0, sizeof(float) * ml::NPARAM, st));
+    MLP_CUDA(cudaMemcpyAsync(xf.p, X, sizeof(float) * (size_t)M * ml::IN, cudaMemcpyHostToDevice, st));
+    MLP_CUDA(cudaMemcpyAsync(w.yall.p, Y, sizeof(float) * M, cudaMemcpyHostToDevice, st));
+    MLP_CUDA(cudaMemcpyAsync(w.params.p, params, sizeof(float) * ml::NPARAM, cudaMemcpyHostToDevice, st));
+    ml::k_features_bf16<<<(M * ml::IN_PAD + 255) / 256, 256, 0, st>>>(xf.as<float>(), M, w.xall.as<bf>());
+    MLP_CUDA(cudaGetLastError());
+    std::mt19937 rng(seed);
+    std::vector<int> perm(M);
+    for (int i = 0; i < M; ++i) perm[i] = i;
+    int pos = M;  // force a shuffle on the first step
+    const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+    float c1 = 1.f, c2 = 1.f;
+    for (int step = 0; step < steps; ++step) {
+        if (pos + batch > M) {
+            std::shuffle(perm.begin(), perm.end(), rng);
+            MLP_CUDA(cudaMemcpyAsync(w.idx.p, perm.data(), sizeof(int) * M, cudaMemcpyHostToDevice, st));
+            MLP_CUDA(cudaStreamSynchronize(st));  // perm is reshuffled on the host next time
+            pos = 0;
+        }
+        ml::k_gather<<<(batch * ml::IN_PAD + 255) / 256, 256, 0, st>>>(w.xall.as<bf>(), w.yall.as<float>(),
+                                                                       w.idx.as<int>() + pos, batch, w.x.as<bf>(),
+                                                                       w.t.as<float>());
+        pos += batch;
+        rc = mlp_pack(w, st);
+        if (rc) return rc;
+        double loss = 0;
+        rc = mlp_loss_grad(w, batch, st, loss_hist ? &loss : nullptr);
+        if (rc) return rc;
+        if (loss_hist) loss_hist[step] = (float)loss;
+        c1 *= b1;
+        c2 *= b2;
+        ml::k_adam<<<(ml::NPARAM + 255) / 256, 256, 0, st>>>(w.params.as<float>(), w.grad.as<float>(), w.m.as<float>(),
+                                                              w.v.as<float>(), lr, b1, b2, eps, 1.f - c1, 1.f - c2);
+        MLP_CUDA(cudaGetLastError());
+    }
+    MLP_CUDA(cudaMemcpyAsync(params, w.params.p, sizeof(float) * ml::NPARAM, cudaMemcpyDeviceToHost, st));
+    MLP_CUDA(cudaStreamSynchronize(st));
+    return BTE_OK;
+}
+
+}  // extern "C"

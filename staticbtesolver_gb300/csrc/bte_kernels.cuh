@@ -51,6 +51,11 @@ __device__ __forceinline__ void block_sum(double (&v)[K], double (*smem)[NWARP])
         }
 }
 
+// Fused multiply-add in the vector type: fmaf for float, fma for double
+// (a plain fma() on floats would promote them to FP64).
+__device__ __forceinline__ float fmat(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ double fmat(double a, double b, double c) { return fma(a, b, c); }
+
 // Sum of the per-chunk partials of one system, in chunk order.
 __device__ __forceinline__ double sum_parts(const double* p, int n) {
     double s = 0;
@@ -204,7 +209,7 @@ __global__ void __launch_bounds__(THREADS) k_bicg_init(Op op, BicgVecs<T> v, Bic
         v.invD[o + c] = (T)op.inv_diag(y, c);
         v.r[o + c] = bb; v.p[o + c] = bb; v.rw[o + c] = bb; v.q[o + c] = 0;
         x[c] = 0;
-        acc_t = fma(bb, bb, acc_t);
+        acc_t = fmat(bb, bb, acc_t);
     }
     double acc[2] = {(double)acc_t, (double)acc_t};
     block_sum<2>(acc, sm);
@@ -245,7 +250,7 @@ __device__ __forceinline__ void bicg_restart_chunk(const Op& op, const BicgVecs<
         const T rh = bb * (T)6.8 + (T)0.6;
         x[c] = 0; v.q[o + c] = 0; v.p[o + c] = 0; v.r[o + c] = bb;
         v.rw[o + c] = rh;
-        acc_t = fma(rh, bb, acc_t);
+        acc_t = fmat(rh, bb, acc_t);
     }
     double acc[1] = {(double)acc_t};
     block_sum<1>(acc, sm);
@@ -298,8 +303,8 @@ __global__ void __launch_bounds__(THREADS) k_bicg_p(Op op, BicgVecs<T> v, BicgSt
     const size_t o = (size_t)y * v.Np;
     BTE_CELL_LOOP(c) {
         // cublasDaxpy(-omega, q, p); cublasDscal(beta, p); cublasDaxpy(1, r, p)
-        T pv = fma(-om, v.q[o + c], v.p[o + c]);
-        pv = fma(bt, pv, v.r[o + c]);
+        T pv = fmat(-om, v.q[o + c], v.p[o + c]);
+        pv = fmat(bt, pv, v.r[o + c]);
         v.p[o + c] = pv;
         v.ph[o + c] = v.invD[o + c] * pv;
     }
@@ -318,7 +323,7 @@ __global__ void __launch_bounds__(THREADS) k_bicg_spmv1(Op op, BicgVecs<T> v, Bi
     BTE_CELL_LOOP(c) {
         const T qv = op.template apply<T>(y, c, ph);
         v.q[o + c] = qv;
-        acc_t = fma(v.rw[o + c], qv, acc_t);
+        acc_t = fmat(v.rw[o + c], qv, acc_t);
     }
     double acc[1] = {(double)acc_t};
     block_sum<1>(acc, sm);
@@ -347,7 +352,7 @@ __global__ void __launch_bounds__(THREADS) k_bicg_s(Op op, BicgVecs<T> v, BicgSt
     const T al = (T)alpha;
     const size_t o = (size_t)y * v.Np;
     BTE_CELL_LOOP(c) {
-        const T s = fma(-al, v.q[o + c], v.r[o + c]);
+        const T s = fmat(-al, v.q[o + c], v.r[o + c]);
         v.r[o + c] = s;
         v.z[o + c] = v.invD[o + c] * s;
     }
@@ -366,8 +371,8 @@ __global__ void __launch_bounds__(THREADS) k_bicg_spmv2(Op op, BicgVecs<T> v, Bi
     BTE_CELL_LOOP(c) {
         const T tv = op.template apply<T>(y, c, z);
         v.t[o + c] = tv;
-        a0 = fma(tv, v.r[o + c], a0);
-        a1 = fma(tv, tv, a1);
+        a0 = fmat(tv, v.r[o + c], a0);
+        a1 = fmat(tv, tv, a1);
     }
     double acc[2] = {(double)a0, (double)a1};
     block_sum<2>(acc, sm);
@@ -393,13 +398,13 @@ __global__ void __launch_bounds__(THREADS) k_bicg_x(Op op, BicgVecs<T> v, BicgSt
     T* x = op.x_of(y);
     T a0 = 0, a1 = 0;
     BTE_CELL_LOOP(c) {
-        T xv = fma(al, v.ph[o + c], x[c]);
-        xv = fma(om, v.z[o + c], xv);
+        T xv = fmat(al, v.ph[o + c], x[c]);
+        xv = fmat(om, v.z[o + c], xv);
         x[c] = xv;
-        const T r = fma(-om, v.t[o + c], v.r[o + c]);
+        const T r = fmat(-om, v.t[o + c], v.r[o + c]);
         v.r[o + c] = r;
-        a0 = fma(r, r, a0);
-        a1 = fma(v.rw[o + c], r, a1);
+        a0 = fmat(r, r, a0);
+        a1 = fmat(v.rw[o + c], r, a1);
     }
     double acc[2] = {(double)a0, (double)a1};
     block_sum<2>(acc, sm);

@@ -287,6 +287,8 @@ int upload(const Prepared& P, bte_ctx* ctx) {
     rc = bte_set_quadrature(ctx, P.n_dir, P.s.data(), P.S.data(), P.omega.data(), P.DM, P.num_theta, P.num_phi,
                             P.solid_angle, P.T_ref);
     if (rc) return rc;
+    rc = bte_set_centroids(ctx, P.centroid.data());
+    if (rc) return rc;
     rc = bte_set_bands(ctx, P.n_band, P.vg.data(), P.tau.data(), P.C.data(), P.Lr.data());
     if (rc) return rc;
     return bte_set_bcs(ctx, P.n_bc, P.bc_index.data(), P.bc_type.data(), P.bc_T.data());

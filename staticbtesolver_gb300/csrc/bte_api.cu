@@ -1125,6 +1125,23 @@ extern "C" bte_status bte_solve(bte_ctx* ctx, const bte_options* opts, bte_repor
             BTE_CUDA(cudaStreamSynchronize(st));
             ctx->history_rows = it + 1;
         }
+        float t01 = 0, t12 = 0, t23 = 0;
+        cudaEventElapsedTime(&t01, ev[0], ev[1]);
+        cudaEventElapsedTime(&t12, ev[1], ev[2]);
+        cudaEventElapsedTime(&t23, ev[2], ev[3]);
+        rep.ms_rhs += t01;
+        rep.ms_inner += t12;
+        rep.ms_reduce += t23;
+        rep.ms_total += t01 + t12 + t23;
+        ctx->margins.push_back(m);
+        rep.n_iter = it + 1;
+        rep.final_margin = m;
+        if (o.on_iteration) o.on_iteration(o.user, it, m, (double)(t01 + t12 + t23));
+        if (!std::isfinite(m)) {
+            result = BTE_ERR_NUMERICAL;
+            ctx->err = "non-finite margin in outer iteration " + std::to_string(it);
+            break;
+        }
         if (m <= o.tol) {
             rep.converged = 1;
             result = BTE_OK;

@@ -162,18 +162,20 @@ bte_status bte_get_margins(bte_ctx* ctx, double* margins, int cap, int* n);
 /* Learned outer-iteration acceleration (no counterpart in the reference; the
  * plain source iteration still runs to the same margin, so the accelerator
  * changes how fast the fixed point is reached, not which one).  Every
- * accel_every outer iterations a per-cell MLP (8 -> 128 -> 128 -> 128 -> 1,
- * BF16 weights, FP32 accumulation on the tensor cores) maps the cell's last
- * four temperatures and its geometry to an extrapolated equilibrium
- * temperature; T and the equilibrium energy density are reset to it.  If the
- * margin accel_every-1 iterations after a jump is not below the margin at the
- * jump, extrapolation stops for the rest of the solve.
- * Features per cell (d_i = T_{k-i+1} - T_{k-i}, s = |d1| + |d2| + |d3|):
- *   d1/s, d2/s, d3/s, (T_k - T_ref)/max|T_bc - T_ref|, x and y of the centroid
- *   scaled to [0, 1] over the mesh, log(V / mean V), log10(Kn), Kn =
- *   (sum_b Lr_b v_b tau_b / sum_b Lr_b) / V^(1/dim); output (T* - T_k) / s,
- *   clipped to [-64, 64].  Parameters: FP32, bte_mlp_param_count() values,
- *   W1[8][128] b1 W2[128][128] b2 W3[128][128] b3 W4[128][1] b4. */
+ * accel_every outer iterations each cell's temperature is reset to an
+ * extrapolation from its last four values and the equilibrium energy density
+ * follows.  With d_i = T_{k-i+1} - T_{k-i}, s = |d1| + |d2| + |d3| and the
+ * Aitken estimate A = d1 r / (1 - r) / s (r = d1 / d2, used when 0 < r < 1,
+ * else 0, clipped to +-64): accel = 2 jumps by s A; accel = 1 jumps by
+ * s clip(A + y, +-64), where y is a per-cell MLP's learned correction
+ * (8 -> 128 -> 128 -> 128 -> 1, BF16 weights, FP32 accumulation on the tensor
+ * cores).  MLP inputs: d1/s, d2/s, d3/s, A/64, x and y of the centroid scaled
+ * to [0, 1] over the mesh, log(V / mean V), log10(Kn) with Kn =
+ * (sum_b Lr_b v_b tau_b / sum_b Lr_b) / V^(1/dim).  If the margin
+ * accel_every-1 iterations after a jump is not below the margin at the jump,
+ * extrapolation stops for the rest of the solve.  Parameters: FP32,
+ * bte_mlp_param_count() values, W1[8][128] b1 W2[128][128] b2 W3[128][128] b3
+ * W4[128][1] b4. */
 int bte_mlp_param_count(void);
 bte_status bte_set_mlp(bte_ctx* ctx, const float* params);
 /* Cell centroids [n_cell][3] (used only for the accelerator's features). */

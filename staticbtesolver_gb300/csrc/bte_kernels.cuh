@@ -23,7 +23,7 @@
 namespace bte {
 
 constexpr int THREADS = 256;
-constexpr int CPT = 4;                 // cells per thread per chunk
+constexpr int CPT = 8;                 // cells per thread per chunk
 constexpr int CH = THREADS * CPT;      // cells per block ("chunk")
 constexpr int NWARP = THREADS / 32;
 
@@ -51,15 +51,28 @@ __device__ __forceinline__ void block_sum(double (&v)[K], double (*smem)[NWARP])
         }
 }
 
+// Serial sum of the per-chunk partials (for kernels with one thread per system).
+__device__ __forceinline__ double sum_parts_serial(const double* p, int n) {
+    double s = 0;
+    for (int i = 0; i < n; ++i) s += p[i];
+    return s;
+}
+
 // Fused multiply-add in the vector type: fmaf for float, fma for double
 // (a plain fma() on floats would promote them to FP64).
 __device__ __forceinline__ float fmat(float a, float b, float c) { return fmaf(a, b, c); }
 __device__ __forceinline__ double fmat(double a, double b, double c) { return fma(a, b, c); }
 
-// Sum of the per-chunk partials of one system, in chunk order.
+// Sum of the per-chunk partials of one system.  Each warp loads them in
+// parallel (lane l sums partials l, l+32, ... in order) and combines the lanes
+// with a fixed butterfly, so every warp of every block gets the same value
+// and the order never depends on timing.  Must be called by whole warps.
 __device__ __forceinline__ double sum_parts(const double* p, int n) {
+    const int lane = threadIdx.x & 31;
     double s = 0;
-    for (int i = 0; i < n; ++i) s += p[i];
+    for (int i = lane; i < n; i += 32) s += p[i];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
     return s;
 }
 
@@ -224,7 +237,7 @@ __global__ void __launch_bounds__(THREADS) k_bicg_init(Op op, BicgVecs<T> v, Bic
 __global__ void k_bicg_init_scalars(BicgState st, const int* skip) {
     int y = blockIdx.x * blockDim.x + threadIdx.x;
     if (y >= st.S) return;
-    double n0 = sqrt(sum_parts(st.P(PK_RR0, y), st.nchunk));
+    double n0 = sqrt(sum_parts_serial(st.P(PK_RR0, y), st.nchunk));
     st.nrm0[y] = n0;
     st.nrmr[y] = n0;
     st.rho[y] = 1.0; st.rho[st.S + y] = 1.0;

@@ -434,6 +434,15 @@ struct FeatureGeom {
     double vmean, xmin, xspan, ymin, yspan, kn_num, inv_dim, T_ref, dT_bc;
 };
 
+// Per-cell Aitken estimate of the remaining change, in units of s:
+// r = d1 / d2; A = d1 r / (1 - r) / s when 0 < r < 1, else 0; clipped to +-64.
+__device__ __forceinline__ double aitken_norm(double d1, double d2, double s) {
+    if (d2 == 0.0) return 0.0;
+    const double r = d1 / d2;
+    if (!(r > 0.0 && r < 1.0)) return 0.0;
+    return fmin(fmax(d1 * r / (1.0 - r) / s, -64.0), 64.0);
+}
+
 // Per-cell features from the last four temperatures (ring slots s0 = newest).
 __global__ void k_accel_features(const double* __restrict__ ring, int s0, int s1, int s2, int s3, size_t Np, int n,
                                  FeatureGeom fg, __nv_bfloat16* __restrict__ x, double* __restrict__ scale) {
@@ -448,7 +457,7 @@ __global__ void k_accel_features(const double* __restrict__ ring, int s0, int s1
     f[0] = d1 / s;
     f[1] = d2 / s;
     f[2] = d3 / s;
-    f[3] = (t0 - fg.T_ref) / fg.dT_bc;
+    f[3] = aitken_norm(d1, d2, s) / 64.0;
     f[4] = fg.xspan > 0 ? (fg.centroid[3 * c] - fg.xmin) / fg.xspan : 0.0;
     f[5] = fg.yspan > 0 ? (fg.centroid[3 * c + 1] - fg.ymin) / fg.yspan : 0.0;
     f[6] = log(V / fg.vmean);
@@ -458,9 +467,10 @@ __global__ void k_accel_features(const double* __restrict__ ring, int s0, int s1
     scale[c] = s;
 }
 
-// Extrapolation step: T = T_k + s * clip(y) (learned, y from the MLP) or the
-// per-cell Aitken limit T_k + d1 r / (1 - r), r = d1 / d2, when 0 < r < 1
-// (capped at 64 s); then ebar[b][c] = C_b / Omega_tot (T - T_ref).
+// Extrapolation step.  A = the per-cell Aitken estimate (aitken_norm) and
+// s = |d1| + |d2| + |d3|; learned: T = T_k + s clip(A + y, +-64) with y the
+// MLP's learned correction; Aitken alone: T = T_k + s A.  Then
+// ebar[b][c] = C_b / Omega_tot (T - T_ref).
 __global__ void k_accel_apply(const double* __restrict__ ring, int s0, int s1, int s2, size_t Np, int n,
                               const double* __restrict__ scale, const float* __restrict__ y, int learned,
                               const double* __restrict__ Cb, int n_band, double solid_angle, double T_ref,
@@ -468,19 +478,12 @@ __global__ void k_accel_apply(const double* __restrict__ ring, int s0, int s1, i
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= n) return;
     const double t0 = ring[(size_t)s0 * Np + c];
-    double jump;
-    if (learned) {
-        jump = scale[c] * fmin(64.0, fmax(-64.0, (double)y[c]));
-    } else {
-        const double d1 = t0 - ring[(size_t)s1 * Np + c];
-        const double d2 = ring[(size_t)s1 * Np + c] - ring[(size_t)s2 * Np + c];
-        jump = 0.0;
-        if (d2 != 0.0) {
-            const double r = d1 / d2;
-            if (r > 0.0 && r < 1.0) jump = fmin(fmax(d1 * r / (1.0 - r), -64.0 * scale[c]), 64.0 * scale[c]);
-        }
-    }
-    const double Tn = t0 + jump;
+    const double d1 = t0 - ring[(size_t)s1 * Np + c];
+    const double d2 = ring[(size_t)s1 * Np + c] - ring[(size_t)s2 * Np + c];
+    const double s = scale[c];
+    double u = aitken_norm(d1, d2, s);
+    if (learned) u = fmin(64.0, fmax(-64.0, u + (double)y[c]));
+    const double Tn = t0 + s * u;
     T[c] = Tn;
     for (int b = 0; b < n_band; ++b) ebar[(size_t)b * Np + c] = Cb[b] / solid_angle * (Tn - T_ref);
 }

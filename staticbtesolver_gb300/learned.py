@@ -7,7 +7,8 @@ four outer temperatures and its geometry and predicts the converged
 equilibrium temperature; every few iterations the solver jumps there and the
 plain iteration continues to the same margin.  This module
 
-* computes the features exactly as the device kernel k_accel_features does,
+* computes the features exactly as the device kernel k_accel_features does
+  (the network learns a correction to each cell's Aitken estimate),
 * generates training data from the solver's own iterate histories on seeded
   synthetic problems (bte_options.keep_history),
 * trains the network with the project's GPU kernels (bte_mlp_train), and
@@ -54,30 +55,41 @@ def feature_geometry(arrays: dict) -> dict:
                 T_ref=arrays["T_ref"], dT=dT if dT > 0 else 1.0, centroid=cen, volume=V)
 
 
+def aitken_norm(d1, d2, s):
+    """Per-cell Aitken estimate of the remaining change in units of s (as aitken_norm in bte_mlp.cuh)."""
+    with np.errstate(divide="ignore", invalid="ignore"):
+        r = np.where(d2 != 0.0, d1 / np.where(d2 != 0.0, d2, 1.0), 0.0)
+        ok = (r > 0.0) & (r < 1.0)
+        a = np.where(ok, d1 * r / np.where(ok, 1.0 - r, 1.0) / s, 0.0)
+    return np.clip(a, -CLIP, CLIP)
+
+
 def features(t0, t1, t2, t3, fg: dict):
-    """Features [n][8] (float32) and scale s [n] from T_k, T_{k-1}, T_{k-2}, T_{k-3}."""
+    """Features [n][8] (float32), scale s [n] and Aitken estimate A [n] from T_k .. T_{k-3}."""
     d1, d2, d3 = t0 - t1, t1 - t2, t2 - t3
     s = np.abs(d1) + np.abs(d2) + np.abs(d3) + 1e-300
+    A = aitken_norm(d1, d2, s)
     cen, V = fg["centroid"], fg["volume"]
     f = np.empty((len(t0), 8))
     f[:, 0], f[:, 1], f[:, 2] = d1 / s, d2 / s, d3 / s
-    f[:, 3] = (t0 - fg["T_ref"]) / fg["dT"]
+    f[:, 3] = A / CLIP
     f[:, 4] = (cen[:, 0] - fg["xmin"]) / fg["xspan"] if fg["xspan"] > 0 else 0.0
     f[:, 5] = (cen[:, 1] - fg["ymin"]) / fg["yspan"] if fg["yspan"] > 0 else 0.0
     f[:, 6] = np.log(V / fg["vmean"])
     f[:, 7] = np.log10(fg["kn_num"] / V ** fg["inv_dim"])
-    return f.astype(np.float32), s
+    return f.astype(np.float32), s, A
 
 
 def samples_from_history(hist: np.ndarray, fg: dict, every: int = 2, rng=None, max_rows: int = 0):
     """(X, Y) pairs from one solve's temperature history (rows = outer iterations).
 
-    Target: (T* - T_k) / s clipped to +-64, T* = the last (converged) row."""
+    Target: the correction to the Aitken estimate, clip((T* - T_k) / s, +-64) - A,
+    with T* = the last (converged) row."""
     T_star = hist[-1]
     X, Y = [], []
     for k in range(3, len(hist) - 1, every):
-        f, s = features(hist[k], hist[k - 1], hist[k - 2], hist[k - 3], fg)
-        y = np.clip((T_star - hist[k]) / s, -CLIP, CLIP).astype(np.float32)
+        f, s, A = features(hist[k], hist[k - 1], hist[k - 2], hist[k - 3], fg)
+        y = (np.clip((T_star - hist[k]) / s, -CLIP, CLIP) - A).astype(np.float32)
         X.append(f)
         Y.append(y)
     X, Y = np.concatenate(X), np.concatenate(Y)

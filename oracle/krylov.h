@@ -222,7 +222,7 @@ inline KrylovResult bicgstab_jacobi(const Csr& A, const double* b, double* x, do
         spmv(A, z.data(), t.data());
         double ts = dot(n, t.data(), r.data());
         double tt = dot(n, t.data(), t.data());
-        omega = ts / tt;
+        omega = tt > 0.0 ? ts / tt : 0.0;  // s == 0: the reference would form 0/0 here
         for (int k = 0; k < n; ++k) x[k] += alpha * ph[k];  // two axpys, :283 and :285
         for (int k = 0; k < n; ++k) x[k] += omega * z[k];
         for (int k = 0; k < n; ++k) r[k] -= omega * t[k];

@@ -403,7 +403,11 @@ __global__ void __launch_bounds__(THREADS) k_bicg_x(Op op, BicgVecs<T> v, BicgSt
     const int par = i & 1;
     if (st.done[y] | st.flagA[par * st.S + y] | st.flagB[par * st.S + y]) return;
     const bool lead = blockIdx.x == 0 && threadIdx.x == 0;
-    const double omega = sum_parts(st.P(PK_TS, y), st.nchunk) / sum_parts(st.P(PK_TT, y), st.nchunk);
+    // t.t == 0 means s == 0: the half step already solved the system.  The
+    // reference would divide 0 by 0 here (src/bicgstab.hpp:280); omega = 0
+    // keeps x += alpha ph, r = s = 0, and the next p-update retires the system.
+    const double tt = sum_parts(st.P(PK_TT, y), st.nchunk);
+    const double omega = tt > 0.0 ? sum_parts(st.P(PK_TS, y), st.nchunk) / tt : 0.0;
     const double alpha = st.alpha[y];
     if (lead) st.omega[y] = omega;
     const T al = (T)alpha, om = (T)omega;

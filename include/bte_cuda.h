@@ -167,7 +167,7 @@ bte_status bte_get_margins(bte_ctx* ctx, double* margins, int cap, int* n);
  * follows.  With d_i = T_{k-i+1} - T_{k-i}, s = |d1| + |d2| + |d3| and the
  * Aitken estimate A = d1 r / (1 - r) / s (r = d1 / d2, used when 0 < r < 1,
  * else 0, clipped to +-64): accel = 2 jumps by s A; accel = 1 jumps by
- * s clip(A + y, +-64), where y is a per-cell MLP's learned correction
+ * s clip(A + clip(y, +-8), +-64), where y is a per-cell MLP's learned correction
  * (8 -> 128 -> 128 -> 128 -> 1, BF16 weights, FP32 accumulation on the tensor
  * cores).  MLP inputs: d1/s, d2/s, d3/s, A/64, x and y of the centroid scaled
  * to [0, 1] over the mesh, log(V / mean V), log10(Kn) with Kn =

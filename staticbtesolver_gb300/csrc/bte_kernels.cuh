@@ -210,6 +210,10 @@ struct FaceFluxOp32 {
 };
 
 // K0: x = 0, r = p = r_hat = b, q = 0, invD; partial ||b||^2 (src/bicgstab.hpp:146-162).
+// With rho_0 = alpha = omega = 1 the reference's first update is
+// p_1 = r + ||b||^2 b: the same direction scaled by 1 + ||b||^2, harmless in
+// FP64 but an FP32 overflow once ||b||^2 exceeds ~1e19 (t.t and r_hat.q become
+// inf - inf).  The FP32 solve therefore starts from p_0 = 0, so p_1 = r.
 template <typename Op, typename T>
 __global__ void __launch_bounds__(THREADS) k_bicg_init(Op op, BicgVecs<T> v, BicgState st) {
     __shared__ double sm[2][NWARP];
@@ -220,7 +224,9 @@ __global__ void __launch_bounds__(THREADS) k_bicg_init(Op op, BicgVecs<T> v, Bic
     BTE_CELL_LOOP(c) {
         const T bb = v.b[o + c];
         v.invD[o + c] = (T)op.inv_diag(y, c);
-        v.r[o + c] = bb; v.p[o + c] = bb; v.rw[o + c] = bb; v.q[o + c] = 0;
+        v.r[o + c] = bb; v.rw[o + c] = bb; v.q[o + c] = 0;
+        if constexpr (sizeof(T) == sizeof(float)) v.p[o + c] = 0;
+        else v.p[o + c] = bb;
         x[c] = 0;
         acc_t = fmat(bb, bb, acc_t);
     }

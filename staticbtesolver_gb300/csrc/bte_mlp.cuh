@@ -468,8 +468,8 @@ __global__ void k_accel_features(const double* __restrict__ ring, int s0, int s1
 }
 
 // Extrapolation step.  A = the per-cell Aitken estimate (aitken_norm) and
-// s = |d1| + |d2| + |d3|; learned: T = T_k + s clip(A + y, +-64) with y the
-// MLP's learned correction; Aitken alone: T = T_k + s A.  Then
+// s = |d1| + |d2| + |d3|; learned: T = T_k + s clip(A + clip(y, +-8), +-64)
+// with y the MLP's learned correction; Aitken alone: T = T_k + s A.  Then
 // ebar[b][c] = C_b / Omega_tot (T - T_ref).
 __global__ void k_accel_apply(const double* __restrict__ ring, int s0, int s1, int s2, size_t Np, int n,
                               const double* __restrict__ scale, const float* __restrict__ y, int learned,
@@ -482,7 +482,7 @@ __global__ void k_accel_apply(const double* __restrict__ ring, int s0, int s1, i
     const double d2 = ring[(size_t)s1 * Np + c] - ring[(size_t)s2 * Np + c];
     const double s = scale[c];
     double u = aitken_norm(d1, d2, s);
-    if (learned) u = fmin(64.0, fmax(-64.0, u + (double)y[c]));
+    if (learned) u = fmin(64.0, fmax(-64.0, u + fmin(8.0, fmax(-8.0, (double)y[c]))));
     const double Tn = t0 + s * u;
     T[c] = Tn;
     for (int b = 0; b < n_band; ++b) ebar[(size_t)b * Np + c] = Cb[b] / solid_angle * (Tn - T_ref);

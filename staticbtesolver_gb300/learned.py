@@ -26,6 +26,8 @@ from . import synth
 
 NPARAM = 34305
 CLIP = 64.0
+CORR = 8.0  # the learned correction is clipped to +-CORR (as in k_accel_apply)
+EVERY = 6  # outer iterations between extrapolations used with the committed weights
 DATA = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data")
 WEIGHTS = os.path.join(DATA, "mlp_accel.npy")
 
@@ -80,24 +82,54 @@ def features(t0, t1, t2, t3, fg: dict):
     return f.astype(np.float32), s, A
 
 
-def samples_from_history(hist: np.ndarray, fg: dict, every: int = 2, rng=None, max_rows: int = 0):
+def jump_rows(margins, every: int = EVERY, tol: float = 1e-5):
+    """Outer iterations at which bte_solve extrapolated (its rule, replayed from the margins):
+    from iteration 3 on, every `every` iterations, until the margin `every`-1 iterations
+    after a jump is not below the margin at it."""
+    on, last, m_at, out = True, -1, 0.0, []
+    for it, m in enumerate(margins):
+        if not np.isfinite(m) or m <= tol:
+            break
+        if on and last >= 0 and it == last + every - 1 and m >= m_at:
+            on = False
+        if on and it >= 3 and (last < 0 or it - last >= every):
+            out.append(it)
+            last, m_at = it, m
+    return out
+
+
+def samples_from_history(hist: np.ndarray, fg: dict, every: int = 2, rng=None, max_rows: int = 0, jumps=()):
     """(X, Y) pairs from one solve's temperature history (rows = outer iterations).
 
-    Target: the correction to the Aitken estimate, clip((T* - T_k) / s, +-64) - A,
-    with T* = the last (converged) row."""
+    Target: the correction to the Aitken estimate, clip(clip((T* - T_k) / s, +-64) - A, +-8),
+    with T* = the last (converged) row.  Row j of a run that extrapolated at j is the
+    field before the jump, so windows T_{k-3} .. T_k with a jump j in [k-3, k-1] are skipped."""
     T_star = hist[-1]
+    jset = set(int(j) for j in jumps)
     X, Y = [], []
     for k in range(3, len(hist) - 1, every):
+        if any(j in jset for j in range(k - 3, k)):
+            continue
         f, s, A = features(hist[k], hist[k - 1], hist[k - 2], hist[k - 3], fg)
-        y = (np.clip((T_star - hist[k]) / s, -CLIP, CLIP) - A).astype(np.float32)
+        y = np.clip(np.clip((T_star - hist[k]) / s, -CLIP, CLIP) - A, -CORR, CORR).astype(np.float32)
         X.append(f)
         Y.append(y)
+    if not X:
+        return np.zeros((0, 8), np.float32), np.zeros(0, np.float32)
     X, Y = np.concatenate(X), np.concatenate(Y)
     if max_rows and len(Y) > max_rows:
         rng = rng or np.random.default_rng(0)
         sel = rng.choice(len(Y), max_rows, replace=False)
         X, Y = X[sel], Y[sel]
     return X, Y
+
+
+def mirrored(X, Y):
+    """The same samples with T reflected about T_ref: the difference features and the
+    Aitken feature change sign and so does the target (doubles the data, makes the fit odd)."""
+    Xm = X.copy()
+    Xm[:, :4] *= -1.0
+    return np.concatenate([X, Xm]), np.concatenate([Y, -Y])
 
 
 def training_problems(n: int, seed: int = 7):
@@ -129,8 +161,11 @@ def write_problem(spec: dict, out_dir: str) -> synth.Problem:
     return synth.Problem("train", geo, band, bc, 2, 8, 8, 300.0, 20000, spec["side"], spec["side"], 0.0)
 
 
-def generate(specs, max_rows_per_problem: int = 40000, device: int = 0, seed: int = 0):
-    """Run each problem with the sweep form keeping the T history; return X, Y."""
+def generate(specs, max_rows_per_problem: int = 40000, device: int = 0, seed: int = 0, accel: int = 0,
+             params=None, accel_every: int = EVERY):
+    """Run each problem with the sweep form keeping the T history; return X, Y, info.
+    accel = 2 (Aitken) or 1 (learned, `params`) records the trajectories the
+    accelerator itself produces, so the network is trained on the states it meets."""
     import staticbtesolver_gb300 as S
 
     rng = np.random.default_rng(seed)
@@ -140,13 +175,19 @@ def generate(specs, max_rows_per_problem: int = 40000, device: int = 0, seed: in
             p = write_problem(spec, os.path.join(tmp, str(i)))
             prob = S.Problem(p.geo, p.bc_file, p.band_file, p.DM, p.num_theta, p.num_phi, p.T_ref, p.L_x, p.L_y, p.L_z)
             ctx = S.Context(device).load(prob)
-            st, rep = ctx.solve(max_iter=p.max_iter, tol=1e-5, form=S.FORM_SWEEP, keep_history=True)
+            if accel == 1:
+                ctx.set_mlp(params)
+            st, rep = ctx.solve(max_iter=p.max_iter, tol=1e-5, form=S.FORM_SWEEP, keep_history=True, accel=accel,
+                                accel_every=accel_every)
             hist = ctx.history()
+            jumps = jump_rows(ctx.margins(), accel_every) if accel else []
             ctx.close()
-            X, Y = samples_from_history(hist, feature_geometry(prob.arrays()), rng=rng, max_rows=max_rows_per_problem)
+            assert len(jumps) == rep.accel_steps, (len(jumps), rep.accel_steps)
+            X, Y = samples_from_history(hist, feature_geometry(prob.arrays()), rng=rng, max_rows=max_rows_per_problem,
+                                        jumps=jumps)
             Xs.append(X)
             Ys.append(Y)
-            info.append(dict(spec, n_iter=rep.n_iter))
+            info.append(dict(spec, n_iter=rep.n_iter, accel=accel, jumps=rep.accel_steps))
     return np.concatenate(Xs), np.concatenate(Ys), info
 
 
@@ -164,6 +205,62 @@ def train(X, Y, steps=3000, batch=4096, lr=1e-3, seed=0, params=None):
     if st != 0:
         raise S.BteError(st, L.bte_last_error(None).decode())
     return p, loss
+
+
+def predict(params, X):
+    """MLP outputs on the GPU (bte_mlp_predict)."""
+    import staticbtesolver_gb300 as S
+
+    L, _ = S._load()
+    X = np.ascontiguousarray(X, np.float32)
+    p = np.ascontiguousarray(params, np.float32)
+    y = np.zeros(len(X), np.float32)
+    st = L.bte_mlp_predict(X.ctypes.data_as(C.c_void_p), len(X), p.ctypes.data_as(C.c_void_p),
+                           y.ctypes.data_as(C.c_void_p))
+    if st != 0:
+        raise S.BteError(st, L.bte_last_error(None).decode())
+    return y
+
+
+def shrink(params, X_val, Y_val):
+    """Scale the output layer by lam = clip(<t, y> / <y, y>, 0, 1) fitted on held-out rows,
+    so the correction is only as large as it predicts well.  Returns (params, lam)."""
+    y = np.clip(predict(params, X_val).astype(np.float64), -CORR, CORR)
+    lam = float(np.clip(np.dot(Y_val, y) / max(np.dot(y, y), 1e-30), 0.0, 1.0))
+    return scaled(params, lam), lam
+
+
+def scaled(params, lam):
+    """The network with its output (last layer weights and bias) multiplied by lam."""
+    p = np.array(params, np.float32)
+    p[NPARAM - 129:] *= lam
+    return p
+
+
+def select_scale(params, specs, lams=(0.0, 0.25, 0.5, 0.75, 1.0), accel_every: int = EVERY, device: int = 0):
+    """Pick the output scale by what it does: total outer iterations to margin <= 1e-5 of
+    learned-accelerated solves on held-out problems, for each lam (lam = 0 is the Aitken
+    extrapolation itself).  Returns (params scaled by the best lam, {lam: iterations})."""
+    import staticbtesolver_gb300 as S
+
+    totals = {}
+    with tempfile.TemporaryDirectory() as tmp:
+        probs = []
+        for i, spec in enumerate(specs):
+            p = write_problem(spec, os.path.join(tmp, str(i)))
+            probs.append((S.Problem(p.geo, p.bc_file, p.band_file, p.DM, p.num_theta, p.num_phi, p.T_ref, p.L_x,
+                                    p.L_y, p.L_z), p.max_iter))
+        for lam in lams:
+            tot = 0
+            for prob, max_iter in probs:
+                ctx = S.Context(device).load(prob)
+                ctx.set_mlp(scaled(params, lam))
+                st, rep = ctx.solve(max_iter=max_iter, tol=1e-5, form=S.FORM_SWEEP, accel=1, accel_every=accel_every)
+                ctx.close()
+                tot += rep.n_iter if st == 0 else 10 * max_iter
+            totals[float(lam)] = tot
+    best = min(totals, key=lambda k: (totals[k], k))
+    return scaled(params, best), totals
 
 
 def load(path: str = WEIGHTS) -> np.ndarray:

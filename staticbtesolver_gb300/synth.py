@@ -318,6 +318,12 @@ class Problem:
     def args(self):
         return asdict(self)
 
+    def btecmd_flags(self):
+        """The BTEcmd command line of this problem (-m is the band file, -b the boundary file)."""
+        return ["-g", self.geo, "-m", self.band_file, "-b", self.bc_file, "-d", str(self.DM), "-t",
+                str(self.num_theta), "-p", str(self.num_phi), "-T", repr(self.T_ref), "-I", str(self.max_iter),
+                "-x", repr(self.L_x), "-y", repr(self.L_y), "-z", repr(self.L_z)]
+
 
 def make_problem(name: str, out_dir: str, seed: int = 20261203) -> Problem:
     """Write one named synthetic configuration into out_dir and describe it.
@@ -381,3 +387,13 @@ def make_problem(name: str, out_dir: str, seed: int = 20261203) -> Problem:
         n, b = name[len("cube"):].split("_b")
         return cube(int(n), int(b), 1e-8)
     raise ValueError(f"unknown synthetic configuration {name!r}")
+
+
+if __name__ == "__main__":
+    # python -m staticbtesolver_gb300.synth NAME OUT_DIR: write the files, print the BTEcmd flags.
+    import sys
+
+    if len(sys.argv) != 3:
+        sys.exit("usage: python -m staticbtesolver_gb300.synth NAME OUT_DIR")
+    prob = make_problem(sys.argv[1], sys.argv[2])
+    print(" ".join(prob.btecmd_flags()))

@@ -1,0 +1,57 @@
+"""Regenerate tests/golden/full/<name>.npz: a full-size synthetic workload solved by the oracle.
+
+The oracle (oracle/bte_oracle.cpp, the reference's CPU algorithm: ILU(0)-GMRES inner
+solves, margin <= 1e-5 as in src/StaticBTESolver.cpp:798) runs the whole source
+iteration on the workload that the benchmark times.  The fixture keeps the cell
+temperatures, the heat flux per boundary and per band, the margin trajectory, and
+SHA-256 hashes of the generated mesh / band / boundary files so a test can check
+that the generator still writes the same problem.
+
+square20k takes about 40 minutes on 8 host threads.
+
+Usage:  python tests/golden/full/make_full.py [square20k] [--threads 8]
+"""
+from __future__ import annotations
+
+import argparse
+import hashlib
+import json
+import os
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(HERE)))
+sys.path.insert(0, ROOT)
+
+from oracle.oracle import Oracle  # noqa: E402
+from staticbtesolver_gb300 import synth  # noqa: E402
+
+
+def file_hashes(p) -> dict:
+    return {k: hashlib.sha256(open(getattr(p, k), "rb").read()).hexdigest() for k in ("geo", "band_file", "bc_file")}
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("name", nargs="?", default="square20k")
+    ap.add_argument("--threads", type=int, default=8)
+    ap.add_argument("--max-iter", type=int, default=1000)
+    a = ap.parse_args()
+    with tempfile.TemporaryDirectory() as tmp:
+        p = synth.make_problem(a.name, tmp)
+        h = file_hashes(p)
+        o = Oracle(p.geo, p.bc_file, p.band_file, p.DM, p.num_theta, p.num_phi, p.T_ref, p.L_x, p.L_y, p.L_z)
+        t = time.time()
+        r = o.run(a.max_iter, 1e-5, threads=a.threads)
+        el = time.time() - t
+    print(a.name, "outer iterations", r.n_iter, "seconds", round(el, 1), "q", r.q)
+    np.savez_compressed(os.path.join(HERE, f"{a.name}.npz"), T=r.T, q=r.q, q_band=r.q_band, margins=r.margins,
+                        n_iter=r.n_iter, seconds=el, inner_iterations=r.inner["iterations"], hashes=json.dumps(h))
+
+
+if __name__ == "__main__":
+    main()

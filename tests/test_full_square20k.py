@@ -1,0 +1,88 @@
+"""Full-size square20k (20,000 triangles x 40 bands x 32 directions) against the
+oracle's complete run (tests/golden/full/square20k.npz, made by make_full.py:
+ILU(0)-GMRES inner solves, margin <= 1e-5, 198 outer iterations).
+
+The FP64 forms must land within relative L2 1e-6 of the oracle's (T - T_ref)
+field.  The outer-iteration accelerators (Aitken, learned) must reach the same
+margin in fewer outer iterations than the plain iteration, with a field within
+relative L2 1e-5 of the fully converged one (margin <= 1e-10; the oracle's own
+field, stopped at 1e-5, is ~4e-6 from it)."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, rel_l2
+
+FIX = os.path.join(GOLDEN, "full", "square20k.npz")
+
+
+@pytest.fixture(scope="module")
+def full():
+    return np.load(FIX)
+
+
+@pytest.fixture(scope="module")
+def problem(tmp_path_factory):
+    from staticbtesolver_gb300 import synth
+    return synth.make_problem("square20k", str(tmp_path_factory.mktemp("sq20k")))
+
+
+def test_generator_reproduces_fixture_inputs(full, problem):
+    import hashlib
+    want = json.loads(str(full["hashes"]))
+    for k in ("geo", "band_file", "bc_file"):
+        assert hashlib.sha256(open(getattr(problem, k), "rb").read()).hexdigest() == want[k], k
+    assert int(full["n_iter"]) == 198 and full["margins"][-1] <= 1e-5 < full["margins"][-2]
+
+
+def _solve(sbte, p, mlp=None, **kw):
+    prob = sbte.Problem(p.geo, p.bc_file, p.band_file, p.DM, p.num_theta, p.num_phi, p.T_ref, p.L_x, p.L_y, p.L_z)
+    ctx = sbte.Context(0).load(prob)
+    if mlp is not None:
+        ctx.set_mlp(mlp)
+    kw.setdefault("max_iter", 1000)
+    kw.setdefault("tol", 1e-5)
+    st, rep = ctx.solve(**kw)
+    res = ctx.result(st, rep)
+    ctx.close()
+    assert res.status == 0 and res.report["converged"]
+    return res
+
+
+@pytest.fixture(scope="module")
+def converged(sbte, problem):
+    return _solve(sbte, problem, form=sbte.FORM_SWEEP, tol=1e-10, max_iter=5000).T
+
+
+def _q_close(q, q0, rtol):
+    big = np.abs(q0) > 1e-2 * np.abs(q0).max()
+    np.testing.assert_allclose(q[big], q0[big], rtol=rtol)
+
+
+@pytest.mark.gpu
+def test_sweep_matches_full_oracle(sbte, full, problem):
+    res = _solve(sbte, problem, form=sbte.FORM_SWEEP)
+    err = rel_l2(res.T - 300.0, full["T"] - 300.0)
+    print("sweep n_iter", res.report["n_iter"], "rel_l2(T-300)", err)
+    assert abs(res.report["n_iter"] - int(full["n_iter"])) <= 1
+    assert err < 1e-6
+    _q_close(res.q, full["q"], 1e-5)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("accel", ["aitken", "learned"])
+def test_accelerator_gain_at_full_size(sbte, full, problem, converged, accel):
+    from staticbtesolver_gb300 import learned
+    mlp = learned.load() if accel == "learned" else None
+    res = _solve(sbte, problem, mlp=mlp, form=sbte.FORM_SWEEP, accel=1 if accel == "learned" else 2,
+                 accel_every=learned.EVERY)
+    err = rel_l2(res.T - 300.0, converged - 300.0)
+    err_oracle = rel_l2(full["T"] - 300.0, converged - 300.0)
+    print(accel, "n_iter", res.report["n_iter"], "jumps", res.report["accel_steps"], "rel_l2 to converged", err,
+          "(oracle at margin 1e-5:", err_oracle, ")")
+    assert res.report["accel_steps"] > 0
+    assert res.report["n_iter"] < 0.75 * int(full["n_iter"])  # the gain over the plain iteration
+    assert err < 1e-5
+    _q_close(res.q, full["q"], 1e-4)

@@ -113,8 +113,11 @@ struct bte_ctx {
     // upwind sweep plan (form BTE_FORM_SWEEP)
     bool plan_ready = false;
     int plan_lagged_dirs = 0;
+    bool sweep_margin = false;  // acyclic plan: the sweep sums the margin partials (d_spart)
     long long plan_levels = 0;
-    DevBuf p_cell, p_dg, p_vo, p_nb, p_fc, p_lvl, p_lvl_off, p_part, p_bad, p_invd;
+    DevBuf p_cell, p_dg, p_vo, p_nb, p_fc, p_lvl, p_lvl_off, p_part, p_bad, p_invd, d_spart, p_bidx;
+    DevBuf d_bcell, d_bidx, d_bsum;  // cells with boundary faces, cell -> row, boundary rhs per (system, row)
+    int nbcell = 0;
     // sweep launch shape (bands per block, threads per block) picked by timing
     // the candidates on the first sweep of a plan
     int sweep_group = 4, sweep_threads = 256;
@@ -497,6 +500,15 @@ static bte_status setup(bte_ctx* ctx, int batch_systems) {
     BTE_CUDA(upload(ctx->d_Lr, ctx->Lr, st));
     BTE_CUDA(upload(ctx->d_vg, ctx->vg, st));
     BTE_CUDA(upload(ctx->d_bptr, bptr, st));
+    {
+        std::vector<int> bcell, bidx(n, -1);
+        for (int c = 0; c < n; ++c)
+            if (bptr[c + 1] > bptr[c]) { bidx[c] = (int)bcell.size(); bcell.push_back(c); }
+        ctx->nbcell = (int)bcell.size();
+        if (bcell.empty()) bcell.push_back(0);
+        BTE_CUDA(upload(ctx->d_bcell, bcell, st));
+        BTE_CUDA(upload(ctx->d_bidx, bidx, st));
+    }
     BTE_CUDA(upload(ctx->d_bf_cell, bf_cell, st));
     BTE_CUDA(upload(ctx->d_bf_kind, bf_kind, st));
     BTE_CUDA(upload(ctx->d_bf_bc, bf_bc, st));
@@ -701,14 +713,16 @@ static bte_status build_sweep_plan(bte_ctx* ctx) {
     BTE_CUDA(ctx->p_vo.alloc(sizeof(double) * ND * n));
     BTE_CUDA(ctx->p_nb.alloc(sizeof(int) * ND * F * n));
     BTE_CUDA(ctx->p_fc.alloc(sizeof(double) * ND * F * n));
+    BTE_CUDA(ctx->p_bidx.alloc(sizeof(int) * ND * n));
+    BTE_CUDA(ctx->d_bsum.alloc(sizeof(double) * (size_t)ctx->nbb * ND * std::max(ctx->nbcell, 1)));
     bte::k_sweep_layout<<<dim3((n + 255) / 256, ND), 256, 0, st>>>(
         d_perm.as<int>(), d_pos.as<int>(), d_lag.as<int>(), ctx->d_dg.as<double>(), ctx->d_vo.as<double>(), ctx->d_fc.as<double>(),
-        ctx->d_nbr.as<int>(), F, n, Np, ND, ctx->p_cell.as<int>(), ctx->p_dg.as<double>(), ctx->p_vo.as<double>(),
-        ctx->p_nb.as<int>(), ctx->p_fc.as<double>());
+        ctx->d_nbr.as<int>(), ctx->d_bidx.as<int>(), F, n, Np, ND, ctx->p_cell.as<int>(), ctx->p_bidx.as<int>(),
+        ctx->p_dg.as<double>(), ctx->p_vo.as<double>(), ctx->p_nb.as<int>(), ctx->p_fc.as<double>());
     BTE_LAUNCHED();
     BTE_CUDA(ctx->p_invd.alloc(sizeof(double) * ctx->n_band * ND * n));
     {
-        bte::SweepPlan sp{ctx->p_cell.as<int>(), ctx->p_dg.as<double>(), ctx->p_vo.as<double>(), ctx->p_nb.as<int>(),
+        bte::SweepPlan sp{ctx->p_cell.as<int>(), ctx->p_bidx.as<int>(), ctx->p_dg.as<double>(), ctx->p_vo.as<double>(), ctx->p_nb.as<int>(),
                           ctx->p_fc.as<double>(), ctx->p_lvl.as<int>(), ctx->p_lvl_off.as<int>(), n, F};
         bte::k_sweep_invd<<<dim3((n + 255) / 256, ND), 256, 0, st>>>(sp, ctx->d_kb.as<double>(), ctx->n_band, ND,
                                                                      ctx->p_invd.as<double>());
@@ -717,6 +731,8 @@ static bte_status build_sweep_plan(bte_ctx* ctx) {
     BTE_CUDA(cudaStreamSynchronize(st));  // d_perm / d_lag go out of scope
     ctx->sweep_tuned = false;
     ctx->plan_lagged_dirs = lagged_dirs;
+    ctx->sweep_margin = lagged_dirs == 0;
+    BTE_CUDA(ctx->d_spart.alloc(sizeof(double) * ND * ctx->n_band));
     ctx->plan_levels = levels;
     ctx->plan_ready = true;
     return BTE_OK;
@@ -750,8 +766,9 @@ static bte_status solve_batch_plain(bte_ctx* ctx, int b0, int nbb, const bte_opt
                      ctx->nbf, std::max(ctx->n_bc, 1)};
     dim3 grid(ctx->nchunk, S);
     BTE_LAUNCH(KK_RHS, -1, S * N * 2 * w + geo / 2, 0,
-               bte::k_rhs<<<grid, bte::THREADS, 0, st>>>(op, bd, ctx->d_ebar.as<double>(), ctx->e_prev,
-                                                         ctx->w_b.as<double>(), ctx->n));
+               bte::k_rhs<<<grid, bte::THREADS, 0, st>>>(
+                   op, bte::RhsSrc{bd, ctx->d_ebar.as<double>(), ctx->e_prev, ctx->n_dir, ctx->Np},
+                   ctx->w_b.as<double>(), ctx->n));
 
     const int maxit = o.inner_maxit;
     if (ctx->active_cap < maxit + 2) {
@@ -825,8 +842,9 @@ static bte_status solve_batch_mixed(bte_ctx* ctx, int b0, int nbb, const bte_opt
     const double geo32 = N * ((ctx->F + 2) * 4.0 + ctx->F * 4.0) * std::min(S, ctx->n_dir);
     dim3 grid(ctx->nchunk, S);
     BTE_LAUNCH(KK_RHS, -1, S * N * 16.0 + geo / 2, 0,
-               bte::k_rhs<<<grid, bte::THREADS, 0, st>>>(op, bd, ctx->d_ebar.as<double>(), ctx->e_prev,
-                                                         ctx->w_b.as<double>(), ctx->n));
+               bte::k_rhs<<<grid, bte::THREADS, 0, st>>>(
+                   op, bte::RhsSrc{bd, ctx->d_ebar.as<double>(), ctx->e_prev, ctx->n_dir, ctx->Np},
+                   ctx->w_b.as<double>(), ctx->n));
     BTE_LAUNCH(KK_INIT, -1, S * N * 16.0, 0, bte::k_mixed_start<<<grid, bte::THREADS, 0, st>>>(op, ctx->e_prev));
     const int maxit = o.inner_maxit;
     if (ctx->active_cap < maxit + 2) {
@@ -926,15 +944,21 @@ static bte_status solve_batch_sweep(bte_ctx* ctx, int b0, int nbb, const bte_opt
                      ctx->nbf, std::max(ctx->n_bc, 1)};
     const double geo = N * ((ctx->F + 2) * w + ctx->F * 4.0) * ctx->n_dir;
     dim3 grid(ctx->nchunk, S);
-    BTE_LAUNCH(KK_RHS, -1, S * N * 2 * w + geo / 2, 0,
-               bte::k_rhs_sweep<<<grid, bte::THREADS, 0, st>>>(op, bd, ctx->p_cell.as<int>(), ctx->d_ebar.as<double>(),
-                                                               ctx->e_prev, ctx->w_b.as<double>(), ctx->n));
-    bte::SweepPlan sp{ctx->p_cell.as<int>(), ctx->p_dg.as<double>(), ctx->p_vo.as<double>(), ctx->p_nb.as<int>(),
+    const bte::RhsSrc src{bd, ctx->d_ebar.as<double>(), ctx->e_prev, ctx->n_dir, ctx->Np};
+    if (ctx->nbcell > 0) {
+        BTE_LAUNCH(KK_RHS, -1, (double)S * ctx->nbcell * 2 * w, 0,
+                   bte::k_bound_rhs<<<dim3((ctx->nbcell + 127) / 128, S), 128, 0, st>>>(
+                       src, ctx->d_bcell.as<int>(), ctx->nbcell, ctx->d_kb.as<double>(), nbb, b0,
+                       ctx->d_bsum.as<double>()));
+    }
+    const bte::SweepSrc ssrc{ctx->d_ebar.as<double>(), ctx->d_bsum.as<double>(), ctx->e_prev, ctx->nbcell};
+    bte::SweepPlan sp{ctx->p_cell.as<int>(), ctx->p_bidx.as<int>(), ctx->p_dg.as<double>(), ctx->p_vo.as<double>(), ctx->p_nb.as<int>(),
                       ctx->p_fc.as<double>(), ctx->p_lvl.as<int>(), ctx->p_lvl_off.as<int>(), ctx->n, ctx->F};
     // launch-shape autotuning on the first sweep of this plan (each candidate
     // computes the same x from the same inputs)
     if (!ctx->sweep_tuned) {
-        static const int cand[][2] = {{1, 64}, {1, 128}, {2, 64}, {2, 128}, {2, 256}, {4, 128}, {4, 256}, {8, 256}};
+        // (bands per block, threads); k_sweep takes at most 128 threads
+        static const int cand[][2] = {{1, 64}, {1, 128}, {2, 64}, {2, 128}, {4, 64}, {4, 128}, {8, 128}, {16, 128}};
         const int ncand = (int)(sizeof(cand) / sizeof(cand[0]));
         cudaEvent_t e0, e1;
         BTE_CUDA(cudaEventCreate(&e0));
@@ -943,9 +967,9 @@ static bte_status solve_batch_sweep(bte_ctx* ctx, int b0, int nbb, const bte_opt
         for (int k = 0; k < ncand; ++k) {
             const int Gk = std::max(1, std::min(cand[k][0], nbb));
             BTE_CUDA(cudaEventRecord(e0, st));
-            bte::k_sweep<<<dim3((nbb + Gk - 1) / Gk, ctx->n_dir), cand[k][1], sweep_smem(Gk), st>>>(
-                sp, ctx->d_kb.as<double>(), ctx->p_invd.as<double>(), ctx->w_b.as<double>(), ctx->e_curr,
-                ctx->e_prev, 1, Gk, sweep_ring(Gk), nbb, b0, ctx->n_dir, ctx->Np);
+            bte::k_sweep<false><<<dim3((nbb + Gk - 1) / Gk, ctx->n_dir), cand[k][1], sweep_smem(Gk), st>>>(
+                sp, ctx->d_kb.as<double>(), ctx->p_invd.as<double>(), ssrc, ctx->e_curr, 1, Gk, sweep_ring(Gk), nbb,
+                b0, ctx->n_band, ctx->n_dir, ctx->Np, nullptr);
             BTE_LAUNCHED();
             BTE_CUDA(cudaEventRecord(e1, st));
             BTE_CUDA(cudaEventSynchronize(e1));
@@ -960,22 +984,31 @@ static bte_status solve_batch_sweep(bte_ctx* ctx, int b0, int nbb, const bte_opt
     }
     const int G = std::max(1, std::min(ctx->sweep_group, nbb));
     dim3 sgrid((nbb + G - 1) / G, ctx->n_dir);
-    // algorithmic bytes of a sweep: rhs gather, 1/D and x per system, level-ordered
-    // geometry per direction, one upstream gather per inflow face
-    const double sweep_bytes = S * N * (3 * w + 1.5 * w) + geo;
+    // algorithmic HBM bytes of a sweep per system and cell: 1/D read, x written
+    // (and, with the fused margin, the previous iterate read), plus the
+    // level-ordered geometry per direction; ebar and the boundary values come from L2
+    const bool margin = ctx->sweep_margin;
+    const double sweep_bytes = S * N * (margin ? 3 : 2) * w + geo;
     int sweeps = 0;
     for (;;) {
-        BTE_LAUNCH(KK_SWEEP, -1, sweep_bytes, 0,
-                   bte::k_sweep<<<sgrid, ctx->sweep_threads, sweep_smem(G), st>>>(
-                       sp, ctx->d_kb.as<double>(), ctx->p_invd.as<double>(), ctx->w_b.as<double>(), ctx->e_curr,
-                       ctx->e_prev, sweeps == 0, G, sweep_ring(G), nbb, b0, ctx->n_dir, ctx->Np));
+        if (margin) {
+            BTE_LAUNCH(KK_SWEEP, -1, sweep_bytes, 0,
+                       bte::k_sweep<true><<<sgrid, ctx->sweep_threads, sweep_smem(G), st>>>(
+                           sp, ctx->d_kb.as<double>(), ctx->p_invd.as<double>(), ssrc, ctx->e_curr, 1, G,
+                           sweep_ring(G), nbb, b0, ctx->n_band, ctx->n_dir, ctx->Np, ctx->d_spart.as<double>()));
+        } else {
+            BTE_LAUNCH(KK_SWEEP, -1, sweep_bytes, 0,
+                       bte::k_sweep<false><<<sgrid, ctx->sweep_threads, sweep_smem(G), st>>>(
+                           sp, ctx->d_kb.as<double>(), ctx->p_invd.as<double>(), ssrc, ctx->e_curr, sweeps == 0, G,
+                           sweep_ring(G), nbb, b0, ctx->n_band, ctx->n_dir, ctx->Np, nullptr));
+        }
         ++sweeps;
         if (ctx->plan_lagged_dirs == 0) break;
         BTE_CUDA(ctx->p_part.alloc(sizeof(double) * 2 * (size_t)S * ctx->nchunk));
         BTE_CUDA(ctx->p_bad.alloc(sizeof(int)));
         BTE_CUDA(cudaMemsetAsync(ctx->p_bad.p, 0, sizeof(int), st));
         BTE_LAUNCH(KK_SWEEP_RES, -1, S * N * 2 * w + geo, 0,
-                   bte::k_sweep_residual<<<grid, bte::THREADS, 0, st>>>(op, ctx->p_cell.as<int>(), ctx->w_b.as<double>(),
+                   bte::k_sweep_residual<<<grid, bte::THREADS, 0, st>>>(op, src, ctx->p_cell.as<int>(),
                                                                         ctx->p_part.as<double>(), ctx->nchunk, ctx->n));
         bte::k_sweep_check<<<(S + 127) / 128, 128, 0, st>>>(ctx->p_part.as<double>(), S, ctx->nchunk, o.inner_tol,
                                                              ctx->p_bad.as<int>());
@@ -1047,6 +1080,8 @@ extern "C" bte_status bte_solve(bte_ctx* ctx, const bte_options* opts, bte_repor
     struct EvGuard { cudaEvent_t* e; ~EvGuard() { for (int k = 0; k < 5; ++k) cudaEventDestroy(e[k]); } } guard{ev};
     bte_status result = BTE_ERR_NOT_CONVERGED;
     const int nred = (int)(Np / bte::THREADS);
+    // the sweep of an acyclic plan sums the margin itself; k_reduce then reads e_curr only
+    const bool fused_margin = o.form == BTE_FORM_SWEEP && ctx->sweep_margin;
     // accelerator set-up
     bool accel_on = o.accel != 0;
     int accel_last = -1;
@@ -1088,6 +1123,7 @@ extern "C" bte_status bte_solve(bte_ctx* ctx, const bte_options* opts, bte_repor
                            ctx->e_prev, ctx->d_dlist.as<int>(), ctx->d_bf_cell.as<int>(), ctx->d_wdiff.as<double>(),
                            ctx->d_wden.as<double>(), ctx->ndiff, NB, ND, Np, ctx->nbf, ctx->d_ediff.as<double>()));
         }
+        if (fused_margin) BTE_CUDA(cudaMemsetAsync(ctx->d_spart.p, 0, sizeof(double) * ND * NB, st));
         BTE_CUDA(cudaEventRecord(ev[1], st));
         for (int b0 = 0; b0 < NB; b0 += ctx->nbb) {
             const int nbb = std::min(ctx->nbb, NB - b0);
@@ -1097,16 +1133,25 @@ extern "C" bte_status bte_solve(bte_ctx* ctx, const bte_options* opts, bte_repor
             if (s != BTE_OK) return s;
         }
         BTE_CUDA(cudaEventRecord(ev[2], st));
-        BTE_LAUNCH(KK_REDUCE, -1, (2.0 * NB * ND + NB) * ctx->n * 8.0, 0,
-                   bte::k_reduce<<<dim3(nred, NB), bte::THREADS, 0, st>>>(
-                       ctx->e_curr, ctx->e_prev, ctx->d_omega.as<double>(), ctx->d_Cb.as<double>(), ctx->T_ref,
-                       ctx->n, ND, Np, ctx->d_Tb.as<double>(), ctx->d_mpart.as<double>()));
+        if (fused_margin) {
+            BTE_LAUNCH(KK_REDUCE, -1, (1.0 * NB * ND + NB) * ctx->n * 8.0, 0,
+                       bte::k_reduce<false><<<dim3(nred, NB), bte::THREADS, 0, st>>>(
+                           ctx->e_curr, ctx->e_prev, ctx->d_omega.as<double>(), ctx->d_Cb.as<double>(), ctx->T_ref,
+                           ctx->n, ND, Np, ctx->d_Tb.as<double>(), nullptr));
+        } else {
+            BTE_LAUNCH(KK_REDUCE, -1, (2.0 * NB * ND + NB) * ctx->n * 8.0, 0,
+                       bte::k_reduce<true><<<dim3(nred, NB), bte::THREADS, 0, st>>>(
+                           ctx->e_curr, ctx->e_prev, ctx->d_omega.as<double>(), ctx->d_Cb.as<double>(), ctx->T_ref,
+                           ctx->n, ND, Np, ctx->d_Tb.as<double>(), ctx->d_mpart.as<double>()));
+        }
         BTE_LAUNCH(KK_REDUCE, -1, (2.0 * NB + 1) * ctx->n * 8.0, 0,
                    bte::k_recover<<<(ctx->n + 255) / 256, 256, 0, st>>>(
                        ctx->d_Tb.as<double>(), ctx->d_Cb.as<double>(), ctx->d_Lr.as<double>(), Lr_sum, ctx->T_ref,
                        ctx->solid_angle, ctx->n, NB, Np, ctx->d_T.as<double>(), ctx->d_ebar.as<double>()));
-        bte::k_margin_final<<<1, bte::THREADS, 0, st>>>(ctx->d_mpart.as<double>(), nred * NB, (double)NB * ctx->n,
-                                             ctx->d_margin.as<double>());
+        // margin = sum of the partials / (n_band n_cell), fixed order
+        bte::k_margin_final<<<1, bte::THREADS, 0, st>>>(fused_margin ? ctx->d_spart.as<double>() : ctx->d_mpart.as<double>(),
+                                                        fused_margin ? ND * NB : nred * NB, (double)NB * ctx->n,
+                                                        ctx->d_margin.as<double>());
         BTE_LAUNCHED();
         BTE_CUDA(cudaEventRecord(ev[3], st));
         BTE_CUDA(cudaMemcpyAsync(ctx->h_pinned, ctx->d_margin.p, sizeof(double), cudaMemcpyDeviceToHost, st));

@@ -60,57 +60,22 @@ struct Boundary {
     int nbf, n_bc;
 };
 
-// Right-hand sides of one batch (_get_Re, src/StaticBTESolver.cpp:162-269):
+// Right-hand side of system (band b, direction d) at cell c (_get_Re,
+// src/StaticBTESolver.cpp:162-269):
 //   R[c] = - sum_{inflow boundary faces} e_wall k_b A g + ebar[b][c] V_c Omega_d
 // e_wall: isothermal C_b/Omega_tot (T_bc - T_ref); diffuse: the outgoing
 // energy of the previous iterate averaged over the wall; specular: the previous
-// iterate at the mirrored direction.
-__global__ void __launch_bounds__(THREADS) k_rhs(FaceFluxOp op, Boundary bd, const double* __restrict__ ebar,
-                                                 const double* __restrict__ e_prev, double* rhs, int n) {
-    const int y = blockIdx.y;
-    int b, d;
-    op.bd(y, b, d);
-    const double k = op.kb[b];
-    const size_t o = (size_t)y * op.Np;
-    const double* ep_bd_base = e_prev + (size_t)b * op.n_dir * op.Np;
-    BTE_CELL_LOOP(c) {
-        double r = 0.0;
-        if (c < n) {
-            const int e0 = bd.bptr[c], e1 = bd.bptr[c + 1];
-            for (int e = e0; e < e1; ++e) {
-                const double cf = bd.cin[(size_t)d * bd.nbf + e];
-                if (cf == 0.0) continue;
-                double ew;
-                switch (bd.bf_kind[e]) {
-                    case 1: ew = bd.eiso[(size_t)b * bd.n_bc + bd.bf_bc[e]]; break;
-                    case 2: ew = bd.ediff[(size_t)b * bd.nbf + e]; break;
-                    case 31: ew = ep_bd_base[(size_t)bd.mirror[d] * op.Np + c]; break;
-                    case 32: ew = ep_bd_base[(size_t)bd.mirror[op.n_dir + d] * op.Np + c]; break;
-                    default: ew = ep_bd_base[(size_t)bd.mirror[2 * op.n_dir + d] * op.Np + c]; break;
-                }
-                r -= ew * (k * cf);
-            }
-            r += ebar[(size_t)b * op.Np + c] * op.vo[(size_t)d * op.Np + c];
-        }
-        rhs[o + c] = r;
-    }
-}
-
-// The same right-hand sides written in each direction's sweep order
-// (rhs[y][j] for cell perm[d][j]), so the sweep reads them coalesced and
-// without a dependent gather.
-__global__ void __launch_bounds__(THREADS) k_rhs_sweep(FaceFluxOp op, Boundary bd, const int* __restrict__ perm,
-                                                       const double* __restrict__ ebar, const double* __restrict__ e_prev,
-                                                       double* rhs, int n) {
-    const int y = blockIdx.y;
-    int b, d;
-    op.bd(y, b, d);
-    const double k = op.kb[b];
-    const size_t o = (size_t)y * op.Np;
-    const double* ep_bd_base = e_prev + (size_t)b * op.n_dir * op.Np;
-    BTE_CELL_LOOP(j) {
-        if (j >= n) continue;
-        const int c = perm[(size_t)d * n + j];
+// iterate at the mirrored direction.  Computed where it is consumed, so no
+// right-hand-side array is written or read.
+struct RhsSrc {
+    Boundary bd;
+    const double* ebar;    // [n_band][Np]
+    const double* e_prev;  // [n_band][n_dir][Np]
+    int n_dir;
+    size_t Np;
+    // the boundary part: - sum over the cell's inflow boundary faces of e_wall k A g (k = k_b)
+    __device__ __forceinline__ double boundary(int b, int d, int c, double k) const {
+        const double* ep_b = e_prev + (size_t)b * n_dir * Np;
         double r = 0.0;
         const int e0 = bd.bptr[c], e1 = bd.bptr[c + 1];
         for (int e = e0; e < e1; ++e) {
@@ -120,15 +85,40 @@ __global__ void __launch_bounds__(THREADS) k_rhs_sweep(FaceFluxOp op, Boundary b
             switch (bd.bf_kind[e]) {
                 case 1: ew = bd.eiso[(size_t)b * bd.n_bc + bd.bf_bc[e]]; break;
                 case 2: ew = bd.ediff[(size_t)b * bd.nbf + e]; break;
-                case 31: ew = ep_bd_base[(size_t)bd.mirror[d] * op.Np + c]; break;
-                case 32: ew = ep_bd_base[(size_t)bd.mirror[op.n_dir + d] * op.Np + c]; break;
-                default: ew = ep_bd_base[(size_t)bd.mirror[2 * op.n_dir + d] * op.Np + c]; break;
+                case 31: ew = ep_b[(size_t)bd.mirror[d] * Np + c]; break;
+                case 32: ew = ep_b[(size_t)bd.mirror[n_dir + d] * Np + c]; break;
+                default: ew = ep_b[(size_t)bd.mirror[2 * n_dir + d] * Np + c]; break;
             }
             r -= ew * (k * cf);
         }
-        r += ebar[(size_t)b * op.Np + c] * op.vo[(size_t)d * op.Np + c];
-        rhs[o + j] = r;
+        return r;
     }
+    // vo = V_c Omega_d
+    __device__ __forceinline__ double at(int b, int d, int c, double k, double vo) const {
+        return boundary(b, d, c, k) + ebar[(size_t)b * Np + c] * vo;
+    }
+};
+
+// Boundary part of the right-hand side per (system of the batch, boundary
+// cell), for the sweep: bsum[y][i] = RhsSrc::boundary for cell bcell[i], with
+// y -> direction y / nbb, band b0 + y % nbb as in FaceFluxOp.
+__global__ void k_bound_rhs(RhsSrc src, const int* __restrict__ bcell, int nbcell, const double* __restrict__ kb,
+                            int nbb, int b0, double* bsum) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y;
+    if (i >= nbcell) return;
+    const int d = y / nbb, b = b0 + y % nbb;
+    bsum[(size_t)y * nbcell + i] = src.boundary(b, d, bcell[i], kb[b]);
+}
+
+// Right-hand sides of one batch for the Krylov forms: rhs[y][c].
+__global__ void __launch_bounds__(THREADS) k_rhs(FaceFluxOp op, RhsSrc src, double* rhs, int n) {
+    const int y = blockIdx.y;
+    int b, d;
+    op.bd(y, b, d);
+    const double k = op.kb[b];
+    const size_t o = (size_t)y * op.Np;
+    BTE_CELL_LOOP(c) { rhs[o + c] = c < n ? src.at(b, d, c, k, op.vo[(size_t)d * op.Np + c]) : 0.0; }
 }
 
 // Diffuse wall energy per (band, diffuse face) from the previous iterate
@@ -152,10 +142,12 @@ __global__ void k_diffuse_wall(const double* __restrict__ e_prev, const int* __r
 }
 
 // The reductions that close an outer iteration (src/StaticBTESolver.cpp:96-104
-// and :311-321), one pass over e_curr and e_prev with one block per
-// (256 cells, band):
+// and :311-321), one pass over e_curr (and e_prev for MARGIN) with one block
+// per (256 cells, band):
 //   Tb[b][c] = sum_d e Omega_d / C_b + T_ref
 //   margin partial[b][block] = sum_d (e_curr - e_prev)^2 over the block's cells
+// (without MARGIN the sweep has already summed the margin partials).
+template <bool MARGIN>
 __global__ void __launch_bounds__(THREADS) k_reduce(const double* __restrict__ e_curr, const double* __restrict__ e_prev,
                                                     const double* __restrict__ omega, const double* __restrict__ Cb,
                                                     double T_ref, int n, int n_dir, size_t Np, double* Tb,
@@ -170,15 +162,19 @@ __global__ void __launch_bounds__(THREADS) k_reduce(const double* __restrict__ e
         double e0 = 0.0;
 #pragma unroll 8
         for (int d = 0; d < n_dir; ++d) {
-            const double a = __ldcs(ec + (size_t)d * Np), p = __ldcs(ep + (size_t)d * Np);
+            const double a = __ldcs(ec + (size_t)d * Np);
             e0 += a * omega[d];
-            const double df = a - p;
-            m[0] = fma(df, df, m[0]);
+            if (MARGIN) {
+                const double df = a - __ldcs(ep + (size_t)d * Np);
+                m[0] = fma(df, df, m[0]);
+            }
         }
         Tb[(size_t)b * Np + c] = e0 / Cb[b] + T_ref;
     }
-    block_sum<1>(m, sm);
-    if (threadIdx.x == 0) part[(size_t)b * gridDim.x + blockIdx.x] = m[0];
+    if (MARGIN) {
+        block_sum<1>(m, sm);
+        if (threadIdx.x == 0) part[(size_t)b * gridDim.x + blockIdx.x] = m[0];
+    }
 }
 
 // src/StaticBTESolver.cpp:106-120: T[c] = sum_b Lr_b Tb[b][c] / sum_b Lr_b and
@@ -268,6 +264,7 @@ namespace bte {
 //   start positions (the last entry is n).
 struct SweepPlan {
     const int* cell;
+    const int* bidx;  // [n_dir][n] row of the cell in the boundary-cell list, -1 interior
     const double* dg;
     const double* vo;
     const int* nb;
@@ -290,18 +287,17 @@ __global__ void k_sweep_invd(SweepPlan sp, const double* __restrict__ kb, int n_
 
 // Operands of one sweep item that do not depend on the level being solved.
 struct SweepItem {
-    int c, b;
+    int c, b, bi;
     int u[4];
     double cf[4];
-    double invd, r;
+    double invd, vo, eb, bs, old;
 };
 
-// rhs is in sweep order: rhs[(d * nbb + bl) * Np + j].
-__device__ __forceinline__ void sweep_load(const SweepPlan& sp, const double* __restrict__ invD,
-                                           const double* __restrict__ rhs, int d, int j, int bl, int b0, int nbb,
-                                           int n_dir, size_t Np, SweepItem& it) {
+// Stage A: everything addressed by the position j alone.
+__device__ __forceinline__ void sweep_load_a(const SweepPlan& sp, const double* __restrict__ invD, int d, int j,
+                                             int b, int n_dir, SweepItem& it) {
     const size_t pj = (size_t)d * sp.n + j;
-    it.b = b0 + bl;
+    it.b = b;
     it.c = sp.cell[pj];
 #pragma unroll
     for (int f = 0; f < 4; ++f) {
@@ -314,8 +310,41 @@ __device__ __forceinline__ void sweep_load(const SweepPlan& sp, const double* __
             it.cf[f] = 0.0;
         }
     }
-    it.invd = invD[((size_t)it.b * n_dir + d) * sp.n + j];
-    it.r = rhs[((size_t)d * nbb + bl) * Np + j];
+    it.invd = invD[((size_t)b * n_dir + d) * sp.n + j];
+    it.vo = sp.vo[pj];
+    it.bi = sp.bidx[pj];
+}
+
+// Stage B: what is addressed by the cell (ebar, the boundary part of the
+// right-hand side, and with MARGIN the previous iterate), issued a level after
+// stage A so the cell index has arrived and the loads do not stall the sweep.
+struct SweepSrc {
+    const double* ebar;   // [n_band][Np]
+    const double* bsum;   // [nbb * n_dir][nbcell] (k_bound_rhs)
+    const double* x_old;  // e_prev
+    int nbcell;
+};
+
+template <bool MARGIN>
+__device__ __forceinline__ void sweep_load_b(const SweepSrc& src, int d, int n_dir, int nbb, int b0, size_t Np,
+                                             SweepItem& it) {
+    it.eb = src.ebar[(size_t)it.b * Np + it.c];
+    it.bs = it.bi >= 0 ? src.bsum[((size_t)d * nbb + (it.b - b0)) * src.nbcell + it.bi] : 0.0;
+    if (MARGIN) it.old = src.x_old[((size_t)it.b * n_dir + d) * Np + it.c];
+}
+
+// Fixed-order sum over a block of any whole-warp size (<= 1024 threads); the
+// result is valid in thread 0.
+__device__ __forceinline__ double block_sum_any(double v, double* smem /* [32] */) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if (lane == 0) smem[warp] = v;
+    __syncthreads();
+    double s = 0.0;
+    if (threadIdx.x == 0)
+        for (int w = 0; w < nw; ++w) s += smem[w];
+    return s;
 }
 
 // One block sweeps direction blockIdx.y for bands b0 + blockIdx.x * G .. + G - 1.
@@ -327,11 +356,18 @@ __device__ __forceinline__ void sweep_load(const SweepPlan& sp, const double* __
 // [j0, j1) whenever p >= j1 - W: no position written in this level maps to
 // its slot.  W is a power of two.  Older and lagged upstream values are read
 // from global memory.
-__global__ void __launch_bounds__(512) k_sweep(SweepPlan sp, const double* __restrict__ kb,
-                                               const double* __restrict__ invD, const double* __restrict__ rhs,
-                                               double* x, const double* __restrict__ x_old, int first_sweep,
-                                               int G, int W, int nbb, int b0, int n_dir, size_t Np) {
+// At most 128 threads, 5 blocks per SM (<= 96 registers, no spills): 640
+// blocks of the 40-band, 32-direction workload fit in one wave.
+// MARGIN (acyclic plans: one sweep is the exact solve): the block also sums
+// (x - x_old)^2 over its items, in a fixed order, into
+// mpart[d * n_band + b0 + blockIdx.x * G], the outer iteration's margin partial.
+template <bool MARGIN>
+__global__ void __launch_bounds__(128, 5) k_sweep(SweepPlan sp, const double* __restrict__ kb,
+                                                  const double* __restrict__ invD, SweepSrc src, double* x,
+                                                  int first_sweep, int G, int W, int nbb, int b0, int n_band,
+                                                  int n_dir, size_t Np, double* __restrict__ mpart) {
     extern __shared__ double ring[];  // [G][W]
+    __shared__ double red[32];
     const int d = blockIdx.y;
     const int g0 = blockIdx.x * G;
     const int gn = min(G, nbb - g0);
@@ -340,14 +376,16 @@ __global__ void __launch_bounds__(512) k_sweep(SweepPlan sp, const double* __res
     const int* cell_d = sp.cell + (size_t)d * sp.n;
     SweepItem p1, p2;  // this thread's first item of levels l and l+1
     bool h1 = false, h2 = false;
+    double msum = 0.0;
     auto pre = [&](int l, SweepItem& dst) -> bool {
         if (l >= L1) return false;
         const int j0 = sp.lvl[l];
         if (threadIdx.x >= (sp.lvl[l + 1] - j0) * gn) return false;
-        sweep_load(sp, invD, rhs, d, j0 + threadIdx.x / gn, g0 + threadIdx.x % gn, b0, nbb, n_dir, Np, dst);
+        sweep_load_a(sp, invD, d, j0 + threadIdx.x / gn, b0 + g0 + threadIdx.x % gn, n_dir, dst);
         return true;
     };
     h1 = pre(L0, p1);
+    if (h1) sweep_load_b<MARGIN>(src, d, n_dir, nbb, b0, Np, p1);
     h2 = pre(L0 + 1, p2);
     for (int l = L0; l < L1; ++l) {
         const int j0 = sp.lvl[l], j1 = sp.lvl[l + 1];
@@ -358,7 +396,11 @@ __global__ void __launch_bounds__(512) k_sweep(SweepPlan sp, const double* __res
             const int j = j0 + it / gn;
             const int bl = it % gn;
             if (it == threadIdx.x && h1) cur = p1;
-            else sweep_load(sp, invD, rhs, d, j, g0 + bl, b0, nbb, n_dir, Np, cur);
+            else {
+                sweep_load_a(sp, invD, d, j, b0 + g0 + bl, n_dir, cur);
+                sweep_load_b<MARGIN>(src, d, n_dir, nbb, b0, Np, cur);
+            }
+            const double k = kb[cur.b];
             double* xb = x + ((size_t)cur.b * n_dir + d) * Np;
             double* rg = ring + (size_t)bl * W;
             double off = 0.0;
@@ -370,39 +412,48 @@ __global__ void __launch_bounds__(512) k_sweep(SweepPlan sp, const double* __res
                 if (u >= 0) xu = u >= keep ? rg[u & (W - 1)] : xb[cell_d[u]];
                 else {  // lagged (u = -2 - position): previous sweep's value (or the previous outer iterate)
                     const int cu = cell_d[-u - 2];
-                    xu = first_sweep ? x_old[((size_t)cur.b * n_dir + d) * Np + cu] : xb[cu];
+                    xu = first_sweep ? src.x_old[((size_t)cur.b * n_dir + d) * Np + cu] : xb[cu];
                 }
                 off = fma(cur.cf[f], xu, off);
             }
-            const double v = fma(-kb[cur.b], off, cur.r) * cur.invd;
+            const double v = fma(-k, off, cur.bs + cur.eb * cur.vo) * cur.invd;
             xb[cur.c] = v;
             rg[j & (W - 1)] = v;
+            if (MARGIN) {
+                const double df = v - cur.old;
+                msum = fma(df, df, msum);
+            }
         }
         p1 = p2;
         h1 = h2;
+        if (h1) sweep_load_b<MARGIN>(src, d, n_dir, nbb, b0, Np, p1);
         h2 = pre(l + 2, p2);
         __syncthreads();
     }
+    if (MARGIN) {
+        const double s = block_sum_any(msum, red);
+        if (threadIdx.x == 0) mpart[(size_t)d * n_band + b0 + g0] = s;
+    }
 }
 
-// Residual test of the sweep solution (rhs in sweep order, as k_rhs_sweep
-// writes it): partials of ||R - A x||^2 and ||R||^2 per (row, chunk).
-__global__ void __launch_bounds__(THREADS) k_sweep_residual(FaceFluxOp op, const int* __restrict__ perm,
-                                                            const double* __restrict__ rhs, double* part, int nchunk,
-                                                            int n) {
+// Residual test of the sweep solution: partials of ||R - A x||^2 and ||R||^2
+// per (row, chunk), positions j in sweep order.
+__global__ void __launch_bounds__(THREADS) k_sweep_residual(FaceFluxOp op, RhsSrc src, const int* __restrict__ perm,
+                                                            double* part, int nchunk, int n) {
     __shared__ double sm[2][NWARP];
     const int y = blockIdx.y;
     int b, d;
     op.bd(y, b, d);
-    const size_t o = (size_t)y * op.Np;
+    const double k = op.kb[b];
     const double* xs = op.x_of(y);
     double acc[2] = {0, 0};
     BTE_CELL_LOOP(j) {
         if (j < n) {
             const int c = perm[(size_t)d * n + j];
-            const double r = rhs[o + j] - op.template apply<double>(y, c, xs);
+            const double R = src.at(b, d, c, k, op.vo[(size_t)d * op.Np + c]);
+            const double r = R - op.template apply<double>(y, c, xs);
             acc[0] = fma(r, r, acc[0]);
-            acc[1] = fma(rhs[o + j], rhs[o + j], acc[1]);
+            acc[1] = fma(R, R, acc[1]);
         }
     }
     block_sum<2>(acc, sm);
@@ -442,14 +493,16 @@ __global__ void k_sweep_layout(const int* __restrict__ perm, const int* __restri
                                const int* __restrict__ lagged,  // [n_dir][F][n] 0/1
                                const double* __restrict__ dg, const double* __restrict__ vo,
                                const double* __restrict__ fc, const int* __restrict__ nbr,  // nbr [n][F]
-                               int F, int n, size_t Np, int n_dir, int* cell, double* sdg, double* svo, int* snb,
-                               double* sfc) {
+                               const int* __restrict__ bidx,                                // [n] boundary-cell row or -1
+                               int F, int n, size_t Np, int n_dir, int* cell, int* sbidx, double* sdg, double* svo,
+                               int* snb, double* sfc) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     const int d = blockIdx.y;
     if (j >= n) return;
     const size_t pj = (size_t)d * n + j;
     const int c = perm[pj];
     cell[pj] = c;
+    sbidx[pj] = bidx[c];
     sdg[pj] = dg[(size_t)d * Np + c];
     svo[pj] = vo[(size_t)d * Np + c];
     for (int f = 0; f < F; ++f) {

@@ -8,17 +8,25 @@ a 1e-7 m square, 2 x 100^2 jittered-Delaunay triangles (20,000 cells), DM=2 with
 (seeded synthetic data; the reference ships no such mesh).  One step is one
 complete solve: the source iteration from e = 0 to margin <= 1e-5 with all
 1,280 (band, direction) systems solved on the GPU every outer iteration.
+Default form: upwind sweeps (exact per-direction solves, FP64) with the
+learned outer-iteration accelerator (--accel learned; aitken / none for the
+others).  The line reports the result's relative L2 distance (of T - T_ref) to
+the field converged to margin 1e-10, the same form without the accelerator,
+and the plain FP64 BiCGSTAB and mixed FP32/FP64 forms scaled from a few
+outer iterations to the unaccelerated iteration count.
 
   value  device seconds per solve with inputs resident in HBM (CUDA events on
          the solve stream, summed over the outer loop), max over ranks
   e2e    host wall seconds per solve through the C ABI with host buffers:
-         bte_set_geometry/quadrature/bands/bcs (H2D), bte_solve,
+         bte_set_geometry/quadrature/bands/bcs/centroids and the MLP
+         weights (H2D), bte_solve,
          bte_get_temperature + bte_get_heat_flux (D2H)
   roofline  the dominant kernel of a profiled solve: algorithmic bytes per
          launch / CUDA-event time per launch, against MEASURED_PEAKS.json
   cpu_baseline  the oracle (CPU restatement of the reference's PETSc path:
          GMRES(30)+ILU(0) per system, all host threads), timed on a bounded
-         sample of 2 outer iterations and scaled by the outer-iteration count
+         sample of 2 outer iterations and scaled by the unaccelerated
+         outer-iteration count (the reference's)
 
 --impl reference times the reference's CPU path the same way (the oracle
 port; the reference's own build needs its sources, which are not on the GPU
@@ -59,6 +67,8 @@ def parse_args():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="square20k")
     ap.add_argument("--form", default="sweep", choices=["plain", "mixed", "sweep"])
+    ap.add_argument("--accel", default="learned", choices=["none", "aitken", "learned"],
+                    help="outer-iteration accelerator of the timed solve (the plain iteration still runs to margin 1e-5)")
     ap.add_argument("--plain-iters", type=int, default=3,
                     help="outer iterations of the plain FP64 and mixed BiCGSTAB forms timed for the comparison")
     ap.add_argument("--e2e-steps", type=int, default=2)
@@ -233,6 +243,14 @@ def run_ours(args, rank, world, local):
         torch.cuda.set_device(local)
         ctx = S.Context(local).load(prob)
         solve_kw = dict(max_iter=args.max_iter, tol=1e-5, form=form, inner_tol=1e-9, inner_maxit=1000)
+        mlp = None
+        if args.accel != "none":
+            from staticbtesolver_gb300 import learned
+
+            solve_kw.update(accel=1 if args.accel == "learned" else 2, accel_every=learned.EVERY)
+            if args.accel == "learned":
+                mlp = learned.load()
+                ctx.set_mlp(mlp)
         for _ in range(args.warmup):
             ctx.solve(**solve_kw)
         barrier(world)
@@ -260,11 +278,14 @@ def run_ours(args, rank, world, local):
         h2d = sum(np.asarray(arrays[k]).nbytes for k in ("nbr", "area", "normal", "volume", "s", "S", "omega"))
         h2d += sum(np.asarray(v).nbytes for v in arrays["bands"].values()) + sum(
             np.asarray(v).nbytes for v in arrays["bcs"].values())
+        h2d += sum(np.asarray(arrays[k]).nbytes for k in ("centroid",)) + (mlp.nbytes if mlp is not None else 0)
         ctx2 = S.Context(local)
         T2, q2 = np.zeros(0), np.zeros(0)
         for _ in range(args.e2e_steps):
             w0 = time.perf_counter()
             ctx2.set_arrays(arrays)
+            if mlp is not None:
+                ctx2.set_mlp(mlp)
             st2, rep2 = ctx2.solve(**solve_kw)
             T2 = ctx2.temperature()
             q2, _ = ctx2.heat_flux()
@@ -272,6 +293,34 @@ def run_ours(args, rank, world, local):
         d2h = T2.nbytes + q2.nbytes
         e2e = max_over_ranks(statistics.mean(e2e_t), world) if e2e_t else None
         ctx2.close()
+
+        # accuracy of the timed result against the field converged to margin 1e-10
+        # (same form, no accelerator), and the same form without the accelerator
+        conv_kw = dict(solve_kw, tol=1e-10, accel=0)
+        ctx.solve(**conv_kw)
+        T_conv = ctx.temperature()
+        rel = lambda a: float(np.linalg.norm(a - T_conv) / np.linalg.norm(T_conv - p.T_ref))
+        base_kw = dict(solve_kw, accel=0)
+        ctx.solve(**base_kw)
+        st_b, rep_b = ctx.solve(**base_kw)
+        no_accel = {"s": rep_b.ms_total / 1e3, "outer_iterations": rep_b.n_iter,
+                    "rel_l2_vs_converged": rel(ctx.temperature())}
+        n_plain_outer = rep_b.n_iter  # the reference's iteration count (same recurrence, parity-tested)
+        other = {}
+        from staticbtesolver_gb300 import learned as _learned
+        if mlp is None and os.path.exists(_learned.WEIGHTS):
+            ctx.set_mlp(_learned.load())
+        for name, akw in ((f"aitken_every{_learned.EVERY}", dict(accel=2, accel_every=_learned.EVERY)),
+                          ("aitken_every8", dict(accel=2, accel_every=8)),
+                          (f"learned_every{_learned.EVERY}", dict(accel=1, accel_every=_learned.EVERY))):
+            if akw["accel"] == solve_kw.get("accel") and akw["accel_every"] == solve_kw.get("accel_every"):
+                continue
+            if akw["accel"] == 1 and not os.path.exists(_learned.WEIGHTS):
+                continue
+            ctx.solve(**dict(solve_kw, **akw))
+            st_o, rep_o = ctx.solve(**dict(solve_kw, **akw))
+            other[name] = {"s": rep_o.ms_total / 1e3, "outer_iterations": rep_o.n_iter, "jumps": rep_o.accel_steps,
+                           "reverts": rep_o.accel_reverts, "rel_l2_vs_converged": rel(ctx.temperature())}
 
         # plain FP64 form (the reference GPU algorithm, batched) and the mixed
         # FP32/FP64 form: a bounded number of outer iterations each, scaled by
@@ -285,7 +334,7 @@ def run_ours(args, rank, world, local):
             ctx.solve(profile=True, **pkw)
             pstats = ctx.kernel_stats()
             return {"s_per_outer_iteration": per_outer, "outer_iterations_timed": rep_p.n_iter,
-                    "s_extrapolated": per_outer * last["n_iter"],
+                    "s_extrapolated": per_outer * n_plain_outer,
                     "inner_iterations_per_system": rep_p.inner_iterations / max(rep_p.inner_solves, 1),
                     "kernels": {k: {"launches": v["launches"], "ms": round(v["ms"], 3),
                                     "GB/s": round(v["bytes"] / (v["ms"] / 1e3) / 1e9, 1) if v["ms"] > 0 else None}
@@ -323,20 +372,23 @@ def run_ours(args, rank, world, local):
         if rank != 0:
             return
         cpu = None
-        n_outer = last["n_iter"]
+        n_outer = n_plain_outer
         if not args.no_cpu_baseline and world == 1:
             threads = os.cpu_count() or 1
             t_iter, inner = cpu_sample(p, threads)
             cpu = {"value": t_iter * n_outer, "unit": UNIT, "cores": threads, "kind": "port",
                    "sample": f"oracle (GMRES(30)+ILU(0) per system, as the reference CPU path) on 2 outer "
                              f"iterations x {inner['solves'] // 2} systems, {t_iter:.2f} s per outer iteration, "
-                             f"scaled by the {n_outer} outer iterations of this solve"}
+                             f"scaled by the {n_outer} outer iterations of the unaccelerated solve"}
         line = {
             "metric": METRIC, "value": t_step, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": args.workload, "form": args.form, "cells": prob.n_cell, "directions": prob.n_dir,
-                       "bands": prob.n_band, "systems": prob.n_dir * prob.n_band, "outer_iterations": n_outer,
+            "config": {"workload": args.workload, "form": args.form, "accel": args.accel,
+                       "accel_every": solve_kw.get("accel_every"), "accel_jumps": last["accel_steps"],
+                       "rel_l2_vs_converged": rel(T), "cells": prob.n_cell, "directions": prob.n_dir,
+                       "bands": prob.n_band, "systems": prob.n_dir * prob.n_band, "outer_iterations": last["n_iter"],
+                       "no_accel": no_accel, "other_accelerators": other,
                        "inner_iterations": last["inner_iterations"], "final_margin": last["final_margin"],
                        "ms_rhs": round(last["ms_rhs"], 2), "ms_inner": round(last["ms_inner"], 2),
                        "ms_reduce": round(last["ms_reduce"], 2), "wall_s_per_step": statistics.mean(wall),

@@ -104,6 +104,7 @@ typedef struct bte_report {
     int sweep_group;           /* sweep form: bands per block and threads per block */
     int sweep_threads;         /* chosen by timing candidate shapes on a plan's first sweep */
     int accel_steps;           /* outer-iteration extrapolations applied */
+    int accel_reverts;         /* extrapolations undone (state restored) */
 } bte_report;
 
 /* Fill opts with the reference's defaults (max_iter 10000 as BTEcmd's -I default,
@@ -171,9 +172,11 @@ bte_status bte_get_margins(bte_ctx* ctx, double* margins, int cap, int* n);
  * (8 -> 128 -> 128 -> 128 -> 1, BF16 weights, FP32 accumulation on the tensor
  * cores).  MLP inputs: d1/s, d2/s, d3/s, A/64, x and y of the centroid scaled
  * to [0, 1] over the mesh, log(V / mean V), log10(Kn) with Kn =
- * (sum_b Lr_b v_b tau_b / sum_b Lr_b) / V^(1/dim).  If the margin
- * accel_every-1 iterations after a jump is not below the margin at the jump,
- * extrapolation stops for the rest of the solve.  Parameters: FP32,
+ * (sum_b Lr_b v_b tau_b / sum_b Lr_b) / V^(1/dim).  The state before each
+ * jump is kept; if the margin accel_every-1 iterations after a jump is not
+ * below the margin at the jump, the state is restored and extrapolation stops
+ * for the rest of the solve, so a bad jump costs accel_every-1 iterations and
+ * no more.  Parameters: FP32,
  * bte_mlp_param_count() values, W1[8][128] b1 W2[128][128] b2 W3[128][128] b3
  * W4[128][1] b4. */
 int bte_mlp_param_count(void);

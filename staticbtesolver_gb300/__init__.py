@@ -61,7 +61,7 @@ class Report(C.Structure):
                 ("inner_unconverged", C.c_longlong), ("refinements", C.c_longlong), ("ms_total", C.c_double),
                 ("ms_rhs", C.c_double), ("ms_inner", C.c_double), ("ms_reduce", C.c_double),
                 ("kernel_launches", C.c_longlong), ("sweep_group", C.c_int), ("sweep_threads", C.c_int),
-                ("accel_steps", C.c_int)]
+                ("accel_steps", C.c_int), ("accel_reverts", C.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -116,7 +116,8 @@ struct bte_ctx {
     bool sweep_margin = false;  // acyclic plan: the sweep sums the margin partials (d_spart)
     long long plan_levels = 0;
     DevBuf p_cell, p_dg, p_vo, p_nb, p_fc, p_lvl, p_lvl_off, p_part, p_bad, p_invd, d_spart, p_bidx;
-    DevBuf d_bcell, d_bidx, d_bsum;  // cells with boundary faces, cell -> row, boundary rhs per (system, row)
+    DevBuf d_bcell, d_bidx, d_bsum;
+    DevBuf d_snap_e, d_snap_T, d_snap_ebar;  // accelerator: state before the last jump  // cells with boundary faces, cell -> row, boundary rhs per (system, row)
     int nbcell = 0;
     // sweep launch shape (bands per block, threads per block) picked by timing
     // the candidates on the first sweep of a plan
@@ -1094,6 +1095,10 @@ extern "C" bte_status bte_solve(bte_ctx* ctx, const bte_options* opts, bte_repor
             return fail(ctx, BTE_ERR_STATE, "bte_solve: the accelerator needs bte_set_centroids");
         BTE_CUDA(upload(ctx->d_centroid, ctx->centroid, st));
         BTE_CUDA(ctx->d_ring.alloc(sizeof(double) * 4 * Np));
+        // the state before the last jump, restored when the jump does not pay off
+        BTE_CUDA(ctx->d_snap_e.alloc(sizeof(double) * (size_t)NB * ND * Np));
+        BTE_CUDA(ctx->d_snap_T.alloc(sizeof(double) * Np));
+        BTE_CUDA(ctx->d_snap_ebar.alloc(sizeof(double) * (size_t)NB * Np));
         BTE_CUDA(ctx->d_feat.alloc(sizeof(__nv_bfloat16) * bte::mlp::IN_PAD * ctx->n));
         BTE_CUDA(ctx->d_scale.alloc(sizeof(double) * ctx->n));
         BTE_CUDA(ctx->d_y.alloc(sizeof(float) * ctx->n));
@@ -1194,11 +1199,28 @@ extern "C" bte_status bte_solve(bte_ctx* ctx, const bte_options* opts, bte_repor
         }
         // outer-iteration extrapolation (accel): stop for good when the margin
         // accel_every-1 iterations after a jump is not below the margin at it
-        if (o.accel && accel_on && accel_last >= 0 && it == accel_last + o.accel_every - 1 && m >= accel_margin)
+        // accel_every-1 iterations after a jump: keep it if the margin is below
+        // the margin at the jump (right after a jump the margin rises while the
+        // intensities follow the new source, so it is judged once they have);
+        // otherwise restore the state before the jump and stop extrapolating
+        if (o.accel && accel_on && accel_last >= 0 && it == accel_last + o.accel_every - 1 &&
+            !(m < accel_margin)) {
             accel_on = false;
+            const size_t ne = (size_t)NB * ND * Np;
+            BTE_CUDA(cudaMemcpyAsync(ctx->e_curr, ctx->d_snap_e.p, sizeof(double) * ne, cudaMemcpyDeviceToDevice, st));
+            BTE_CUDA(cudaMemcpyAsync(ctx->d_T.p, ctx->d_snap_T.p, sizeof(double) * Np, cudaMemcpyDeviceToDevice, st));
+            BTE_CUDA(cudaMemcpyAsync(ctx->d_ebar.p, ctx->d_snap_ebar.p, sizeof(double) * NB * Np,
+                                     cudaMemcpyDeviceToDevice, st));
+            ++rep.accel_reverts;
+        }
         if (o.accel && accel_on && it >= 3 && (accel_last < 0 || it - accel_last >= o.accel_every)) {
             const int n = ctx->n;
             const int s0 = it % 4, s1 = (it + 3) % 4, s2 = (it + 2) % 4, s3 = (it + 1) % 4;
+            BTE_CUDA(cudaMemcpyAsync(ctx->d_snap_e.p, ctx->e_curr, sizeof(double) * (size_t)NB * ND * Np,
+                                     cudaMemcpyDeviceToDevice, st));
+            BTE_CUDA(cudaMemcpyAsync(ctx->d_snap_T.p, ctx->d_T.p, sizeof(double) * Np, cudaMemcpyDeviceToDevice, st));
+            BTE_CUDA(cudaMemcpyAsync(ctx->d_snap_ebar.p, ctx->d_ebar.p, sizeof(double) * NB * Np,
+                                     cudaMemcpyDeviceToDevice, st));
             BTE_LAUNCH(KK_REDUCE, -1, 0, 0,
                        bte::mlp::k_accel_features<<<(n + 255) / 256, 256, 0, st>>>(
                            ctx->d_ring.as<double>(), s0, s1, s2, s3, Np, n, fg, ctx->d_feat.as<__nv_bfloat16>(),

@@ -141,6 +141,19 @@ struct FaceFluxOp {
             off = fma(fc[((size_t)d * F + f) * Np + c], (double)xs[nb[(size_t)f * Np + c]], off);
         return (T)fma(k, off, acc);
     }
+    // (A M v)[c] with M = 1/D (the Jacobi preconditioner) and ph = M v: the
+    // diagonal term D (M v)[c] is v[c] itself, so only the inflow coupling is
+    // computed -- 2 FP64 operations per cell fewer than apply(ph), which
+    // matters on GB300's FP64 pipe.  Equal to apply(ph) up to rounding.
+    template <typename T>
+    __device__ __forceinline__ T apply_pc(int y, int c, const T* __restrict__ ph, const T* __restrict__ v) const {
+        int b, d;
+        bd(y, b, d);
+        double off = 0.0;
+        for (int f = 0; f < F; ++f)
+            off = fma(fc[((size_t)d * F + f) * Np + c], (double)ph[nb[(size_t)f * Np + c]], off);
+        return (T)fma(kb[b], off, (double)v[c]);
+    }
 };
 
 // One or more independent CSR systems (the reference's BICGSTAB boundary).
@@ -168,10 +181,22 @@ struct CsrOp {
         for (int k = rowptr[c]; k < rowptr[c + 1]; ++k) s = fma(val[k], (double)xs[col[k]], s);
         return (T)s;
     }
+    // a general CSR matrix: A (M v) computed as A ph (the reference's SpMV)
+    template <typename T>
+    __device__ __forceinline__ T apply_pc(int y, int c, const T* __restrict__ ph, const T* __restrict__) const {
+        return apply<T>(y, c, ph);
+    }
 };
 
 #define BTE_CELL_LOOP(c)                                                     \
-    for (int _k = 0, c = blockIdx.x * CH + threadIdx.x; _k < CPT; ++_k, c += THREADS)
+    _Pragma("unroll") for (int _k = 0, c = blockIdx.x * CH + threadIdx.x; _k < CPT; ++_k, c += THREADS)
+
+// The vector-update kernels load a group of GRP cells' operands into registers
+// before computing and storing any of them, so each thread keeps GRP x (number
+// of operands) loads in flight.
+constexpr int GRP = 4;
+#define BTE_GROUP_LOOP(c0)                                                   \
+    _Pragma("unroll") for (int c0 = blockIdx.x * CH + threadIdx.x; c0 < (int)(blockIdx.x + 1) * CH; c0 += GRP * THREADS)
 
 // FP32 counterpart of FaceFluxOp for the mixed form: per-direction geometry
 // stored in FP32 and pre-scaled by kappa_d = 1 / mean(V Omega_d), so the
@@ -206,6 +231,14 @@ struct FaceFluxOp32 {
         float off = 0.0f;
         for (int f = 0; f < F; ++f) off = fmaf(fc[((size_t)d * F + f) * Np + c], (float)xs[nb[(size_t)f * Np + c]], off);
         return (T)fmaf(k, off, acc);
+    }
+    template <typename T>
+    __device__ __forceinline__ T apply_pc(int y, int c, const T* __restrict__ ph, const T* __restrict__ v) const {
+        int b, d;
+        bd(y, b, d);
+        float off = 0.0f;
+        for (int f = 0; f < F; ++f) off = fmaf(fc[((size_t)d * F + f) * Np + c], (float)ph[nb[(size_t)f * Np + c]], off);
+        return (T)fmaf(kb[b], off, (float)v[c]);
     }
 };
 
@@ -320,16 +353,33 @@ __global__ void __launch_bounds__(THREADS) k_bicg_p(Op op, BicgVecs<T> v, BicgSt
         st.flagA[par * st.S + y] = 0; st.flagB[par * st.S + y] = 0;
     }
     const size_t o = (size_t)y * v.Np;
-    BTE_CELL_LOOP(c) {
-        // cublasDaxpy(-omega, q, p); cublasDscal(beta, p); cublasDaxpy(1, r, p)
-        T pv = fmat(-om, v.q[o + c], v.p[o + c]);
-        pv = fmat(bt, pv, v.r[o + c]);
-        v.p[o + c] = pv;
-        v.ph[o + c] = v.invD[o + c] * pv;
+    // restrict-qualified row pointers: the unrolled cell loop may issue all
+    // its loads before the first store
+    const T* __restrict__ q = v.q + o;
+    const T* __restrict__ r = v.r + o;
+    const T* __restrict__ iD = v.invD + o;
+    T* __restrict__ p = v.p + o;
+    T* __restrict__ ph = v.ph + o;
+    BTE_GROUP_LOOP(c0) {
+        T qv[GRP], pv[GRP], rv[GRP], dv[GRP];
+#pragma unroll
+        for (int k = 0; k < GRP; ++k) {
+            const int c = c0 + k * THREADS;
+            qv[k] = q[c]; pv[k] = p[c]; rv[k] = r[c]; dv[k] = iD[c];
+        }
+#pragma unroll
+        for (int k = 0; k < GRP; ++k) {
+            const int c = c0 + k * THREADS;
+            // cublasDaxpy(-omega, q, p); cublasDscal(beta, p); cublasDaxpy(1, r, p)
+            T u = fmat(-om, qv[k], pv[k]);
+            u = fmat(bt, u, rv[k]);
+            p[c] = u;
+            ph[c] = dv[k] * u;
+        }
     }
 }
 
-// K2: q = A ph; partial r_hat . q
+// K2: q = A ph (= A M p); partial r_hat . q
 template <typename Op, typename T>
 __global__ void __launch_bounds__(THREADS) k_bicg_spmv1(Op op, BicgVecs<T> v, BicgState st, int i) {
     __shared__ double sm[1][NWARP];
@@ -337,12 +387,15 @@ __global__ void __launch_bounds__(THREADS) k_bicg_spmv1(Op op, BicgVecs<T> v, Bi
     const int par = i & 1;
     if (st.done[y] | st.flagA[par * st.S + y]) return;
     const size_t o = (size_t)y * v.Np;
-    const T* ph = v.ph + o;
+    const T* __restrict__ ph = v.ph + o;
+    const T* __restrict__ pv = v.p + o;
+    const T* __restrict__ rw = v.rw + o;
+    T* __restrict__ q = v.q + o;
     T acc_t = 0;
     BTE_CELL_LOOP(c) {
-        const T qv = op.template apply<T>(y, c, ph);
-        v.q[o + c] = qv;
-        acc_t = fmat(v.rw[o + c], qv, acc_t);
+        const T qv = op.template apply_pc<T>(y, c, ph, pv);
+        q[c] = qv;
+        acc_t = fmat(rw[c], qv, acc_t);
     }
     double acc[1] = {(double)acc_t};
     block_sum<1>(acc, sm);
@@ -370,14 +423,28 @@ __global__ void __launch_bounds__(THREADS) k_bicg_s(Op op, BicgVecs<T> v, BicgSt
     if (lead) st.alpha[y] = alpha;
     const T al = (T)alpha;
     const size_t o = (size_t)y * v.Np;
-    BTE_CELL_LOOP(c) {
-        const T s = fmat(-al, v.q[o + c], v.r[o + c]);
-        v.r[o + c] = s;
-        v.z[o + c] = v.invD[o + c] * s;
+    const T* __restrict__ q = v.q + o;
+    const T* __restrict__ iD = v.invD + o;
+    T* __restrict__ r = v.r + o;
+    T* __restrict__ z = v.z + o;
+    BTE_GROUP_LOOP(c0) {
+        T qv[GRP], rv[GRP], dv[GRP];
+#pragma unroll
+        for (int k = 0; k < GRP; ++k) {
+            const int c = c0 + k * THREADS;
+            qv[k] = q[c]; rv[k] = r[c]; dv[k] = iD[c];
+        }
+#pragma unroll
+        for (int k = 0; k < GRP; ++k) {
+            const int c = c0 + k * THREADS;
+            const T sv = fmat(-al, qv[k], rv[k]);
+            r[c] = sv;
+            z[c] = dv[k] * sv;
+        }
     }
 }
 
-// K4: t = A z; partials t.s, t.t
+// K4: t = A z (= A M s); partials t.s, t.t
 template <typename Op, typename T>
 __global__ void __launch_bounds__(THREADS) k_bicg_spmv2(Op op, BicgVecs<T> v, BicgState st, int i) {
     __shared__ double sm[2][NWARP];
@@ -385,12 +452,14 @@ __global__ void __launch_bounds__(THREADS) k_bicg_spmv2(Op op, BicgVecs<T> v, Bi
     const int par = i & 1;
     if (st.done[y] | st.flagA[par * st.S + y] | st.flagB[par * st.S + y]) return;
     const size_t o = (size_t)y * v.Np;
-    const T* z = v.z + o;
+    const T* __restrict__ z = v.z + o;
+    const T* __restrict__ sv = v.r + o;  // s, stored in r by K3
+    T* __restrict__ t = v.t + o;
     T a0 = 0, a1 = 0;
     BTE_CELL_LOOP(c) {
-        const T tv = op.template apply<T>(y, c, z);
-        v.t[o + c] = tv;
-        a0 = fmat(tv, v.r[o + c], a0);
+        const T tv = op.template apply_pc<T>(y, c, z, sv);
+        t[c] = tv;
+        a0 = fmat(tv, sv[c], a0);
         a1 = fmat(tv, tv, a1);
     }
     double acc[2] = {(double)a0, (double)a1};
@@ -418,16 +487,31 @@ __global__ void __launch_bounds__(THREADS) k_bicg_x(Op op, BicgVecs<T> v, BicgSt
     if (lead) st.omega[y] = omega;
     const T al = (T)alpha, om = (T)omega;
     const size_t o = (size_t)y * v.Np;
-    T* x = op.x_of(y);
+    T* __restrict__ x = op.x_of(y);
+    const T* __restrict__ ph = v.ph + o;
+    const T* __restrict__ z = v.z + o;
+    const T* __restrict__ t = v.t + o;
+    const T* __restrict__ rw = v.rw + o;
+    T* __restrict__ r = v.r + o;
     T a0 = 0, a1 = 0;
-    BTE_CELL_LOOP(c) {
-        T xv = fmat(al, v.ph[o + c], x[c]);
-        xv = fmat(om, v.z[o + c], xv);
-        x[c] = xv;
-        const T r = fmat(-om, v.t[o + c], v.r[o + c]);
-        v.r[o + c] = r;
-        a0 = fmat(r, r, a0);
-        a1 = fmat(v.rw[o + c], r, a1);
+    BTE_GROUP_LOOP(c0) {
+        T xv[GRP], phv[GRP], zv[GRP], tv[GRP], rv[GRP], wv[GRP];
+#pragma unroll
+        for (int k = 0; k < GRP; ++k) {
+            const int c = c0 + k * THREADS;
+            xv[k] = x[c]; phv[k] = ph[c]; zv[k] = z[c]; tv[k] = t[c]; rv[k] = r[c]; wv[k] = rw[c];
+        }
+#pragma unroll
+        for (int k = 0; k < GRP; ++k) {
+            const int c = c0 + k * THREADS;
+            T u = fmat(al, phv[k], xv[k]);
+            u = fmat(om, zv[k], u);
+            x[c] = u;
+            const T rn = fmat(-om, tv[k], rv[k]);
+            r[c] = rn;
+            a0 = fmat(rn, rn, a0);
+            a1 = fmat(wv[k], rn, a1);
+        }
     }
     double acc[2] = {(double)a0, (double)a1};
     block_sum<2>(acc, sm);

@@ -83,27 +83,32 @@ def features(t0, t1, t2, t3, fg: dict):
 
 
 def jump_rows(margins, every: int = EVERY, tol: float = 1e-5):
-    """Outer iterations at which bte_solve extrapolated (its rule, replayed from the margins):
-    from iteration 3 on, every `every` iterations, until the margin `every`-1 iterations
-    after a jump is not below the margin at it."""
-    on, last, m_at, out = True, -1, 0.0, []
+    """Outer iterations at which bte_solve extrapolated, and those after which it
+    restored the state before a jump (its rule, replayed from the margins): from
+    iteration 3 on, every `every` iterations; `every`-1 iterations after a jump
+    the jump is undone, and extrapolation stops, unless the margin is below the
+    margin at the jump.
+    Returns (jumps, reverts): rows after which the field changed discontinuously."""
+    on, last, m_at, jumps, reverts = True, -1, 0.0, [], []
     for it, m in enumerate(margins):
         if not np.isfinite(m) or m <= tol:
             break
-        if on and last >= 0 and it == last + every - 1 and m >= m_at:
+        if on and last >= 0 and it == last + every - 1 and not (m < m_at):
             on = False
+            reverts.append(it)
         if on and it >= 3 and (last < 0 or it - last >= every):
-            out.append(it)
+            jumps.append(it)
             last, m_at = it, m
-    return out
+    return jumps, reverts
 
 
 def samples_from_history(hist: np.ndarray, fg: dict, every: int = 2, rng=None, max_rows: int = 0, jumps=()):
     """(X, Y) pairs from one solve's temperature history (rows = outer iterations).
 
     Target: the correction to the Aitken estimate, clip(clip((T* - T_k) / s, +-64) - A, +-8),
-    with T* = the last (converged) row.  Row j of a run that extrapolated at j is the
-    field before the jump, so windows T_{k-3} .. T_k with a jump j in [k-3, k-1] are skipped."""
+    with T* = the last (converged) row.  Row j of a run that extrapolated (or restored
+    its state) after iteration j is followed by a discontinuity, so windows
+    T_{k-3} .. T_k with such a j in [k-3, k-1] are skipped."""
     T_star = hist[-1]
     jset = set(int(j) for j in jumps)
     X, Y = [], []
@@ -132,15 +137,15 @@ def mirrored(X, Y):
     return np.concatenate([X, Xm]), np.concatenate([Y, -Y])
 
 
-def training_problems(n: int, seed: int = 7):
+def training_problems(n: int, seed: int = 7, cell_range=(40, 101)):
     """Seeded 2D problems around the 1e-7 m square: size, bands, walls and wall
-    temperatures vary (side log-uniform in [3e-8, 3e-7] m, 12-24 cells per side,
+    temperatures vary (side log-uniform in [3e-8, 3e-7] m, 40-100 cells per side,
     20 or 40 bands, diffuse or specular side walls, 0.5-5 K between the ends)."""
     rng = np.random.default_rng(seed)
     out = []
     for i in range(n):
         side = float(np.exp(rng.uniform(np.log(3e-8), np.log(3e-7))))
-        cells = int(rng.integers(12, 25))
+        cells = int(rng.integers(*cell_range))
         bands = int(rng.choice([20, 40]))
         wall = int(rng.choice([2, 31]))
         dT = float(rng.uniform(0.5, 5.0))
@@ -180,14 +185,14 @@ def generate(specs, max_rows_per_problem: int = 40000, device: int = 0, seed: in
             st, rep = ctx.solve(max_iter=p.max_iter, tol=1e-5, form=S.FORM_SWEEP, keep_history=True, accel=accel,
                                 accel_every=accel_every)
             hist = ctx.history()
-            jumps = jump_rows(ctx.margins(), accel_every) if accel else []
+            jumps, reverts = jump_rows(ctx.margins(), accel_every) if accel else ([], [])
             ctx.close()
-            assert len(jumps) == rep.accel_steps, (len(jumps), rep.accel_steps)
+            assert (len(jumps), len(reverts)) == (rep.accel_steps, rep.accel_reverts), (jumps, reverts, rep.as_dict())
             X, Y = samples_from_history(hist, feature_geometry(prob.arrays()), rng=rng, max_rows=max_rows_per_problem,
-                                        jumps=jumps)
+                                        jumps=jumps + reverts)
             Xs.append(X)
             Ys.append(Y)
-            info.append(dict(spec, n_iter=rep.n_iter, accel=accel, jumps=rep.accel_steps))
+            info.append(dict(spec, n_iter=rep.n_iter, accel=accel, jumps=rep.accel_steps, reverts=rep.accel_reverts))
     return np.concatenate(Xs), np.concatenate(Ys), info
 
 

@@ -39,7 +39,8 @@ def evaluate(params, name="square20k", everies=(4, 6, 8), tol=1e-5):
                 ctx.set_mlp(params)
             ctx.solve(max_iter=20000, tol=t, form=S.FORM_SWEEP, accel=accel, accel_every=every)  # warm
             st, rep = ctx.solve(max_iter=20000, tol=t, form=S.FORM_SWEEP, accel=accel, accel_every=every)
-            out[label] = dict(status=st, n_iter=rep.n_iter, accel_steps=rep.accel_steps, ms=rep.ms_total,
+            out[label] = dict(status=st, n_iter=rep.n_iter, accel_steps=rep.accel_steps, reverts=rep.accel_reverts,
+                              ms=rep.ms_total,
                               T=ctx.temperature())
             ctx.close()
         T0, Tc = out["plain"]["T"] - p.T_ref, out["converged"]["T"] - p.T_ref

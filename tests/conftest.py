@@ -49,8 +49,8 @@ class Case:
         else:
             d = os.path.join(GOLDEN, name)
             meta = json.load(open(os.path.join(d, "expected.json")))
-            if name == "2Dcase2":
-                self.geo = os.path.join(tmpdir, "2Dcase2.mphtxt")
+            if name in ("2Dcase2", "2Dcase5"):
+                self.geo = os.path.join(tmpdir, f"{name}.mphtxt")
                 if not os.path.exists(self.geo):
                     with gzip.open(os.path.join(d, "mesh.mphtxt.gz"), "rb") as fi, open(self.geo, "wb") as fo:
                         shutil.copyfileobj(fi, fo)

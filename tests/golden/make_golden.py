@@ -5,6 +5,8 @@ Sources, all from the reference or from the reference's own code run here:
     2DM2DG,3DM2DG,3DM3DG}): their input files are copied, and their recorded
     logs (*.sol) are parsed into expected.json (margin trajectory and heat
     flux per boundary, 6 significant digits; those logs stop at margin < 1e-4);
+  * tests/testcase/2Dcase5 (78,190-cell mesh, gray band, specular side walls):
+    mesh (gzipped), bands, boundary file, and its recorded GPU log;
   * tests/testcase/2Dcase2 (11,630-cell mesh): mesh (gzipped), bands and both
     recorded logs (GPU BiCGSTAB and CPU GMRES).  Those logs were made with
     specular (type 31) side walls at L = 1e-8 m: with the type-2 file shipped
@@ -96,9 +98,11 @@ def main():
         meta["ref_n_iter"] = int(r.n_iter)
         json.dump(meta, open(os.path.join(dst, "expected.json"), "w"), indent=1)
         print(name, "ref iters", r.n_iter, "q", r.q)
-    # 2Dcase2
+    # 2Dcase2, 2Dcase5
     if want("2Dcase2"):
         case_2dcase2(ref)
+    if want("2Dcase5"):
+        case_2dcase5(ref)
     for name in SYNTH:
         if want(name):
             case_synth(name)
@@ -127,6 +131,30 @@ def case_2dcase2(ref):
     meta["ref_n_iter"] = int(r.n_iter)
     json.dump(meta, open(os.path.join(dst, "expected.json"), "w"), indent=1)
     print("2Dcase2 ref iters", r.n_iter, "q", r.q)
+
+
+def case_2dcase5(ref):
+    """tests/testcase/2Dcase5: 78,190 triangles, gray band, specular side walls as in
+    its inputbc_2D.dat; its GPU log pins the margins (stop below 1e-4) and q."""
+    src = os.path.join(ref, "tests", "testcase", "2Dcase5")
+    dst = os.path.join(HERE, "2Dcase5")
+    os.makedirs(dst, exist_ok=True)
+    with open(os.path.join(src, "2D_78000.mphtxt"), "rb") as fi, gzip.open(os.path.join(dst, "mesh.mphtxt.gz"), "wb") as fo:
+        fo.write(fi.read())
+    shutil.copyfile(os.path.join(src, "inputbc_2D.dat"), os.path.join(dst, "inputbc.dat"))
+    shutil.copyfile(os.path.join(src, "Input-dispersion-relation-fp.dat"), os.path.join(dst, "band.dat"))
+    gm, gq = parse_sol(os.path.join(src, "StaticBTESolver-2DM-1np.sol"))
+    meta = dict(source="tests/testcase/2Dcase5", DM=2, num_theta=8, num_phi=8, L_x=1e-8, L_y=1e-8, L_z=0.0,
+                max_iter=1000, T_ref=300.0, gpu_sol_margins=gm, gpu_sol_heat_flux=gq,
+                sol_stop="first margin below 1e-4")
+    tmp = os.path.join(dst, "mesh.mphtxt")
+    shutil.copyfile(os.path.join(src, "2D_78000.mphtxt"), tmp)
+    r = run_ref(dst, tmp, os.path.join(dst, "inputbc.dat"), os.path.join(dst, "band.dat"), 2, 8, 8, 1e-8, 1e-8, 0.0,
+                1000)
+    os.remove(tmp)
+    meta["ref_n_iter"] = int(r.n_iter)
+    json.dump(meta, open(os.path.join(dst, "expected.json"), "w"), indent=1)
+    print("2Dcase5 ref iters", r.n_iter, "q", r.q)
 
 
 def case_synth(name):

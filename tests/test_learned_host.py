@@ -5,17 +5,23 @@ from staticbtesolver_gb300 import learned
 
 
 def test_jump_rows_replays_the_solver_rule():
-    # geometric decay: a jump every EVERY iterations from iteration 3 on
+    # every jump pays off: a jump every EVERY iterations from iteration 3 on
     m = 10.0 * 0.8 ** np.arange(40)
-    assert learned.jump_rows(m, 6) == [3, 9, 15, 21, 27, 33, 39]
-    # the margin 5 iterations after the jump at 9 is not below the margin at it: stop for good
-    m2 = m.copy()
-    m2[14] = m2[9]
-    assert learned.jump_rows(m2, 6) == [3, 9]
+    good = m.copy()
+    for j in range(3, 40, 6):
+        good[j + 1:] *= 0.1
+    jumps, reverts = learned.jump_rows(good, 6, tol=0.0)
+    assert jumps == [3, 9, 15, 21, 27, 33, 39] and reverts == []
+    # the margin 5 iterations after the jump at 3 is not below the margin at
+    # the jump: restore, and no more jumps
+    bad = m.copy()
+    bad[8] = bad[3]
+    jumps, reverts = learned.jump_rows(bad, 6, tol=0.0)
+    assert jumps == [3] and reverts == [8]
     # no jump on or after the converged iteration
-    m3 = m.copy()
-    m3[12] = 1e-6
-    assert learned.jump_rows(m3, 6, tol=1e-5) == [3, 9]
+    g2 = good.copy()
+    g2[12] = 1e-6
+    assert learned.jump_rows(g2, 6, tol=1e-5) == ([3, 9], [])
 
 
 def test_windows_spanning_a_jump_are_skipped():

@@ -17,6 +17,8 @@
 #include "BTEBand.h"
 #include "BTEBoundaryCondition.h"
 #include "BTEMesh.h"
+#include <string>
+
 #include "utility.h"
 
 struct bte_ctx;
@@ -47,6 +49,9 @@ public:
     const std::vector<double>& bandHeatFlux() const { return bc_band_heat_flux_; }     // [N_bc][N_band]
     const std::vector<double>& margins() const { return margins_; }
     double iterationMilliseconds() const { return ms_iteration_; }
+    // The field dump the reference has commented out (src/StaticBTESolver.cpp:818-831):
+    // "x/L_x y/L_y [z/L_z] T" per cell; false if nothing was solved or the file fails.
+    bool writeTempcell(const std::string& path = "Tempcell.dat") const;
 
 private:
     BTEMesh* mesh_;
@@ -61,6 +66,8 @@ private:
     double ms_iteration_ = 0;
     bte_ctx* ctx_ = nullptr;
     std::vector<double> cell_temperature_, cell_band_temperature_, bc_heat_flux_, bc_band_heat_flux_, margins_;
+    std::vector<double> cell_centroid_;
+    int dim_ = 0;
 };
 
 #endif

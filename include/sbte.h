@@ -31,6 +31,10 @@ void sbte_bands(const sbte_problem* p, double* vg, double* tau, double* C, doubl
 void sbte_bcs(const sbte_problem* p, int* index, int* type, double* T);
 /* bte_set_geometry/quadrature/bands/bcs on ctx; returns a bte_status. */
 int sbte_upload(const sbte_problem* p, bte_ctx* ctx);
+/* Write T [n] at the cell centroids [n][3] in the reference's Tempcell.dat
+ * format (src/StaticBTESolver.cpp:818-831, commented out there); 0 on success. */
+int sbte_write_tempcell(const char* path, int n, int dim, const double* centroid, const double* T, double L_x,
+                        double L_y, double L_z);
 /* BTEcmd's main (argv[0] is the program name). */
 int sbte_main(int argc, char** argv);
 

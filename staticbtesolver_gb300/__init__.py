@@ -137,6 +137,8 @@ def _load():
     H.sbte_bcs.argtypes = [vp, _ip, _ip, _dp]
     H.sbte_upload.restype = C.c_int
     H.sbte_upload.argtypes = [vp, vp]
+    H.sbte_write_tempcell.restype = C.c_int
+    H.sbte_write_tempcell.argtypes = [C.c_char_p, C.c_int, C.c_int, _dp, _dp, C.c_double, C.c_double, C.c_double]
     _cuda, _host = L, H
     return L, H
 
@@ -349,6 +351,20 @@ class Context:
                       report=rep.as_dict(), status=st)
 
 
+def write_tempcell(path, centroid, T, dim, L):
+    """T at the cell centroids in the reference's Tempcell.dat format
+    (src/StaticBTESolver.cpp:818-831): "x/L_x y/L_y [z/L_z] T" per cell."""
+    _, H = _load()
+    cen = np.ascontiguousarray(centroid, np.float64).reshape(-1, 3)
+    T = np.ascontiguousarray(T, np.float64)
+    if len(T) != len(cen):
+        raise BteError(1, "write_tempcell: centroid and T sizes differ")
+    st = H.sbte_write_tempcell(str(path).encode(), len(T), int(dim), cen, T,
+                               *map(float, L))
+    if st != 0:
+        raise BteError(st, H.sbte_error().decode())
+
+
 class StaticBTESolver:
     """Python mirror of the reference's StaticBTESolver (ctor, setParam, solve) on file inputs."""
 
@@ -367,8 +383,14 @@ class StaticBTESolver:
         ctx = Context(self._device).load(p)
         st, rep = ctx.solve(max_iter=max_iter, tol=tol, form=form, inner_tol=inner_tol, on_iteration=on_iteration)
         self.result = ctx.result(st, rep)
+        self._geometry = (p.arrays()["centroid"], p.dim)
         ctx.close()
         return self.result
+
+    def writeTempcell(self, path="Tempcell.dat"):
+        if self.result is None:
+            raise BteError(2, "writeTempcell: solve first")
+        write_tempcell(path, self._geometry[0], self.result.T, self._geometry[1], self._L)
 
 
 def bicgstab_csr(rowptr, col, val, b, maxit=1000, tol=1e-9):

@@ -4,6 +4,8 @@
 //   --form plain|mixed|sweep   inner-solve form (default plain: FP64 BiCGSTAB as the reference GPU path)
 //   --tol X              outer margin threshold (default 1e-5)
 //   --inner-tol X        inner relative residual (default 1e-9)
+//   --tempcell FILE      write the cell temperatures as the reference's Tempcell.dat
+//                        ("x/L_x y/L_y [z/L_z] T" per cell, src/StaticBTESolver.cpp:818-831)
 #include <getopt.h>
 
 #include <chrono>
@@ -31,8 +33,9 @@ extern "C" int sbte_main(int argc, char** argv) {
                                        {"form", required_argument, nullptr, 1001},
                                        {"tol", required_argument, nullptr, 1002},
                                        {"inner-tol", required_argument, nullptr, 1003},
+                                       {"tempcell", required_argument, nullptr, 1004},
                                        {nullptr, 0, nullptr, 0}};
-    std::string geo, bandfile, bcfile;
+    std::string geo, bandfile, bcfile, tempcell;
     double L_x = 0, L_y = 0, L_z = 0, T_ref = 300, tol = 1e-5, inner_tol = 1e-9;
     int DM = 3, ntheta = 4, nphi = 4, maxIter = 10000, form = 0;
     bool has_bc = false;
@@ -54,6 +57,7 @@ extern "C" int sbte_main(int argc, char** argv) {
             case 1001: form = std::string(optarg) == "mixed" ? 1 : std::string(optarg) == "sweep" ? 2 : 0; break;
             case 1002: tol = std::stod(optarg); break;
             case 1003: inner_tol = std::stod(optarg); break;
+            case 1004: tempcell = optarg; break;
             default: std::cerr << "Unknown option " << c << std::endl; return 1;
         }
     }
@@ -94,6 +98,10 @@ extern "C" int sbte_main(int argc, char** argv) {
         solver.setInnerTolerance(inner_tol);
         solver.solve(maxIter);
         rc = (solver.status() == 0 || solver.status() == 6) ? 0 : 1;
+        if (rc == 0 && !tempcell.empty() && !solver.writeTempcell(tempcell)) {
+            std::cerr << "cannot write " << tempcell << std::endl;
+            rc = 1;
+        }
     }
     const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - start).count();
     std::cout << "Time taken by process: " << ms << " milliseconds" << std::endl;  // src/BTEMain.cpp:185-188

@@ -99,6 +99,8 @@ void StaticBTESolver::solve(int max_iter) {
     bte_get_temperature(ctx_, cell_temperature_.data());
     bte_get_band_temperature(ctx_, cell_band_temperature_.data());
     if (P.n_bc > 0) bte_get_heat_flux(ctx_, bc_heat_flux_.data(), bc_band_heat_flux_.data());
+    cell_centroid_ = P.centroid;
+    dim_ = mesh_->dim;
     margins_.assign(rep.n_iter, 0.0);
     int nm = 0;
     bte_get_margins(ctx_, margins_.data(), (int)margins_.size(), &nm);
@@ -106,4 +108,11 @@ void StaticBTESolver::solve(int max_iter) {
         for (int i = 0; i < P.n_bc; ++i)  // :365-368
             std::cout << "heat flux of Boundary Condition #" << -1 - P.bc_index[i] << ": " << bc_heat_flux_[i]
                       << std::endl;
+}
+
+bool StaticBTESolver::writeTempcell(const std::string& path) const {
+    const int n = (int)cell_temperature_.size();
+    if (n == 0 || (int)cell_centroid_.size() != 3 * n) return false;
+    return sbte::write_tempcell(path, n, dim_, cell_centroid_.data(), cell_temperature_.data(), mesh_->L_x, mesh_->L_y,
+                                mesh_->L_z);
 }

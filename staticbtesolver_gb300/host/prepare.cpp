@@ -12,6 +12,7 @@
 //    among the boundary elements, and keeps 0 (an interior link to cell 0)
 //    when none matches;
 //  * the boundary element that wins is the first one in file order.
+#include <fstream>
 #include "prepare.h"
 
 #include <chrono>
@@ -292,6 +293,19 @@ int upload(const Prepared& P, bte_ctx* ctx) {
     rc = bte_set_bands(ctx, P.n_band, P.vg.data(), P.tau.data(), P.C.data(), P.Lr.data());
     if (rc) return rc;
     return bte_set_bcs(ctx, P.n_bc, P.bc_index.data(), P.bc_type.data(), P.bc_T.data());
+}
+
+bool write_tempcell(const std::string& path, int n, int dim, const double* centroid, const double* T, double L_x,
+                    double L_y, double L_z) {
+    std::ofstream out(path);
+    if (!out) return false;
+    for (int i = 0; i < n; ++i) {
+        out << centroid[3 * i] / L_x << " ";
+        if (dim >= 2) out << centroid[3 * i + 1] / L_y << " ";
+        if (dim == 3) out << centroid[3 * i + 2] / L_z << " ";
+        out << T[i] << "\n";
+    }
+    return static_cast<bool>(out);
 }
 
 }  // namespace sbte

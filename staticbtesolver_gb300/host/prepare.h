@@ -32,4 +32,12 @@ int prepare(const BTEMesh& mesh, const BTEBand& bands, const BTEBoundaryConditio
 // bte_set_geometry / bte_set_quadrature / bte_set_bands / bte_set_bcs.
 int upload(const Prepared& p, bte_ctx* ctx);
 
+// Cell temperatures in the format of the reference's (commented-out) field
+// dump, src/StaticBTESolver.cpp:818-831: one line per cell, "x/L_x y/L_y T"
+// (3D: "x/L_x y/L_y z/L_z T"), default stream formatting.  1D meshes write
+// "x/L_x T" (the reference would divide y = 0 by L_y = 0).  False if the file
+// cannot be written.
+bool write_tempcell(const std::string& path, int n, int dim, const double* centroid, const double* T, double L_x,
+                    double L_y, double L_z);
+
 }  // namespace sbte

@@ -80,4 +80,17 @@ void sbte_bcs(const sbte_problem* p, int* index, int* type, double* T) {
 
 int sbte_upload(const sbte_problem* p, bte_ctx* ctx) { return sbte::upload(p->P, ctx); }
 
+int sbte_write_tempcell(const char* path, int n, int dim, const double* centroid, const double* T, double L_x,
+                        double L_y, double L_z) {
+    if (!path || n < 0 || (n > 0 && (!centroid || !T))) {
+        g_err = "sbte_write_tempcell: bad arguments";
+        return BTE_ERR_INVALID_ARGUMENT;
+    }
+    if (!sbte::write_tempcell(path, n, dim, centroid, T, L_x, L_y, L_z)) {
+        g_err = std::string("sbte_write_tempcell: cannot write ") + path;
+        return BTE_ERR_INVALID_ARGUMENT;
+    }
+    return BTE_OK;
+}
+
 }  // extern "C"

@@ -60,3 +60,18 @@ def test_bad_inputs_raise(sbte, tmp_path):
     bc.write_text("2 #n\n\n#h\n0 1 301\n1 1 299\n")
     with pytest.raises(sbte.BteError):
         sbte.Problem("100", str(bc), str(band), 4, 8, 1, 300, 1e-8)  # DM must be 2 or 3
+
+
+def test_tempcell_writer_format(sbte, tmp_path):
+    """The reference's field dump (src/StaticBTESolver.cpp:818-831): x/L_x y/L_y [z/L_z] T."""
+    cen = np.array([[0.5e-8, 0.25e-8, 0.0], [1e-8, 2e-9, 0.0]])
+    T = np.array([300.5, 299.123456789])
+    f2 = tmp_path / "t2.dat"
+    sbte.write_tempcell(f2, cen, T, 2, (1e-8, 1e-8, 0.0))
+    assert f2.read_text() == "0.5 0.25 300.5\n1 0.2 299.123\n"
+    cen3 = np.array([[1e-8, 5e-9, 2.5e-9]])
+    f3 = tmp_path / "t3.dat"
+    sbte.write_tempcell(f3, cen3, [301.0], 3, (1e-8, 1e-8, 1e-8))
+    assert f3.read_text() == "1 0.5 0.25 301\n"
+    with pytest.raises(sbte.BteError):
+        sbte.write_tempcell(tmp_path / "no" / "such" / "dir.dat", cen, T, 2, (1e-8, 1e-8, 0.0))

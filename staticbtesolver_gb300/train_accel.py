@@ -62,6 +62,7 @@ def main():
     ap.add_argument("--rounds", type=int, default=3)
     ap.add_argument("--val-problems", type=int, default=12)
     ap.add_argument("--report", default="")
+    ap.add_argument("--no-eval", action="store_true", help="skip the square20k evaluation")
     args = ap.parse_args()
     t0 = time.time()
     specs = learned.training_problems(args.problems, args.seed)
@@ -90,7 +91,7 @@ def main():
     t2 = time.time()
     os.makedirs(os.path.dirname(os.path.abspath(args.out)), exist_ok=True)
     np.save(args.out, p)
-    ev = evaluate(p)
+    ev = None if args.no_eval else evaluate(p)
     rep = dict(problems=info, train_s=t2 - t0, rounds=rounds, scale_selection=totals, eval=ev)
     print(json.dumps(rep))
     if args.report:

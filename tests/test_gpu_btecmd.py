@@ -1,0 +1,36 @@
+"""BTEcmd, the drop-in for the reference's command-line tool: same flags
+(src/BTEMain.cpp:56), the reference's stdout lines, and the --tempcell dump."""
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("form", ["plain", "sweep"])
+def test_btecmd_2dm2dg(sbte, get_case, tmp_path, form):
+    from staticbtesolver_gb300 import _build
+    c = get_case("2DM2DG")
+    out = tmp_path / "Tempcell.dat"
+    cmd = [_build.BTECMD, "-g", c.geo, "-m", c.band, "-b", c.bc, "-d", str(c.DM), "-t", str(c.nt), "-p", str(c.np),
+           "-T", "300", "-I", str(c.max_iter), "-x", repr(c.L[0]), "-y", repr(c.L[1]), "--form", form,
+           "--tempcell", str(out)]
+    r = subprocess.run(cmd, capture_output=True, text=True, timeout=300, cwd=tmp_path)
+    assert r.returncode == 0, r.stderr
+    margins = [float(m) for m in re.findall(r"Iteration #\d+\t Margin per band per cell: (\S+)", r.stdout)]
+    assert len(margins) == int(c.ref["n_iter"])
+    q = {int(k): float(v) for k, v in re.findall(r"heat flux of Boundary Condition #(\d+): (\S+)", r.stdout)}
+    q = np.array([q[k] for k in sorted(q)])
+    big = np.abs(c.ref["q"]) > 1e-3 * np.abs(c.ref["q"]).max()
+    # the printed fluxes carry 6 significant digits
+    np.testing.assert_allclose(q[big], c.ref["q"][big], rtol=6e-6)
+    assert re.search(r"N_cell: \d+", r.stdout) and "Time taken by iteration" in r.stdout
+    rows = np.loadtxt(out)
+    assert rows.shape == (c.ref["T"].size, 3)
+    assert np.abs(rows[:, 2] - c.ref["T"]).max() <= 6e-4  # printed to 6 significant digits
+    assert rows[:, :2].min() >= 0.0 and rows[:, :2].max() <= 1.0  # centroids / L

@@ -8,9 +8,9 @@ a 1e-7 m square, 2 x 100^2 jittered-Delaunay triangles (20,000 cells), DM=2 with
 (seeded synthetic data; the reference ships no such mesh).  One step is one
 complete solve: the source iteration from e = 0 to margin <= 1e-5 with all
 1,280 (band, direction) systems solved on the GPU every outer iteration.
-Default form: upwind sweeps (exact per-direction solves, FP64) with the
-learned outer-iteration accelerator (--accel learned; aitken / none for the
-others).  The line reports the result's relative L2 distance (of T - T_ref) to
+Default form: upwind sweeps (exact per-direction solves, FP64) with Anderson
+mixing of the outer iteration (depth 8; --accel learned / aitken / none for
+the others, all reported in the line).  The line reports the result's relative L2 distance (of T - T_ref) to
 the field converged to margin 1e-10, the same form without the accelerator,
 and the plain FP64 BiCGSTAB and mixed FP32/FP64 forms scaled from a few
 outer iterations to the unaccelerated iteration count.
@@ -67,7 +67,7 @@ def parse_args():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="square20k")
     ap.add_argument("--form", default="sweep", choices=["plain", "mixed", "sweep"])
-    ap.add_argument("--accel", default="learned", choices=["none", "aitken", "learned"],
+    ap.add_argument("--accel", default="anderson", choices=["none", "aitken", "learned", "anderson"],
                     help="outer-iteration accelerator of the timed solve (the plain iteration still runs to margin 1e-5)")
     ap.add_argument("--plain-iters", type=int, default=3,
                     help="outer iterations of the plain FP64 and mixed BiCGSTAB forms timed for the comparison")
@@ -244,10 +244,12 @@ def run_ours(args, rank, world, local):
         ctx = S.Context(local).load(prob)
         solve_kw = dict(max_iter=args.max_iter, tol=1e-5, form=form, inner_tol=1e-9, inner_maxit=1000)
         mlp = None
-        if args.accel != "none":
-            from staticbtesolver_gb300 import learned
+        from staticbtesolver_gb300 import learned
 
-            solve_kw.update(accel=1 if args.accel == "learned" else 2, accel_every=learned.EVERY)
+        accel_cfg = {"none": (0, 8), "learned": (1, learned.EVERY), "aitken": (2, 8), "anderson": (3, 8)}
+        if args.accel != "none":
+            a, every = accel_cfg[args.accel]
+            solve_kw.update(accel=a, accel_every=every)
             if args.accel == "learned":
                 mlp = learned.load()
                 ctx.set_mlp(mlp)
@@ -307,15 +309,12 @@ def run_ours(args, rank, world, local):
                     "rel_l2_vs_converged": rel(ctx.temperature())}
         n_plain_outer = rep_b.n_iter  # the reference's iteration count (same recurrence, parity-tested)
         other = {}
-        from staticbtesolver_gb300 import learned as _learned
-        if mlp is None and os.path.exists(_learned.WEIGHTS):
-            ctx.set_mlp(_learned.load())
-        for name, akw in ((f"aitken_every{_learned.EVERY}", dict(accel=2, accel_every=_learned.EVERY)),
-                          ("aitken_every8", dict(accel=2, accel_every=8)),
-                          (f"learned_every{_learned.EVERY}", dict(accel=1, accel_every=_learned.EVERY))):
-            if akw["accel"] == solve_kw.get("accel") and akw["accel_every"] == solve_kw.get("accel_every"):
-                continue
-            if akw["accel"] == 1 and not os.path.exists(_learned.WEIGHTS):
+        if mlp is None and os.path.exists(learned.WEIGHTS):
+            ctx.set_mlp(learned.load())
+        for name in ("learned", "aitken", "anderson"):
+            a, every = accel_cfg[name]
+            akw = dict(accel=a, accel_every=every)
+            if name == args.accel or (a == 1 and not os.path.exists(learned.WEIGHTS)):
                 continue
             ctx.solve(**dict(solve_kw, **akw))
             st_o, rep_o = ctx.solve(**dict(solve_kw, **akw))
@@ -327,7 +326,7 @@ def run_ours(args, rank, world, local):
         # the outer-iteration count of the solve (the mixed form's warm start
         # helps more in later iterations, so its scaled time is an upper bound)
         def compare(fm):
-            pkw = dict(solve_kw, form=fm, max_iter=args.plain_iters)
+            pkw = dict(solve_kw, form=fm, max_iter=args.plain_iters, accel=0)
             ctx.solve(**pkw)  # warm
             st_p, rep_p = ctx.solve(**pkw)
             per_outer = rep_p.ms_total / 1e3 / rep_p.n_iter

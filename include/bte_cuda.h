@@ -74,9 +74,11 @@ typedef struct bte_options {
     void* user;
     int profile;          /* nonzero: time every inner-solve kernel with CUDA events
                              (bte_get_kernel_stats); adds event records between launches */
-    int accel;            /* outer-iteration extrapolation: 0 none (the reference), 1 learned
-                             (the MLP set by bte_set_mlp), 2 Aitken per cell (non-learned) */
-    int accel_every;      /* outer iterations between extrapolations (>= 4) */
+    int accel;            /* outer-iteration acceleration: 0 none (the reference), 1 learned
+                             (the MLP set by bte_set_mlp), 2 Aitken per cell (non-learned),
+                             3 Anderson mixing of T (non-learned) */
+    int accel_every;      /* 1, 2: outer iterations between extrapolations (>= 4);
+                             3: Anderson depth (1..8) */
     int keep_history;     /* nonzero: keep T after every outer iteration (bte_get_history) */
 } bte_options;
 
@@ -179,6 +181,15 @@ bte_status bte_get_margins(bte_ctx* ctx, double* margins, int cap, int* n);
  * no more.  Parameters: FP32,
  * bte_mlp_param_count() values, W1[8][128] b1 W2[128][128] b2 W3[128][128] b3
  * W4[128][1] b4. */
+/* accel = 3 (Anderson mixing, no counterpart in the reference): the outer
+ * iteration is a fixed-point map T -> G(T).  With the last accel_every + 1
+ * pairs (g_i = G(x_i), f_i = g_i - x_i) the next iteration starts from
+ * T = sum_i alpha_i g_i, alpha minimising ||sum_i alpha_i f_i||_2 subject to
+ * sum_i alpha_i = 1 (Gram matrix on the GPU in a fixed order, the small system
+ * on the host); the history restarts when the margin grows tenfold or a weight
+ * exceeds 1e3.  The wall intensities the next sweep reads (diffuse, specular)
+ * are those of the last sweep.  The plain iteration's margin still decides
+ * convergence. */
 int bte_mlp_param_count(void);
 bte_status bte_set_mlp(bte_ctx* ctx, const float* params);
 /* Cell centroids [n_cell][3] (used only for the accelerator's features). */

@@ -117,7 +117,9 @@ struct bte_ctx {
     long long plan_levels = 0;
     DevBuf p_cell, p_dg, p_vo, p_nb, p_fc, p_lvl, p_lvl_off, p_part, p_bad, p_invd, d_spart, p_bidx;
     DevBuf d_bcell, d_bidx, d_bsum;
-    DevBuf d_snap_e, d_snap_T, d_snap_ebar;  // accelerator: state before the last jump  // cells with boundary faces, cell -> row, boundary rhs per (system, row)
+    DevBuf d_snap_e, d_snap_T, d_snap_ebar;  // accelerator: state before the last jump
+    DevBuf d_aa_x, d_aa_g, d_aa_f, d_aa_part, d_aa_gram, d_aa_slot;  // Anderson mixing
+    double aa_prev_margin = 0.0;  // cells with boundary faces, cell -> row, boundary rhs per (system, row)
     int nbcell = 0;
     // sweep launch shape (bands per block, threads per block) picked by timing
     // the candidates on the first sweep of a plan
@@ -1031,6 +1033,103 @@ static bte_status solve_batch_sweep(bte_ctx* ctx, int b0, int nbb, const bte_opt
     return BTE_OK;
 }
 
+// One Anderson step after outer iteration it (it >= 1): store (g, f) of this
+// iteration, form the Gram matrix of the stored f, solve for alpha and set
+// T = sum alpha_i g_i (and ebar).  The history restarts when the margin grew
+// tenfold or the weights blow up.
+static bte_status anderson_step(bte_ctx* ctx, int slots, int& count, int& next, std::vector<int>& order, double m,
+                                bte_report& rep) {
+    namespace M = bte::mlp;
+    cudaStream_t st = ctx->stream;
+    const int n = ctx->n;
+    const size_t Np = ctx->Np;
+    if (count > 0 && m > 10.0 * ctx->aa_prev_margin) {  // diverging: keep only this iteration
+        count = 0;
+        order.clear();
+    }
+    ctx->aa_prev_margin = m;
+    const int slot = next;
+    next = (next + 1) % slots;
+    if (count == slots) order.erase(order.begin());
+    else ++count;
+    order.push_back(slot);
+    BTE_LAUNCH(KK_REDUCE, -1, 4.0 * n * 8.0, 0,
+               M::k_aa_store<<<(n + 255) / 256, 256, 0, st>>>(ctx->d_T.as<double>(), ctx->d_aa_x.as<double>(), n,
+                                                             ctx->d_aa_g.as<double>() + (size_t)slot * Np,
+                                                             ctx->d_aa_f.as<double>() + (size_t)slot * Np));
+    const int k = count;
+    if (k < 2) return BTE_OK;  // nothing to mix yet
+    int h_slot[M::AA_MAX] = {};
+    for (int i = 0; i < k; ++i) h_slot[i] = order[i];
+    BTE_CUDA(cudaMemcpyAsync(ctx->d_aa_slot.p, h_slot, sizeof(h_slot), cudaMemcpyHostToDevice, st));
+    const int nblk = (n + M::AA_THREADS - 1) / M::AA_THREADS;
+    const int npairs = M::AA_MAX * (M::AA_MAX + 1) / 2;
+    BTE_LAUNCH(KK_REDUCE, -1, (double)k * n * 8.0, 0,
+               M::k_aa_gram<<<nblk, M::AA_THREADS, 0, st>>>(ctx->d_aa_f.as<double>(), Np, n, k,
+                                                           ctx->d_aa_slot.as<int>(), ctx->d_aa_part.as<double>()));
+    M::k_aa_gram_final<<<1, 64, 0, st>>>(ctx->d_aa_part.as<double>(), nblk, ctx->d_aa_gram.as<double>());
+    BTE_LAUNCHED();
+    double h_gram[M::AA_MAX * (M::AA_MAX + 1) / 2];
+    BTE_CUDA(cudaMemcpyAsync(h_gram, ctx->d_aa_gram.p, sizeof(double) * npairs, cudaMemcpyDeviceToHost, st));
+    BTE_CUDA(cudaStreamSynchronize(st));
+    // G alpha' = 1 (Tikhonov-regularised), alpha = alpha' / sum alpha'
+    double G[M::AA_MAX][M::AA_MAX + 1];
+    double dmax = 0.0;
+    for (int i = 0, pr = 0; i < M::AA_MAX; ++i)
+        for (int j = i; j < M::AA_MAX; ++j, ++pr)
+            if (i < k && j < k) {
+                G[i][j] = G[j][i] = h_gram[pr];
+                if (i == j) dmax = std::max(dmax, h_gram[pr]);
+            }
+    if (!(dmax > 0.0) || !std::isfinite(dmax)) return BTE_OK;
+    for (int i = 0; i < k; ++i) {
+        G[i][i] += 1e-12 * dmax;
+        G[i][k] = 1.0;
+    }
+    for (int c = 0; c < k; ++c) {  // Gaussian elimination with partial pivoting
+        int piv = c;
+        for (int r = c + 1; r < k; ++r)
+            if (std::fabs(G[r][c]) > std::fabs(G[piv][c])) piv = r;
+        if (piv != c)
+            for (int j = 0; j <= k; ++j) std::swap(G[c][j], G[piv][j]);
+        if (G[c][c] == 0.0) return BTE_OK;
+        for (int r = c + 1; r < k; ++r) {
+            const double f = G[r][c] / G[c][c];
+            for (int j = c; j <= k; ++j) G[r][j] -= f * G[c][j];
+        }
+    }
+    double a[M::AA_MAX], sum = 0.0;
+    for (int r = k - 1; r >= 0; --r) {
+        double v = G[r][k];
+        for (int j = r + 1; j < k; ++j) v -= G[r][j] * a[j];
+        a[r] = v / G[r][r];
+    }
+    for (int i = 0; i < k; ++i) sum += a[i];
+    double amax = 0.0;
+    for (int i = 0; i < k; ++i) {
+        a[i] /= sum;
+        amax = std::max(amax, std::fabs(a[i]));
+    }
+    if (!std::isfinite(amax) || amax > 1e3) {  // ill-conditioned history: restart from this iteration
+        order.assign(1, slot);
+        count = 1;
+        return BTE_OK;
+    }
+    M::AaMix mx{};
+    mx.k = k;
+    for (int i = 0; i < k; ++i) {
+        mx.slot[i] = h_slot[i];
+        mx.alpha[i] = a[i];
+    }
+    BTE_LAUNCH(KK_REDUCE, -1, ((double)k + 1 + ctx->n_band) * n * 8.0, 0,
+               M::k_aa_mix<<<(n + 255) / 256, 256, 0, st>>>(ctx->d_aa_g.as<double>(), Np, n, mx,
+                                                           ctx->d_Cb.as<double>(), ctx->n_band, ctx->solid_angle,
+                                                           ctx->T_ref, ctx->d_T.as<double>(),
+                                                           ctx->d_ebar.as<double>()));
+    ++rep.accel_steps;
+    return BTE_OK;
+}
+
 extern "C" bte_status bte_solve(bte_ctx* ctx, const bte_options* opts, bte_report* report) {
     if (!ctx) return BTE_ERR_INVALID_ARGUMENT;
     if (!(ctx->has_geom && ctx->has_quad && ctx->has_bands && ctx->has_bcs))
@@ -1088,7 +1187,23 @@ extern "C" bte_status bte_solve(bte_ctx* ctx, const bte_options* opts, bte_repor
     int accel_last = -1;
     double accel_margin = 0.0;
     bte::mlp::FeatureGeom fg{};
-    if (o.accel) {
+    if (o.accel < 0 || o.accel > 3) return fail(ctx, BTE_ERR_INVALID_ARGUMENT, "bte_solve: accel must be 0..3");
+    // Anderson mixing (accel = 3): depth m = accel_every, slots m + 1
+    const int aa_slots = o.accel == 3 ? o.accel_every + 1 : 0;
+    int aa_count = 0, aa_next = 0;  // stored pairs, next slot
+    std::vector<int> aa_order;      // stored slots, oldest first
+    if (o.accel == 3) {
+        if (o.accel_every < 1 || aa_slots > bte::mlp::AA_MAX)
+            return fail(ctx, BTE_ERR_INVALID_ARGUMENT, "bte_solve: Anderson depth (accel_every) must be 1..8");
+        const int nblk = (ctx->n + bte::mlp::AA_THREADS - 1) / bte::mlp::AA_THREADS;
+        BTE_CUDA(ctx->d_aa_x.alloc(sizeof(double) * Np));
+        BTE_CUDA(ctx->d_aa_g.alloc(sizeof(double) * aa_slots * Np));
+        BTE_CUDA(ctx->d_aa_f.alloc(sizeof(double) * aa_slots * Np));
+        BTE_CUDA(ctx->d_aa_part.alloc(sizeof(double) * bte::mlp::AA_MAX * (bte::mlp::AA_MAX + 1) / 2 * nblk));
+        BTE_CUDA(ctx->d_aa_gram.alloc(sizeof(double) * bte::mlp::AA_MAX * (bte::mlp::AA_MAX + 1) / 2));
+        BTE_CUDA(ctx->d_aa_slot.alloc(sizeof(int) * bte::mlp::AA_MAX));
+    }
+    if (o.accel == 1 || o.accel == 2) {
         if (o.accel_every < 4) return fail(ctx, BTE_ERR_INVALID_ARGUMENT, "bte_solve: accel_every must be >= 4");
         if (o.accel == 1 && !ctx->has_mlp) return fail(ctx, BTE_ERR_STATE, "bte_solve: accel = 1 needs bte_set_mlp");
         if ((int)ctx->centroid.size() != 3 * ctx->n)
@@ -1121,6 +1236,8 @@ extern "C" bte_status bte_solve(bte_ctx* ctx, const bte_options* opts, bte_repor
     for (int it = 0; it < o.max_iter; ++it) {
         std::swap(ctx->e_curr, ctx->e_prev);
         BTE_CUDA(cudaEventRecord(ev[0], st));
+        if (aa_slots && it > 0)  // the field this iteration starts from (iteration 0 starts from T_ref)
+            BTE_CUDA(cudaMemcpyAsync(ctx->d_aa_x.p, ctx->d_T.p, sizeof(double) * ctx->n, cudaMemcpyDeviceToDevice, st));
         if (ctx->ndiff > 0) {
             const int nt = ctx->ndiff * NB;
             BTE_LAUNCH(KK_DIFFUSE, -1, (double)nt * (ND + 1) * 8.0, 0,
@@ -1164,7 +1281,7 @@ extern "C" bte_status bte_solve(bte_ctx* ctx, const bte_options* opts, bte_repor
         if (ctx->profile) prof_resolve(ctx, nullptr, 0);
         const double m = ctx->h_pinned[0];
         // the last four temperature fields (accelerator) and the history
-        if (o.accel) {
+        if (o.accel == 1 || o.accel == 2) {
             BTE_CUDA(cudaMemcpyAsync(ctx->d_ring.as<double>() + (size_t)(it % 4) * Np, ctx->d_T.p,
                                      sizeof(double) * Np, cudaMemcpyDeviceToDevice, st));
         }
@@ -1203,7 +1320,11 @@ extern "C" bte_status bte_solve(bte_ctx* ctx, const bte_options* opts, bte_repor
         // the margin at the jump (right after a jump the margin rises while the
         // intensities follow the new source, so it is judged once they have);
         // otherwise restore the state before the jump and stop extrapolating
-        if (o.accel && accel_on && accel_last >= 0 && it == accel_last + o.accel_every - 1 &&
+        if (aa_slots && it > 0) {
+            bte_status s = anderson_step(ctx, aa_slots, aa_count, aa_next, aa_order, m, rep);
+            if (s != BTE_OK) return s;
+        }
+        if ((o.accel == 1 || o.accel == 2) && accel_on && accel_last >= 0 && it == accel_last + o.accel_every - 1 &&
             !(m < accel_margin)) {
             accel_on = false;
             const size_t ne = (size_t)NB * ND * Np;
@@ -1213,7 +1334,8 @@ extern "C" bte_status bte_solve(bte_ctx* ctx, const bte_options* opts, bte_repor
                                      cudaMemcpyDeviceToDevice, st));
             ++rep.accel_reverts;
         }
-        if (o.accel && accel_on && it >= 3 && (accel_last < 0 || it - accel_last >= o.accel_every)) {
+        if ((o.accel == 1 || o.accel == 2) && accel_on && it >= 3 &&
+            (accel_last < 0 || it - accel_last >= o.accel_every)) {
             const int n = ctx->n;
             const int s0 = it % 4, s1 = (it + 3) % 4, s2 = (it + 2) % 4, s3 = (it + 1) % 4;
             BTE_CUDA(cudaMemcpyAsync(ctx->d_snap_e.p, ctx->e_curr, sizeof(double) * (size_t)NB * ND * Np,
@@ -1239,6 +1361,15 @@ extern "C" bte_status bte_solve(bte_ctx* ctx, const bte_options* opts, bte_repor
             accel_last = it;
             accel_margin = m;
             ++rep.accel_steps;
+        }
+        // the accelerator's kernels and copies run after ev[3]: time them too
+        if (o.accel) {
+            BTE_CUDA(cudaEventRecord(ev[4], st));
+            BTE_CUDA(cudaEventSynchronize(ev[4]));
+            float t34 = 0;
+            cudaEventElapsedTime(&t34, ev[3], ev[4]);
+            rep.ms_reduce += t34;
+            rep.ms_total += t34;
         }
     }
     if (o.max_iter == 0) result = BTE_OK;

@@ -488,5 +488,80 @@ __global__ void k_accel_apply(const double* __restrict__ ring, int s0, int s1, i
     for (int b = 0; b < n_band; ++b) ebar[(size_t)b * Np + c] = Cb[b] / solid_angle * (Tn - T_ref);
 }
 
+// ---------------------------------------------------------------------------
+// Anderson mixing of the outer iteration (accel = 3).  The source iteration
+// is a fixed-point map T -> G(T) (one sweep of every system and the
+// reductions); with the last k pairs (g_i = G(x_i), f_i = g_i - x_i) the next
+// input is T = sum_i alpha_i g_i, alpha minimising ||sum_i alpha_i f_i|| with
+// sum_i alpha_i = 1 (the host solves the k x k system from the Gram matrix).
+
+// g[slot] = T, f[slot] = T - x (x = the field the iteration started from).
+__global__ void k_aa_store(const double* __restrict__ T, const double* __restrict__ x, int n, double* g, double* f) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    const double t = T[c];
+    g[c] = t;
+    f[c] = t - x[c];
+}
+
+constexpr int AA_MAX = 9;  // slots (depth + 1)
+constexpr int AA_THREADS = 256;
+
+// Partial Gram sums f_i . f_j (i <= j < k, slots in `slot`) over this block's
+// cells, in a fixed order: part[pair][block].
+__global__ void __launch_bounds__(AA_THREADS) k_aa_gram(const double* __restrict__ f, size_t Np, int n, int k,
+                                                        const int* __restrict__ slot, double* part) {
+    __shared__ double sm[AA_MAX * (AA_MAX + 1) / 2][AA_THREADS / 32];
+    const int c = blockIdx.x * AA_THREADS + threadIdx.x;
+    double v[AA_MAX];
+#pragma unroll
+    for (int i = 0; i < AA_MAX; ++i) v[i] = (i < k && c < n) ? f[(size_t)slot[i] * Np + c] : 0.0;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int pr = 0;
+#pragma unroll
+    for (int i = 0; i < AA_MAX; ++i)
+#pragma unroll
+        for (int j = i; j < AA_MAX; ++j, ++pr) {
+            double a = v[i] * v[j];  // 0 for slots >= k
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+            if (lane == 0) sm[pr][warp] = a;
+        }
+    __syncthreads();
+    const int npairs = AA_MAX * (AA_MAX + 1) / 2;
+    for (int q = threadIdx.x; q < npairs; q += AA_THREADS) {
+        double s = 0.0;
+        for (int w = 0; w < AA_THREADS / 32; ++w) s += sm[q][w];
+        part[(size_t)q * gridDim.x + blockIdx.x] = s;
+    }
+}
+
+// One block: gram[pair] = sum over blocks of the partials, in block order.
+__global__ void k_aa_gram_final(const double* __restrict__ part, int nblk, double* gram) {
+    const int q = threadIdx.x;
+    if (q >= AA_MAX * (AA_MAX + 1) / 2) return;
+    double s = 0.0;
+    for (int b = 0; b < nblk; ++b) s += part[(size_t)q * nblk + b];
+    gram[q] = s;
+}
+
+struct AaMix {
+    int slot[AA_MAX];
+    double alpha[AA_MAX];
+    int k;
+};
+
+// T = sum_i alpha_i g_i; ebar[b][c] = C_b / Omega_tot (T - T_ref).
+__global__ void k_aa_mix(const double* __restrict__ g, size_t Np, int n, AaMix mx, const double* __restrict__ Cb,
+                         int n_band, double solid_angle, double T_ref, double* __restrict__ T,
+                         double* __restrict__ ebar) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    double t = 0.0;
+    for (int i = 0; i < mx.k; ++i) t = fma(mx.alpha[i], g[(size_t)mx.slot[i] * Np + c], t);
+    T[c] = t;
+    for (int b = 0; b < n_band; ++b) ebar[(size_t)b * Np + c] = Cb[b] / solid_angle * (t - T_ref);
+}
+
 }  // namespace mlp
 }  // namespace bte

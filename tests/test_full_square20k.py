@@ -72,15 +72,16 @@ def test_sweep_matches_full_oracle(sbte, full, problem):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("accel,every", [("aitken", 8), ("learned", None)])
+@pytest.mark.parametrize("accel,every", [("aitken", 8), ("learned", None), ("anderson", 8)])
 def test_accelerator_gain_at_full_size(sbte, full, problem, converged, accel, every):
     """Fewer outer iterations than the plain iteration (198) to the same margin, and a
     field within relative L2 1e-5 of the oracle's.  (Aitken is run at its better
-    interval: every 6 outer iterations it ends 1.3e-5 from the converged field.)"""
+    interval: every 6 outer iterations it ends 1.3e-5 from the converged field.
+    Anderson mixing, depth 8, takes 47.)"""
     from staticbtesolver_gb300 import learned
     mlp = learned.load() if accel == "learned" else None
-    res = _solve(sbte, problem, mlp=mlp, form=sbte.FORM_SWEEP, accel=1 if accel == "learned" else 2,
-                 accel_every=every or learned.EVERY)
+    code = {"learned": 1, "aitken": 2, "anderson": 3}[accel]
+    res = _solve(sbte, problem, mlp=mlp, form=sbte.FORM_SWEEP, accel=code, accel_every=every or learned.EVERY)
     err = rel_l2(res.T - 300.0, full["T"] - 300.0)
     err_conv = rel_l2(res.T - 300.0, converged - 300.0)
     print(accel, "n_iter", res.report["n_iter"], "jumps", res.report["accel_steps"], "reverts",
@@ -90,3 +91,7 @@ def test_accelerator_gain_at_full_size(sbte, full, problem, converged, accel, ev
     assert res.report["n_iter"] < 0.75 * int(full["n_iter"])  # the gain over the plain iteration
     assert err < 1e-5
     _q_close(res.q, full["q"], 1e-4)
+    if accel == "anderson":
+        assert res.report["n_iter"] < 0.3 * int(full["n_iter"])  # 47 outer iterations here
+        again = _solve(sbte, problem, form=sbte.FORM_SWEEP, accel=3, accel_every=8)
+        np.testing.assert_array_equal(again.T, res.T)  # fixed-order Gram sums: bitwise reproducible

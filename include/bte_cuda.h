@@ -182,14 +182,15 @@ bte_status bte_get_margins(bte_ctx* ctx, double* margins, int cap, int* n);
  * bte_mlp_param_count() values, W1[8][128] b1 W2[128][128] b2 W3[128][128] b3
  * W4[128][1] b4. */
 /* accel = 3 (Anderson mixing, no counterpart in the reference): the outer
- * iteration is a fixed-point map T -> G(T).  With the last accel_every + 1
- * pairs (g_i = G(x_i), f_i = g_i - x_i) the next iteration starts from
- * T = sum_i alpha_i g_i, alpha minimising ||sum_i alpha_i f_i||_2 subject to
- * sum_i alpha_i = 1 (Gram matrix on the GPU in a fixed order, the small system
- * on the host); the history restarts when the margin grows tenfold or a weight
- * exceeds 1e3.  The wall intensities the next sweep reads (diffuse, specular)
- * are those of the last sweep.  The plain iteration's margin still decides
- * convergence. */
+ * iteration is a fixed-point map x -> G(x) on its state x = (T, the
+ * intensities at the cells with boundary faces, scaled by Omega_tot / C_b),
+ * which is all the next sweep reads besides constants.  With the last
+ * accel_every + 1 pairs (g_i = G(x_i), f_i = g_i - x_i) the next iteration
+ * starts from sum_i alpha_i g_i, alpha minimising ||sum_i alpha_i f_i||_2
+ * subject to sum_i alpha_i = 1 (Gram matrix on the GPU in a fixed order, the
+ * small system on the host); the history restarts when the margin grows
+ * tenfold or a weight exceeds 1e3.  The plain iteration's margin still
+ * decides convergence. */
 int bte_mlp_param_count(void);
 bte_status bte_set_mlp(bte_ctx* ctx, const float* params);
 /* Cell centroids [n_cell][3] (used only for the accelerator's features). */

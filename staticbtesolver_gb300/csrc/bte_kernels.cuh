@@ -88,19 +88,26 @@ struct BicgState {
     double* omega;    // [S]
     double* nrmr;     // [S] last ||r||
     double* nrm0;     // [S] ||b||
+    double* bestr;    // [2][S] smallest ||r|| so far (used when BicgVecs::xb is set)
     double* part;     // [7][S][nchunk] partial dot products
     int* active;      // [maxit + 2] number of active systems at each iteration
     int S, nchunk;
     double tol;
     int maxit;
+    int cycles = 1;   // with BicgVecs::xb: the iteration limit is cycles x maxit
     __device__ double* P(int kind, int y) const { return part + ((size_t)kind * S + y) * nchunk; }
 };
 enum { PK_RR0 = 0, PK_RR1 = 1, PK_RWR0 = 2, PK_RWR1 = 3, PK_RWQ = 4, PK_TS = 5, PK_TT = 6 };
 
+// xb (optional, nullptr to follow the reference exactly): the iterate with the
+// smallest residual norm so far, returned instead of the last one when the
+// iteration limit (BicgState::cycles x maxit) is reached or the residual stops
+// being finite.
 template <typename T>
 struct BicgVecs {
     T* r; T* rw; T* p; T* ph; T* q; T* z; T* t; const T* b; T* invD;
     size_t Np;
+    T* xb = nullptr;
 };
 
 // Matrix-free upwind operator of all (band, direction) systems of a batch.
@@ -260,6 +267,7 @@ __global__ void __launch_bounds__(THREADS) k_bicg_init(Op op, BicgVecs<T> v, Bic
         v.r[o + c] = bb; v.rw[o + c] = bb; v.q[o + c] = 0;
         if constexpr (sizeof(T) == sizeof(float)) v.p[o + c] = 0;
         else v.p[o + c] = bb;
+        if (v.xb) v.xb[o + c] = 0;
         x[c] = 0;
         acc_t = fmat(bb, bb, acc_t);
     }
@@ -279,6 +287,7 @@ __global__ void k_bicg_init_scalars(BicgState st, const int* skip) {
     double n0 = sqrt(sum_parts_serial(st.P(PK_RR0, y), st.nchunk));
     st.nrm0[y] = n0;
     st.nrmr[y] = n0;
+    if (st.bestr) st.bestr[y] = st.bestr[st.S + y] = n0;  // x0 = 0 has ||r|| = ||b||
     st.rho[y] = 1.0; st.rho[st.S + y] = 1.0;
     st.alpha[y] = 1.0; st.omega[y] = 1.0;
     st.done[y] = (skip && skip[y]) ? 4 : 0;
@@ -318,6 +327,7 @@ __global__ void __launch_bounds__(THREADS) k_bicg_p(Op op, BicgVecs<T> v, BicgSt
     const int par = i & 1, pp = par ^ 1;
     const bool lead = blockIdx.x == 0 && threadIdx.x == 0;
     double nr;
+    bool fresh = false;  // nr is the residual norm of the current x
     if (i > 1 && !(st.flagA[pp * st.S + y] | st.flagB[pp * st.S + y])) {
         nr = sqrt(sum_parts(st.P(pp ? PK_RR1 : PK_RR0, y), st.nchunk));
         if (nr / st.nrm0[y] < st.tol) {  // src/bicgstab.hpp:295
@@ -325,10 +335,26 @@ __global__ void __launch_bounds__(THREADS) k_bicg_p(Op op, BicgVecs<T> v, BicgSt
             return;
         }
         if (lead) st.nrmr[y] = nr;
+        fresh = true;
     } else {
         nr = st.nrmr[y];
     }
-    if (i > st.maxit) {
+    const size_t ox = (size_t)y * v.Np;
+    T* __restrict__ xcur = op.x_of(y);
+    if (v.xb) {
+        const double best = st.bestr[pp * st.S + y];
+        const bool improved = fresh && nr < best;  // false for NaN
+        const double best_now = improved ? nr : best;
+        if (lead) st.bestr[par * st.S + y] = best_now;
+        if (i > st.maxit * st.cycles || !(nr <= 1.0e300)) {  // limit reached or the iteration blew up
+            if (!improved)
+                BTE_CELL_LOOP(c) { xcur[c] = v.xb[ox + c]; }
+            if (lead) { st.done[y] = 3; st.iters[y] = i - 1; }
+            return;
+        }
+        if (improved)
+            BTE_CELL_LOOP(c) { v.xb[ox + c] = xcur[c]; }
+    } else if (i > st.maxit) {
         if (lead) { st.done[y] = 3; st.iters[y] = st.maxit; }
         return;
     }

@@ -490,49 +490,93 @@ __global__ void k_accel_apply(const double* __restrict__ ring, int s0, int s1, i
 
 // ---------------------------------------------------------------------------
 // Anderson mixing of the outer iteration (accel = 3).  The source iteration
-// is a fixed-point map T -> G(T) (one sweep of every system and the
-// reductions); with the last k pairs (g_i = G(x_i), f_i = g_i - x_i) the next
-// input is T = sum_i alpha_i g_i, alpha minimising ||sum_i alpha_i f_i|| with
+// is a fixed-point map on its state -- the cell temperatures T (which fix the
+// equilibrium source) and the intensities at the cells with boundary faces
+// (which the diffuse and specular walls reflect).  With the last k pairs
+// (g_i = G(x_i), f_i = g_i - x_i) of state vectors the next iteration starts
+// from sum_i alpha_i g_i, alpha minimising ||sum_i alpha_i f_i|| with
 // sum_i alpha_i = 1 (the host solves the k x k system from the Gram matrix).
+// State vector: [T (n) | e[b][d][boundary cell] * Omega_tot / C_b], the
+// intensities scaled to temperature units so both parts weigh alike.
 
-// g[slot] = T, f[slot] = T - x (x = the field the iteration started from).
-__global__ void k_aa_store(const double* __restrict__ T, const double* __restrict__ x, int n, double* g, double* f) {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= n) return;
-    const double t = T[c];
-    g[c] = t;
-    f[c] = t - x[c];
+struct AaState {
+    const int* bcell;  // cells with boundary faces
+    int n, nbcell, n_band, n_dir;
+    size_t Np;
+    const double* Cb;
+    double solid_angle;
+    __device__ __forceinline__ size_t len() const { return (size_t)n + (size_t)n_band * n_dir * nbcell; }
+    // e index and scale of state entry j >= n
+    __device__ __forceinline__ size_t e_index(size_t j, double& scale) const {
+        const size_t jj = j - n;
+        const int i = (int)(jj % nbcell);
+        const size_t bd = jj / nbcell;
+        const int b = (int)(bd / n_dir), d = (int)(bd % n_dir);
+        scale = solid_angle / Cb[b];
+        return ((size_t)b * n_dir + d) * Np + bcell[i];
+    }
+};
+
+// out = the state (T, e at the boundary cells).
+__global__ void k_aa_gather(AaState a, const double* __restrict__ T, const double* __restrict__ e, double* out) {
+    const size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= a.len()) return;
+    if (j < (size_t)a.n) {
+        out[j] = T[j];
+    } else {
+        double sc;
+        const size_t k = a.e_index(j, sc);
+        out[j] = e[k] * sc;
+    }
+}
+
+// f = g - x over the state.
+__global__ void k_aa_store(const double* __restrict__ g, const double* __restrict__ x, size_t len, double* f) {
+    const size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < len) f[j] = g[j] - x[j];
 }
 
 constexpr int AA_MAX = 9;  // slots (depth + 1)
 constexpr int AA_THREADS = 256;
 
-// Partial Gram sums f_i . f_j (i <= j < k, slots in `slot`) over this block's
-// cells, in a fixed order: part[pair][block].
-__global__ void __launch_bounds__(AA_THREADS) k_aa_gram(const double* __restrict__ f, size_t Np, int n, int k,
-                                                        const int* __restrict__ slot, double* part) {
-    __shared__ double sm[AA_MAX * (AA_MAX + 1) / 2][AA_THREADS / 32];
-    const int c = blockIdx.x * AA_THREADS + threadIdx.x;
-    double v[AA_MAX];
+// Partial Gram sums f_i . f_j (i <= j < k, slots in `slot`): AA_BLOCKS blocks
+// (a constant, so the summation order does not depend on the device), each
+// thread accumulating its grid-stride share of the state, then a fixed-order
+// block reduction per pair: part[pair][block].
+constexpr int AA_BLOCKS = 304;
+__global__ void __launch_bounds__(AA_THREADS) k_aa_gram(const double* __restrict__ f, size_t stride, size_t len,
+                                                        int k, const int* __restrict__ slot, double* part) {
+    constexpr int NP = AA_MAX * (AA_MAX + 1) / 2;
+    __shared__ double sm[AA_THREADS / 32][NP];
+    double acc[NP];
 #pragma unroll
-    for (int i = 0; i < AA_MAX; ++i) v[i] = (i < k && c < n) ? f[(size_t)slot[i] * Np + c] : 0.0;
+    for (int q = 0; q < NP; ++q) acc[q] = 0.0;
+    int sl[AA_MAX];
+#pragma unroll
+    for (int i = 0; i < AA_MAX; ++i) sl[i] = i < k ? slot[i] : 0;
+    for (size_t c = (size_t)blockIdx.x * AA_THREADS + threadIdx.x; c < len; c += (size_t)gridDim.x * AA_THREADS) {
+        double v[AA_MAX];
+#pragma unroll
+        for (int i = 0; i < AA_MAX; ++i) v[i] = i < k ? f[(size_t)sl[i] * stride + c] : 0.0;
+        int q = 0;
+#pragma unroll
+        for (int i = 0; i < AA_MAX; ++i)
+#pragma unroll
+            for (int jj = i; jj < AA_MAX; ++jj, ++q) acc[q] = fma(v[i], v[jj], acc[q]);
+    }
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    int pr = 0;
 #pragma unroll
-    for (int i = 0; i < AA_MAX; ++i)
+    for (int q = 0; q < NP; ++q) {
+        double a = acc[q];
 #pragma unroll
-        for (int j = i; j < AA_MAX; ++j, ++pr) {
-            double a = v[i] * v[j];  // 0 for slots >= k
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
-            if (lane == 0) sm[pr][warp] = a;
-        }
+        for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+        if (lane == 0) sm[warp][q] = a;
+    }
     __syncthreads();
-    const int npairs = AA_MAX * (AA_MAX + 1) / 2;
-    for (int q = threadIdx.x; q < npairs; q += AA_THREADS) {
-        double s = 0.0;
-        for (int w = 0; w < AA_THREADS / 32; ++w) s += sm[q][w];
-        part[(size_t)q * gridDim.x + blockIdx.x] = s;
+    for (int q = threadIdx.x; q < NP; q += AA_THREADS) {
+        double t = 0.0;
+        for (int w = 0; w < AA_THREADS / 32; ++w) t += sm[w][q];
+        part[(size_t)q * gridDim.x + blockIdx.x] = t;
     }
 }
 
@@ -551,16 +595,22 @@ struct AaMix {
     int k;
 };
 
-// T = sum_i alpha_i g_i; ebar[b][c] = C_b / Omega_tot (T - T_ref).
-__global__ void k_aa_mix(const double* __restrict__ g, size_t Np, int n, AaMix mx, const double* __restrict__ Cb,
-                         int n_band, double solid_angle, double T_ref, double* __restrict__ T,
-                         double* __restrict__ ebar) {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= n) return;
+// state = sum_i alpha_i g_i: T and ebar[b][c] = C_b / Omega_tot (T - T_ref), and
+// the boundary-cell intensities written back into e (the next iteration's e_prev).
+__global__ void k_aa_mix(AaState a, const double* __restrict__ g, size_t stride, AaMix mx, double T_ref,
+                         double* __restrict__ T, double* __restrict__ ebar, double* __restrict__ e) {
+    const size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= a.len()) return;
     double t = 0.0;
-    for (int i = 0; i < mx.k; ++i) t = fma(mx.alpha[i], g[(size_t)mx.slot[i] * Np + c], t);
-    T[c] = t;
-    for (int b = 0; b < n_band; ++b) ebar[(size_t)b * Np + c] = Cb[b] / solid_angle * (t - T_ref);
+    for (int i = 0; i < mx.k; ++i) t = fma(mx.alpha[i], g[(size_t)mx.slot[i] * stride + j], t);
+    if (j < (size_t)a.n) {
+        T[j] = t;
+        for (int b = 0; b < a.n_band; ++b) ebar[(size_t)b * a.Np + j] = a.Cb[b] / a.solid_angle * (t - T_ref);
+    } else {
+        double sc;
+        const size_t k = a.e_index(j, sc);
+        e[k] = t / sc;
+    }
 }
 
 }  // namespace mlp

@@ -11,7 +11,7 @@ import pytest
 from conftest import SYNTH_CASES, TESTSH_CASES
 
 
-@pytest.mark.parametrize("name", TESTSH_CASES + ["2Dcase2"] + SYNTH_CASES)
+@pytest.mark.parametrize("name", TESTSH_CASES + ["2Dcase2", "2Dcase5"] + SYNTH_CASES)
 def test_preprocessing_matches_oracle(sbte, oracle_mod, get_case, name):
     c = get_case(name)
     p = sbte.Problem(*c.args())

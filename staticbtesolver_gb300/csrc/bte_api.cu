@@ -804,6 +804,7 @@ static bte_status solve_batch_plain(bte_ctx* ctx, int b0, int nbb, const bte_opt
                             ctx->w_t.as<double>(), ctx->w_b.as<double>(), ctx->w_invD.as<double>(), ctx->Np};
     v.xb = ctx->w_xb.as<double>();  // the best iterate is kept and returned
     bs.cycles = kPlainCycles;
+    bs.track_from = maxit / 2;  // systems converging before that never copy x
     BTE_LAUNCH(KK_INIT, -1, S * N * 7 * w + geo / 2, 0, bte::k_bicg_init<<<grid, bte::THREADS, 0, st>>>(op, v, bs));
     BTE_LAUNCH(KK_INIT, -1, 0, 0, bte::k_bicg_init_scalars<<<(S + 127) / 128, 128, 0, st>>>(bs, nullptr));
     int i = 1;

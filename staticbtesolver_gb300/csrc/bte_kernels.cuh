@@ -95,14 +95,15 @@ struct BicgState {
     double tol;
     int maxit;
     int cycles = 1;   // with BicgVecs::xb: the iteration limit is cycles x maxit
+    int track_from = 0;  // with BicgVecs::xb: iterations before this are not candidates
     __device__ double* P(int kind, int y) const { return part + ((size_t)kind * S + y) * nchunk; }
 };
 enum { PK_RR0 = 0, PK_RR1 = 1, PK_RWR0 = 2, PK_RWR1 = 3, PK_RWQ = 4, PK_TS = 5, PK_TT = 6 };
 
 // xb (optional, nullptr to follow the reference exactly): the iterate with the
-// smallest residual norm so far, returned instead of the last one when the
-// iteration limit (BicgState::cycles x maxit) is reached or the residual stops
-// being finite.
+// smallest residual norm after iteration BicgState::track_from (x = 0 before),
+// returned instead of the last one when the iteration limit (cycles x maxit)
+// is reached or the residual stops being finite.
 template <typename T>
 struct BicgVecs {
     T* r; T* rw; T* p; T* ph; T* q; T* z; T* t; const T* b; T* invD;
@@ -343,7 +344,7 @@ __global__ void __launch_bounds__(THREADS) k_bicg_p(Op op, BicgVecs<T> v, BicgSt
     T* __restrict__ xcur = op.x_of(y);
     if (v.xb) {
         const double best = st.bestr[pp * st.S + y];
-        const bool improved = fresh && nr < best;  // false for NaN
+        const bool improved = fresh && i > st.track_from && nr < best;  // false for NaN
         const double best_now = improved ? nr : best;
         if (lead) st.bestr[par * st.S + y] = best_now;
         if (i > st.maxit * st.cycles || !(nr <= 1.0e300)) {  // limit reached or the iteration blew up

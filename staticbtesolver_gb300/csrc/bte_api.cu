@@ -118,7 +118,7 @@ struct bte_ctx {
     DevBuf p_cell, p_dg, p_vo, p_nb, p_fc, p_lvl, p_lvl_off, p_part, p_bad, p_invd, d_spart, p_bidx;
     DevBuf d_bcell, d_bidx, d_bsum;
     DevBuf d_snap_e, d_snap_T, d_snap_ebar;  // accelerator: state before the last jump
-    DevBuf d_aa_x, d_aa_g, d_aa_f, d_aa_part, d_aa_gram, d_aa_slot;  // Anderson mixing
+    DevBuf d_aa_x, d_aa_g, d_aa_f, d_aa_part, d_aa_gram, d_aa_alpha, d_aa_flag;  // Anderson mixing
     double aa_prev_margin = 0.0;  // cells with boundary faces, cell -> row, boundary rhs per (system, row)
     int nbcell = 0;
     // sweep launch shape (bands per block, threads per block) picked by timing
@@ -1070,7 +1070,6 @@ static bte_status anderson_step(bte_ctx* ctx, int slots, int& count, int& next, 
     namespace M = bte::mlp;
     cudaStream_t st = ctx->stream;
     const int n = ctx->n;
-    const size_t Np = ctx->Np;
     if (count > 0 && m > 10.0 * ctx->aa_prev_margin) {  // diverging: keep only this iteration
         count = 0;
         order.clear();
@@ -1084,79 +1083,28 @@ static bte_status anderson_step(bte_ctx* ctx, int slots, int& count, int& next, 
     const M::AaState as = aa_state(ctx);
     const size_t L = aa_len(ctx);
     const unsigned gl = (unsigned)((L + 255) / 256);
-    BTE_LAUNCH(KK_REDUCE, -1, 5.0 * L * 8.0, 0,
-               M::k_aa_gather<<<gl, 256, 0, st>>>(as, ctx->d_T.as<double>(), ctx->e_curr,
-                                                  ctx->d_aa_g.as<double>() + (size_t)slot * L));
-    M::k_aa_store<<<gl, 256, 0, st>>>(ctx->d_aa_g.as<double>() + (size_t)slot * L, ctx->d_aa_x.as<double>(), L,
-                                      ctx->d_aa_f.as<double>() + (size_t)slot * L);
+    M::AaMix mx{};
+    mx.k = count;
+    for (int i = 0; i < count; ++i) mx.slot[i] = order[i];
+    const int nblk = M::AA_BLOCKS;
+    BTE_LAUNCH(KK_REDUCE, -1, (3.0 + count) * L * 8.0, 0,
+               M::k_aa_push<<<nblk, M::AA_THREADS, 0, st>>>(as, ctx->d_T.as<double>(), ctx->e_curr,
+                                                           ctx->d_aa_x.as<double>(), L, slot, mx,
+                                                           ctx->d_aa_g.as<double>(), ctx->d_aa_f.as<double>(),
+                                                           ctx->d_aa_part.as<double>()));
+    M::k_aa_row<<<1, 32, 0, st>>>(ctx->d_aa_part.as<double>(), nblk, slot, mx, ctx->d_aa_gram.as<double>());
     BTE_LAUNCHED();
     const int k = count;
     if (k < 2) return BTE_OK;  // nothing to mix yet
-    int h_slot[M::AA_MAX] = {};
-    for (int i = 0; i < k; ++i) h_slot[i] = order[i];
-    BTE_CUDA(cudaMemcpyAsync(ctx->d_aa_slot.p, h_slot, sizeof(h_slot), cudaMemcpyHostToDevice, st));
-    const int nblk = M::AA_BLOCKS;
-    const int npairs = M::AA_MAX * (M::AA_MAX + 1) / 2;
-    BTE_LAUNCH(KK_REDUCE, -1, (double)k * L * 8.0, 0,
-               M::k_aa_gram<<<nblk, M::AA_THREADS, 0, st>>>(ctx->d_aa_f.as<double>(), L, L, k,
-                                                           ctx->d_aa_slot.as<int>(), ctx->d_aa_part.as<double>()));
-    M::k_aa_gram_final<<<1, 64, 0, st>>>(ctx->d_aa_part.as<double>(), nblk, ctx->d_aa_gram.as<double>());
+    // the small least-squares system on the device: no host round trip; an
+    // ill-conditioned history sets the flag the host reads with the next margin
+    M::k_aa_solve<<<1, 32, 0, st>>>(ctx->d_aa_gram.as<double>(), mx, ctx->d_aa_alpha.as<double>(),
+                                   ctx->d_aa_flag.as<double>());
     BTE_LAUNCHED();
-    double h_gram[M::AA_MAX * (M::AA_MAX + 1) / 2];
-    BTE_CUDA(cudaMemcpyAsync(h_gram, ctx->d_aa_gram.p, sizeof(double) * npairs, cudaMemcpyDeviceToHost, st));
-    BTE_CUDA(cudaStreamSynchronize(st));
-    // G alpha' = 1 (Tikhonov-regularised), alpha = alpha' / sum alpha'
-    double G[M::AA_MAX][M::AA_MAX + 1];
-    double dmax = 0.0;
-    for (int i = 0, pr = 0; i < M::AA_MAX; ++i)
-        for (int j = i; j < M::AA_MAX; ++j, ++pr)
-            if (i < k && j < k) {
-                G[i][j] = G[j][i] = h_gram[pr];
-                if (i == j) dmax = std::max(dmax, h_gram[pr]);
-            }
-    if (!(dmax > 0.0) || !std::isfinite(dmax)) return BTE_OK;
-    for (int i = 0; i < k; ++i) {
-        G[i][i] += 1e-12 * dmax;
-        G[i][k] = 1.0;
-    }
-    for (int c = 0; c < k; ++c) {  // Gaussian elimination with partial pivoting
-        int piv = c;
-        for (int r = c + 1; r < k; ++r)
-            if (std::fabs(G[r][c]) > std::fabs(G[piv][c])) piv = r;
-        if (piv != c)
-            for (int j = 0; j <= k; ++j) std::swap(G[c][j], G[piv][j]);
-        if (G[c][c] == 0.0) return BTE_OK;
-        for (int r = c + 1; r < k; ++r) {
-            const double f = G[r][c] / G[c][c];
-            for (int j = c; j <= k; ++j) G[r][j] -= f * G[c][j];
-        }
-    }
-    double a[M::AA_MAX], sum = 0.0;
-    for (int r = k - 1; r >= 0; --r) {
-        double v = G[r][k];
-        for (int j = r + 1; j < k; ++j) v -= G[r][j] * a[j];
-        a[r] = v / G[r][r];
-    }
-    for (int i = 0; i < k; ++i) sum += a[i];
-    double amax = 0.0;
-    for (int i = 0; i < k; ++i) {
-        a[i] /= sum;
-        amax = std::max(amax, std::fabs(a[i]));
-    }
-    if (!std::isfinite(amax) || amax > 1e3) {  // ill-conditioned history: restart from this iteration
-        order.assign(1, slot);
-        count = 1;
-        return BTE_OK;
-    }
-    M::AaMix mx{};
-    mx.k = k;
-    for (int i = 0; i < k; ++i) {
-        mx.slot[i] = h_slot[i];
-        mx.alpha[i] = a[i];
-    }
     BTE_LAUNCH(KK_REDUCE, -1, ((double)k + 1) * L * 8.0 + (double)ctx->n_band * n * 8.0, 0,
-               M::k_aa_mix<<<gl, 256, 0, st>>>(as, ctx->d_aa_g.as<double>(), L, mx, ctx->T_ref, ctx->d_T.as<double>(),
-                                                ctx->d_ebar.as<double>(), ctx->e_curr));
+               M::k_aa_mix<<<gl, 256, 0, st>>>(as, ctx->d_aa_g.as<double>(), L, mx, ctx->d_aa_alpha.as<double>(),
+                                                ctx->T_ref, ctx->d_T.as<double>(), ctx->d_ebar.as<double>(),
+                                                ctx->e_curr));
     ++rep.accel_steps;
     return BTE_OK;
 }
@@ -1206,9 +1154,18 @@ extern "C" bte_status bte_solve(bte_ctx* ctx, const bte_options* opts, bte_repor
     ctx->margins.clear();
     double Lr_sum = 0;
     for (int b = 0; b < NB; ++b) Lr_sum += ctx->Lr[b];
-    cudaEvent_t ev[5];
+    cudaEvent_t ev[7];  // [0..3] the phases of an outer iteration, [5..6] the accelerator step after it
     for (auto& e : ev) BTE_CUDA(cudaEventCreate(&e));
-    struct EvGuard { cudaEvent_t* e; ~EvGuard() { for (int k = 0; k < 5; ++k) cudaEventDestroy(e[k]); } } guard{ev};
+    struct EvGuard { cudaEvent_t* e; ~EvGuard() { for (int k = 0; k < 7; ++k) cudaEventDestroy(e[k]); } } guard{ev};
+    bool accel_timed = false;  // ev[5..6] hold an accelerator step not yet added to the report
+    auto add_accel_time = [&]() {
+        if (!accel_timed) return;
+        float t = 0;
+        cudaEventElapsedTime(&t, ev[5], ev[6]);
+        rep.ms_reduce += t;
+        rep.ms_total += t;
+        accel_timed = false;
+    };
     bte_status result = BTE_ERR_NOT_CONVERGED;
     const int nred = (int)(Np / bte::THREADS);
     // the sweep of an acyclic plan sums the margin itself; k_reduce then reads e_curr only
@@ -1231,9 +1188,11 @@ extern "C" bte_status bte_solve(bte_ctx* ctx, const bte_options* opts, bte_repor
         BTE_CUDA(ctx->d_aa_x.alloc(sizeof(double) * L));
         BTE_CUDA(ctx->d_aa_g.alloc(sizeof(double) * aa_slots * L));
         BTE_CUDA(ctx->d_aa_f.alloc(sizeof(double) * aa_slots * L));
-        BTE_CUDA(ctx->d_aa_part.alloc(sizeof(double) * bte::mlp::AA_MAX * (bte::mlp::AA_MAX + 1) / 2 * nblk));
-        BTE_CUDA(ctx->d_aa_gram.alloc(sizeof(double) * bte::mlp::AA_MAX * (bte::mlp::AA_MAX + 1) / 2));
-        BTE_CUDA(ctx->d_aa_slot.alloc(sizeof(int) * bte::mlp::AA_MAX));
+        BTE_CUDA(ctx->d_aa_part.alloc(sizeof(double) * bte::mlp::AA_MAX * nblk));
+        BTE_CUDA(ctx->d_aa_gram.alloc(sizeof(double) * bte::mlp::AA_MAX * bte::mlp::AA_MAX));
+        BTE_CUDA(ctx->d_aa_alpha.alloc(sizeof(double) * bte::mlp::AA_MAX));
+        BTE_CUDA(ctx->d_aa_flag.alloc(sizeof(double)));
+        BTE_CUDA(cudaMemsetAsync(ctx->d_aa_flag.p, 0, sizeof(double), st));
     }
     if (o.accel == 1 || o.accel == 2) {
         if (o.accel_every < 4) return fail(ctx, BTE_ERR_INVALID_ARGUMENT, "bte_solve: accel_every must be >= 4");
@@ -1314,9 +1273,17 @@ extern "C" bte_status bte_solve(bte_ctx* ctx, const bte_options* opts, bte_repor
         BTE_LAUNCHED();
         BTE_CUDA(cudaEventRecord(ev[3], st));
         BTE_CUDA(cudaMemcpyAsync(ctx->h_pinned, ctx->d_margin.p, sizeof(double), cudaMemcpyDeviceToHost, st));
+        if (aa_slots)
+            BTE_CUDA(cudaMemcpyAsync(ctx->h_pinned + 1, ctx->d_aa_flag.p, sizeof(double), cudaMemcpyDeviceToHost, st));
         BTE_CUDA(cudaStreamSynchronize(st));
         if (ctx->profile) prof_resolve(ctx, nullptr, 0);
+        add_accel_time();
         const double m = ctx->h_pinned[0];
+        if (aa_slots && ctx->h_pinned[1] != 0.0) {  // the last Anderson weights blew up: restart the history
+            if (!aa_order.empty()) aa_order.erase(aa_order.begin(), aa_order.end() - 1);
+            aa_count = (int)aa_order.size();
+            BTE_CUDA(cudaMemsetAsync(ctx->d_aa_flag.p, 0, sizeof(double), st));
+        }
         // the last four temperature fields (accelerator) and the history
         if (o.accel == 1 || o.accel == 2) {
             BTE_CUDA(cudaMemcpyAsync(ctx->d_ring.as<double>() + (size_t)(it % 4) * Np, ctx->d_T.p,
@@ -1357,6 +1324,10 @@ extern "C" bte_status bte_solve(bte_ctx* ctx, const bte_options* opts, bte_repor
         // the margin at the jump (right after a jump the margin rises while the
         // intensities follow the new source, so it is judged once they have);
         // otherwise restore the state before the jump and stop extrapolating
+        if (o.accel) {
+            BTE_CUDA(cudaEventRecord(ev[5], st));
+            accel_timed = true;
+        }
         if (aa_slots && it > 0) {
             bte_status s = anderson_step(ctx, aa_slots, aa_count, aa_next, aa_order, m, rep);
             if (s != BTE_OK) return s;
@@ -1399,15 +1370,13 @@ extern "C" bte_status bte_solve(bte_ctx* ctx, const bte_options* opts, bte_repor
             accel_margin = m;
             ++rep.accel_steps;
         }
-        // the accelerator's kernels and copies run after ev[3]: time them too
-        if (o.accel) {
-            BTE_CUDA(cudaEventRecord(ev[4], st));
-            BTE_CUDA(cudaEventSynchronize(ev[4]));
-            float t34 = 0;
-            cudaEventElapsedTime(&t34, ev[3], ev[4]);
-            rep.ms_reduce += t34;
-            rep.ms_total += t34;
-        }
+        // the accelerator's kernels and copies run after ev[3]: timed by
+        // ev[5..6], read after the next synchronisation
+        if (o.accel) BTE_CUDA(cudaEventRecord(ev[6], st));
+    }
+    if (accel_timed) {
+        BTE_CUDA(cudaEventSynchronize(ev[6]));
+        add_accel_time();
     }
     if (o.max_iter == 0) result = BTE_OK;
     // heat flux (src/StaticBTESolver.cpp:323-370)

@@ -530,79 +530,140 @@ __global__ void k_aa_gather(AaState a, const double* __restrict__ T, const doubl
     }
 }
 
-// f = g - x over the state.
-__global__ void k_aa_store(const double* __restrict__ g, const double* __restrict__ x, size_t len, double* f) {
-    const size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (j < len) f[j] = g[j] - x[j];
-}
-
 constexpr int AA_MAX = 9;  // slots (depth + 1)
 constexpr int AA_THREADS = 256;
 
-// Partial Gram sums f_i . f_j (i <= j < k, slots in `slot`): AA_BLOCKS blocks
-// (a constant, so the summation order does not depend on the device), each
-// thread accumulating its grid-stride share of the state, then a fixed-order
-// block reduction per pair: part[pair][block].
-constexpr int AA_BLOCKS = 304;
-__global__ void __launch_bounds__(AA_THREADS) k_aa_gram(const double* __restrict__ f, size_t stride, size_t len,
-                                                        int k, const int* __restrict__ slot, double* part) {
-    constexpr int NP = AA_MAX * (AA_MAX + 1) / 2;
-    __shared__ double sm[AA_THREADS / 32][NP];
-    double acc[NP];
-#pragma unroll
-    for (int q = 0; q < NP; ++q) acc[q] = 0.0;
-    int sl[AA_MAX];
-#pragma unroll
-    for (int i = 0; i < AA_MAX; ++i) sl[i] = i < k ? slot[i] : 0;
-    for (size_t c = (size_t)blockIdx.x * AA_THREADS + threadIdx.x; c < len; c += (size_t)gridDim.x * AA_THREADS) {
-        double v[AA_MAX];
-#pragma unroll
-        for (int i = 0; i < AA_MAX; ++i) v[i] = i < k ? f[(size_t)sl[i] * stride + c] : 0.0;
-        int q = 0;
-#pragma unroll
-        for (int i = 0; i < AA_MAX; ++i)
-#pragma unroll
-            for (int jj = i; jj < AA_MAX; ++jj, ++q) acc[q] = fma(v[i], v[jj], acc[q]);
-    }
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-    for (int q = 0; q < NP; ++q) {
-        double a = acc[q];
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
-        if (lane == 0) sm[warp][q] = a;
-    }
-    __syncthreads();
-    for (int q = threadIdx.x; q < NP; q += AA_THREADS) {
-        double t = 0.0;
-        for (int w = 0; w < AA_THREADS / 32; ++w) t += sm[w][q];
-        part[(size_t)q * gridDim.x + blockIdx.x] = t;
-    }
-}
-
-// One block: gram[pair] = sum over blocks of the partials, in block order.
-__global__ void k_aa_gram_final(const double* __restrict__ part, int nblk, double* gram) {
-    const int q = threadIdx.x;
-    if (q >= AA_MAX * (AA_MAX + 1) / 2) return;
-    double s = 0.0;
-    for (int b = 0; b < nblk; ++b) s += part[(size_t)q * nblk + b];
-    gram[q] = s;
-}
-
 struct AaMix {
-    int slot[AA_MAX];
-    double alpha[AA_MAX];
+    int slot[AA_MAX];  // stored slots, oldest first
     int k;
 };
 
+// The newest pair of the history: g = the state after the iteration (T, e at
+// the boundary cells) written to slot `slot`, f = g - x, and the partial dot
+// products f . f_s for every stored slot s (mx, the new slot included) over
+// this block's grid-stride share of the state, in a fixed order:
+// part[i][block] for mx.slot[i].  AA_BLOCKS blocks (a constant, so the order
+// does not depend on the device).  Only the newest row of the Gram matrix is
+// computed: the others do not change.
+constexpr int AA_BLOCKS = 304;
+__global__ void __launch_bounds__(AA_THREADS) k_aa_push(AaState a, const double* __restrict__ T,
+                                                        const double* __restrict__ e, const double* __restrict__ x,
+                                                        size_t stride, int slot, AaMix mx, double* g, double* f,
+                                                        double* part) {
+    __shared__ double sm[AA_THREADS / 32][AA_MAX];
+    const size_t len = a.len();
+    double acc[AA_MAX];
+#pragma unroll
+    for (int i = 0; i < AA_MAX; ++i) acc[i] = 0.0;
+    double* gs = g + (size_t)slot * stride;
+    double* fs = f + (size_t)slot * stride;
+    for (size_t j = (size_t)blockIdx.x * AA_THREADS + threadIdx.x; j < len; j += (size_t)gridDim.x * AA_THREADS) {
+        double gv;
+        if (j < (size_t)a.n) {
+            gv = T[j];
+        } else {
+            double sc;
+            gv = e[a.e_index(j, sc)] * sc;
+        }
+        const double fv = gv - x[j];
+        gs[j] = gv;
+        fs[j] = fv;
+#pragma unroll
+        for (int i = 0; i < AA_MAX; ++i)
+            if (i < mx.k) acc[i] = fma(fv, mx.slot[i] == slot ? fv : f[(size_t)mx.slot[i] * stride + j], acc[i]);
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int i = 0; i < AA_MAX; ++i) {
+        double v = acc[i];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0) sm[warp][i] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < AA_MAX) {
+        double t = 0.0;
+        for (int w = 0; w < AA_THREADS / 32; ++w) t += sm[w][threadIdx.x];
+        part[(size_t)threadIdx.x * gridDim.x + blockIdx.x] = t;
+    }
+}
+
+// One block: the newest Gram row, G[slot][s] = G[s][slot] = sum over blocks of
+// the partials (block order), into the persistent slot-indexed matrix G.
+__global__ void k_aa_row(const double* __restrict__ part, int nblk, int slot, AaMix mx, double* G) {
+    const int i = threadIdx.x;
+    if (i >= mx.k) return;
+    double t = 0.0;
+    for (int b = 0; b < nblk; ++b) t += part[(size_t)i * nblk + b];
+    G[slot * AA_MAX + mx.slot[i]] = t;
+    G[mx.slot[i] * AA_MAX + slot] = t;
+}
+
+// One thread: alpha = G^-1 1 / (1^T G^-1 1) over the stored slots (Gram
+// matrix indexed by slot, AA_MAX x AA_MAX), Tikhonov 1e-12 max(diag), Gaussian
+// elimination with partial pivoting.  If the weights are not finite or one
+// exceeds 1e3 the newest iterate is taken alone (alpha = e_k) and *flag = 1
+// asks the host to restart the history.
+__global__ void k_aa_solve(const double* __restrict__ Gs, AaMix mx, double* alpha, double* flag) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const int k = mx.k;
+    double G[AA_MAX][AA_MAX + 1];
+    double dmax = 0.0;
+    for (int i = 0; i < k; ++i)
+        for (int j = 0; j < k; ++j) {
+            G[i][j] = Gs[mx.slot[i] * AA_MAX + mx.slot[j]];
+            if (i == j) dmax = fmax(dmax, G[i][i]);
+        }
+    bool ok = dmax > 0.0 && dmax < 1e300;
+    for (int i = 0; i < k; ++i) {
+        G[i][i] += 1e-12 * dmax;
+        G[i][k] = 1.0;
+    }
+    for (int c = 0; ok && c < k; ++c) {
+        int piv = c;
+        for (int r = c + 1; r < k; ++r)
+            if (fabs(G[r][c]) > fabs(G[piv][c])) piv = r;
+        if (piv != c)
+            for (int j = 0; j <= k; ++j) {
+                const double t = G[c][j];
+                G[c][j] = G[piv][j];
+                G[piv][j] = t;
+            }
+        if (G[c][c] == 0.0) {
+            ok = false;
+            break;
+        }
+        for (int r = c + 1; r < k; ++r) {
+            const double f = G[r][c] / G[c][c];
+            for (int j = c; j <= k; ++j) G[r][j] -= f * G[c][j];
+        }
+    }
+    double a[AA_MAX], sum = 0.0;
+    if (ok) {
+        for (int r = k - 1; r >= 0; --r) {
+            double v = G[r][k];
+            for (int j = r + 1; j < k; ++j) v -= G[r][j] * a[j];
+            a[r] = v / G[r][r];
+        }
+        for (int i = 0; i < k; ++i) sum += a[i];
+        for (int i = 0; i < k; ++i) {
+            a[i] /= sum;
+            if (!(fabs(a[i]) <= 1e3)) ok = false;
+        }
+    }
+    for (int i = 0; i < k; ++i) alpha[i] = ok ? a[i] : (i == k - 1 ? 1.0 : 0.0);
+    *flag = ok ? 0.0 : 1.0;
+}
+
 // state = sum_i alpha_i g_i: T and ebar[b][c] = C_b / Omega_tot (T - T_ref), and
 // the boundary-cell intensities written back into e (the next iteration's e_prev).
-__global__ void k_aa_mix(AaState a, const double* __restrict__ g, size_t stride, AaMix mx, double T_ref,
-                         double* __restrict__ T, double* __restrict__ ebar, double* __restrict__ e) {
+__global__ void k_aa_mix(AaState a, const double* __restrict__ g, size_t stride, AaMix mx,
+                         const double* __restrict__ alpha, double T_ref, double* __restrict__ T,
+                         double* __restrict__ ebar, double* __restrict__ e) {
     const size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= a.len()) return;
     double t = 0.0;
-    for (int i = 0; i < mx.k; ++i) t = fma(mx.alpha[i], g[(size_t)mx.slot[i] * stride + j], t);
+    for (int i = 0; i < mx.k; ++i) t = fma(alpha[i], g[(size_t)mx.slot[i] * stride + j], t);
     if (j < (size_t)a.n) {
         T[j] = t;
         for (int b = 0; b < a.n_band; ++b) ebar[(size_t)b * a.Np + j] = a.Cb[b] / a.solid_angle * (t - T_ref);

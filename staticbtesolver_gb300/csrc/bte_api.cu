@@ -115,7 +115,7 @@ struct bte_ctx {
     int plan_lagged_dirs = 0;
     bool sweep_margin = false;  // acyclic plan: the sweep sums the margin partials (d_spart)
     long long plan_levels = 0;
-    DevBuf p_cell, p_dg, p_vo, p_nb, p_fc, p_lvl, p_lvl_off, p_part, p_bad, p_invd, d_spart, p_bidx;
+    DevBuf p_cell, p_dg, p_vo, p_nb, p_fc, p_lvl, p_lvl_off, p_part, p_bad, p_voi, p_kinv, d_spart, p_bidx;
     DevBuf d_bcell, d_bidx, d_bsum;
     DevBuf d_snap_e, d_snap_T, d_snap_ebar;  // accelerator: state before the last jump
     DevBuf d_aa_x, d_aa_g, d_aa_f, d_aa_part, d_aa_gram, d_aa_alpha, d_aa_flag;  // Anderson mixing
@@ -723,12 +723,14 @@ static bte_status build_sweep_plan(bte_ctx* ctx) {
         ctx->d_nbr.as<int>(), ctx->d_bidx.as<int>(), F, n, Np, ND, ctx->p_cell.as<int>(), ctx->p_bidx.as<int>(),
         ctx->p_dg.as<double>(), ctx->p_vo.as<double>(), ctx->p_nb.as<int>(), ctx->p_fc.as<double>());
     BTE_LAUNCHED();
-    BTE_CUDA(ctx->p_invd.alloc(sizeof(double) * ctx->n_band * ND * n));
+    BTE_CUDA(ctx->p_voi.alloc(sizeof(double) * ctx->n_band * ND * n));
+    BTE_CUDA(ctx->p_kinv.alloc(sizeof(double) * ctx->n_band * ND * n));
     {
         bte::SweepPlan sp{ctx->p_cell.as<int>(), ctx->p_bidx.as<int>(), ctx->p_dg.as<double>(), ctx->p_vo.as<double>(), ctx->p_nb.as<int>(),
                           ctx->p_fc.as<double>(), ctx->p_lvl.as<int>(), ctx->p_lvl_off.as<int>(), n, F};
         bte::k_sweep_invd<<<dim3((n + 255) / 256, ND), 256, 0, st>>>(sp, ctx->d_kb.as<double>(), ctx->n_band, ND,
-                                                                     ctx->p_invd.as<double>());
+                                                                     ctx->p_voi.as<double>(),
+                                                                     ctx->p_kinv.as<double>());
         BTE_LAUNCHED();
     }
     BTE_CUDA(cudaStreamSynchronize(st));  // d_perm / d_lag go out of scope
@@ -972,8 +974,8 @@ static bte_status solve_batch_sweep(bte_ctx* ctx, int b0, int nbb, const bte_opt
     if (ctx->nbcell > 0) {
         BTE_LAUNCH(KK_RHS, -1, (double)S * ctx->nbcell * 2 * w, 0,
                    bte::k_bound_rhs<<<dim3((ctx->nbcell + 127) / 128, S), 128, 0, st>>>(
-                       src, ctx->d_bcell.as<int>(), ctx->nbcell, ctx->d_kb.as<double>(), nbb, b0,
-                       ctx->d_bsum.as<double>()));
+                       src, ctx->d_bcell.as<int>(), ctx->nbcell, ctx->d_kb.as<double>(), ctx->d_dg.as<double>(),
+                       ctx->d_vo.as<double>(), nbb, b0, ctx->d_bsum.as<double>()));
     }
     const bte::SweepSrc ssrc{ctx->d_ebar.as<double>(), ctx->d_bsum.as<double>(), ctx->e_prev, ctx->nbcell};
     bte::SweepPlan sp{ctx->p_cell.as<int>(), ctx->p_bidx.as<int>(), ctx->p_dg.as<double>(), ctx->p_vo.as<double>(), ctx->p_nb.as<int>(),
@@ -992,7 +994,7 @@ static bte_status solve_batch_sweep(bte_ctx* ctx, int b0, int nbb, const bte_opt
             const int Gk = std::max(1, std::min(cand[k][0], nbb));
             BTE_CUDA(cudaEventRecord(e0, st));
             bte::k_sweep<false><<<dim3((nbb + Gk - 1) / Gk, ctx->n_dir), cand[k][1], sweep_smem(Gk), st>>>(
-                sp, ctx->d_kb.as<double>(), ctx->p_invd.as<double>(), ssrc, ctx->e_curr, 1, Gk, sweep_ring(Gk), nbb,
+                sp, ctx->p_voi.as<double>(), ctx->p_kinv.as<double>(), ssrc, ctx->e_curr, 1, Gk, sweep_ring(Gk), nbb,
                 b0, ctx->n_band, ctx->n_dir, ctx->Np, nullptr);
             BTE_LAUNCHED();
             BTE_CUDA(cudaEventRecord(e1, st));
@@ -1008,22 +1010,23 @@ static bte_status solve_batch_sweep(bte_ctx* ctx, int b0, int nbb, const bte_opt
     }
     const int G = std::max(1, std::min(ctx->sweep_group, nbb));
     dim3 sgrid((nbb + G - 1) / G, ctx->n_dir);
-    // algorithmic HBM bytes of a sweep per system and cell: 1/D read, x written
-    // (and, with the fused margin, the previous iterate read), plus the
-    // level-ordered geometry per direction; ebar and the boundary values come from L2
+    // algorithmic HBM bytes of a sweep per system and cell: V Omega / D and
+    // k / D read, x written (and, with the fused margin, the previous iterate
+    // read), plus the level-ordered geometry per direction; ebar and the
+    // boundary values come from L2
     const bool margin = ctx->sweep_margin;
-    const double sweep_bytes = S * N * (margin ? 3 : 2) * w + geo;
+    const double sweep_bytes = S * N * (margin ? 4 : 3) * w + geo;
     int sweeps = 0;
     for (;;) {
         if (margin) {
             BTE_LAUNCH(KK_SWEEP, -1, sweep_bytes, 0,
                        bte::k_sweep<true><<<sgrid, ctx->sweep_threads, sweep_smem(G), st>>>(
-                           sp, ctx->d_kb.as<double>(), ctx->p_invd.as<double>(), ssrc, ctx->e_curr, 1, G,
+                           sp, ctx->p_voi.as<double>(), ctx->p_kinv.as<double>(), ssrc, ctx->e_curr, 1, G,
                            sweep_ring(G), nbb, b0, ctx->n_band, ctx->n_dir, ctx->Np, ctx->d_spart.as<double>()));
         } else {
             BTE_LAUNCH(KK_SWEEP, -1, sweep_bytes, 0,
                        bte::k_sweep<false><<<sgrid, ctx->sweep_threads, sweep_smem(G), st>>>(
-                           sp, ctx->d_kb.as<double>(), ctx->p_invd.as<double>(), ssrc, ctx->e_curr, sweeps == 0, G,
+                           sp, ctx->p_voi.as<double>(), ctx->p_kinv.as<double>(), ssrc, ctx->e_curr, sweeps == 0, G,
                            sweep_ring(G), nbb, b0, ctx->n_band, ctx->n_dir, ctx->Np, nullptr));
         }
         ++sweeps;

@@ -100,15 +100,19 @@ struct RhsSrc {
 };
 
 // Boundary part of the right-hand side per (system of the batch, boundary
-// cell), for the sweep: bsum[y][i] = RhsSrc::boundary for cell bcell[i], with
-// y -> direction y / nbb, band b0 + y % nbb as in FaceFluxOp.
+// cell), for the sweep: bsum[y][i] = RhsSrc::boundary / D for cell bcell[i],
+// with y -> direction y / nbb, band b0 + y % nbb as in FaceFluxOp.
 __global__ void k_bound_rhs(RhsSrc src, const int* __restrict__ bcell, int nbcell, const double* __restrict__ kb,
-                            int nbb, int b0, double* bsum) {
+                            const double* __restrict__ dg, const double* __restrict__ vo, int nbb, int b0,
+                            double* bsum) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y;
     if (i >= nbcell) return;
     const int d = y / nbb, b = b0 + y % nbb;
-    bsum[(size_t)y * nbcell + i] = src.boundary(b, d, bcell[i], kb[b]);
+    const int c = bcell[i];
+    const size_t dc = (size_t)d * src.Np + c;
+    // divided by the cell's diagonal k_b dg + vo, as the sweep's other terms
+    bsum[(size_t)y * nbcell + i] = src.boundary(b, d, c, kb[b]) / fma(kb[b], dg[dc], vo[dc]);
 }
 
 // Right-hand sides of one batch for the Krylov forms: rhs[y][c].
@@ -274,15 +278,25 @@ struct SweepPlan {
     int n, F;
 };
 
-// 1/D per system in level order: invD[b][d][j] = 1 / (k_b dg[d][j] + vo[d][j]).
-// The diagonal does not change across outer iterations, so this runs once per solve.
-__global__ void k_sweep_invd(SweepPlan sp, const double* __restrict__ kb, int n_band, int n_dir, double* invD) {
+// The diagonal folded into the sweep's coefficients, per system in level
+// order: with D = k_b dg[d][j] + vo[d][j],
+//   voi[b][d][j] = vo / D,   kinv[b][d][j] = k_b / D,
+// so x = (R - k_b off) / D becomes x = ebar voi + bs/D - kinv off: two FP64
+// operations per cell fewer in the sweep (GB300 issues FP64 at ~2 lanes per SM
+// per clock).  The diagonal does not change across outer iterations: once per solve.
+__global__ void k_sweep_invd(SweepPlan sp, const double* __restrict__ kb, int n_band, int n_dir, double* voi,
+                             double* kinv) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     const int d = blockIdx.y;
     if (j >= sp.n) return;
     const size_t pj = (size_t)d * sp.n + j;
-    for (int b = 0; b < n_band; ++b)
-        invD[((size_t)b * n_dir + d) * sp.n + j] = 1.0 / fma(kb[b], sp.dg[pj], sp.vo[pj]);
+    const double vo = sp.vo[pj], dg = sp.dg[pj];
+    for (int b = 0; b < n_band; ++b) {
+        const double invD = 1.0 / fma(kb[b], dg, vo);
+        const size_t q = ((size_t)b * n_dir + d) * sp.n + j;
+        voi[q] = vo * invD;
+        kinv[q] = kb[b] * invD;
+    }
 }
 
 // Operands of one sweep item that do not depend on the level being solved.
@@ -290,12 +304,13 @@ struct SweepItem {
     int c, b, bi;
     int u[4];
     double cf[4];
-    double invd, vo, eb, bs, old;
+    double kinv, voi, eb, bs, old;
 };
 
 // Stage A: everything addressed by the position j alone.
-__device__ __forceinline__ void sweep_load_a(const SweepPlan& sp, const double* __restrict__ invD, int d, int j,
-                                             int b, int n_dir, SweepItem& it) {
+__device__ __forceinline__ void sweep_load_a(const SweepPlan& sp, const double* __restrict__ voi,
+                                             const double* __restrict__ kinv, int d, int j, int b, int n_dir,
+                                             SweepItem& it) {
     const size_t pj = (size_t)d * sp.n + j;
     it.b = b;
     it.c = sp.cell[pj];
@@ -310,8 +325,9 @@ __device__ __forceinline__ void sweep_load_a(const SweepPlan& sp, const double* 
             it.cf[f] = 0.0;
         }
     }
-    it.invd = invD[((size_t)b * n_dir + d) * sp.n + j];
-    it.vo = sp.vo[pj];
+    const size_t q = ((size_t)b * n_dir + d) * sp.n + j;
+    it.kinv = kinv[q];
+    it.voi = voi[q];
     it.bi = sp.bidx[pj];
 }
 
@@ -362,8 +378,8 @@ __device__ __forceinline__ double block_sum_any(double v, double* smem /* [32] *
 // (x - x_old)^2 over its items, in a fixed order, into
 // mpart[d * n_band + b0 + blockIdx.x * G], the outer iteration's margin partial.
 template <bool MARGIN>
-__global__ void __launch_bounds__(128, 5) k_sweep(SweepPlan sp, const double* __restrict__ kb,
-                                                  const double* __restrict__ invD, SweepSrc src, double* x,
+__global__ void __launch_bounds__(128, 5) k_sweep(SweepPlan sp, const double* __restrict__ voi,
+                                                  const double* __restrict__ kinv, SweepSrc src, double* x,
                                                   int first_sweep, int G, int W, int nbb, int b0, int n_band,
                                                   int n_dir, size_t Np, double* __restrict__ mpart) {
     extern __shared__ double ring[];  // [G][W]
@@ -381,7 +397,7 @@ __global__ void __launch_bounds__(128, 5) k_sweep(SweepPlan sp, const double* __
         if (l >= L1) return false;
         const int j0 = sp.lvl[l];
         if (threadIdx.x >= (sp.lvl[l + 1] - j0) * gn) return false;
-        sweep_load_a(sp, invD, d, j0 + threadIdx.x / gn, b0 + g0 + threadIdx.x % gn, n_dir, dst);
+        sweep_load_a(sp, voi, kinv, d, j0 + threadIdx.x / gn, b0 + g0 + threadIdx.x % gn, n_dir, dst);
         return true;
     };
     h1 = pre(L0, p1);
@@ -397,10 +413,9 @@ __global__ void __launch_bounds__(128, 5) k_sweep(SweepPlan sp, const double* __
             const int bl = it % gn;
             if (it == threadIdx.x && h1) cur = p1;
             else {
-                sweep_load_a(sp, invD, d, j, b0 + g0 + bl, n_dir, cur);
+                sweep_load_a(sp, voi, kinv, d, j, b0 + g0 + bl, n_dir, cur);
                 sweep_load_b<MARGIN>(src, d, n_dir, nbb, b0, Np, cur);
             }
-            const double k = kb[cur.b];
             double* xb = x + ((size_t)cur.b * n_dir + d) * Np;
             double* rg = ring + (size_t)bl * W;
             double off = 0.0;
@@ -416,7 +431,7 @@ __global__ void __launch_bounds__(128, 5) k_sweep(SweepPlan sp, const double* __
                 }
                 off = fma(cur.cf[f], xu, off);
             }
-            const double v = fma(-k, off, cur.bs + cur.eb * cur.vo) * cur.invd;
+            const double v = fma(-cur.kinv, off, fma(cur.eb, cur.voi, cur.bs));
             xb[cur.c] = v;
             rg[j & (W - 1)] = v;
             if (MARGIN) {

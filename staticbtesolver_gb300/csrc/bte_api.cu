@@ -13,7 +13,9 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <mutex>
+#include <tuple>
 #include <string>
 #include <thread>
 #include <vector>
@@ -115,7 +117,7 @@ struct bte_ctx {
     int plan_lagged_dirs = 0;
     bool sweep_margin = false;  // acyclic plan: the sweep sums the margin partials (d_spart)
     long long plan_levels = 0;
-    DevBuf p_cell, p_dg, p_vo, p_nb, p_fc, p_lvl, p_lvl_off, p_part, p_bad, p_voi, p_kinv, d_spart, p_bidx;
+    DevBuf p_cell, p_dg, p_vo, p_nb, p_fc, p_lvl, p_lvl_off, p_part, p_bad, p_voi, p_kinv, d_spart, p_bidx, p_binvd;
     DevBuf d_bcell, d_bidx, d_bsum;
     DevBuf d_snap_e, d_snap_T, d_snap_ebar;  // accelerator: state before the last jump
     DevBuf d_aa_x, d_aa_g, d_aa_f, d_aa_part, d_aa_gram, d_aa_alpha, d_aa_flag;  // Anderson mixing
@@ -123,7 +125,7 @@ struct bte_ctx {
     int nbcell = 0;
     // sweep launch shape (bands per block, threads per block) picked by timing
     // the candidates on the first sweep of a plan
-    int sweep_group = 4, sweep_threads = 256;
+    int sweep_group = 2, sweep_threads = 128;
     bool sweep_tuned = false;
     float sweep_tune_ms[16] = {};
     // profiling (opts->profile): events around each launch, resolved after a sync
@@ -718,6 +720,13 @@ static bte_status build_sweep_plan(bte_ctx* ctx) {
     BTE_CUDA(ctx->p_fc.alloc(sizeof(double) * ND * F * n));
     BTE_CUDA(ctx->p_bidx.alloc(sizeof(int) * ND * n));
     BTE_CUDA(ctx->d_bsum.alloc(sizeof(double) * (size_t)ctx->nbb * ND * std::max(ctx->nbcell, 1)));
+    BTE_CUDA(ctx->p_binvd.alloc(sizeof(double) * (size_t)ctx->n_band * ND * std::max(ctx->nbcell, 1)));
+    if (ctx->nbcell > 0) {
+        bte::k_bound_invd<<<dim3((ctx->nbcell + 127) / 128, ND), 128, 0, st>>>(
+            ctx->d_bcell.as<int>(), ctx->nbcell, ctx->d_kb.as<double>(), ctx->d_dg.as<double>(),
+            ctx->d_vo.as<double>(), ctx->n_band, ND, Np, ctx->p_binvd.as<double>());
+        BTE_LAUNCHED();
+    }
     bte::k_sweep_layout<<<dim3((n + 255) / 256, ND), 256, 0, st>>>(
         d_perm.as<int>(), d_pos.as<int>(), d_lag.as<int>(), ctx->d_dg.as<double>(), ctx->d_vo.as<double>(), ctx->d_fc.as<double>(),
         ctx->d_nbr.as<int>(), ctx->d_bidx.as<int>(), F, n, Np, ND, ctx->p_cell.as<int>(), ctx->p_bidx.as<int>(),
@@ -947,6 +956,12 @@ static bte_status solve_batch_mixed(bte_ctx* ctx, int b0, int nbb, const bte_opt
     return BTE_OK;
 }
 
+// Launch shapes chosen by the sweep's autotuner, per (device, cells, faces,
+// directions, bands per batch, levels).
+using SweepTuneKey = std::tuple<int, int, int, int, int, long long>;
+static std::mutex g_sweep_tune_mutex;
+static std::map<SweepTuneKey, std::pair<int, int>> g_sweep_tune;
+
 // Shared-memory ring of the sweep: W (a power of two) positions per band, 32 KB per block.
 static int sweep_ring(int G) {
     int w = 4096;
@@ -974,14 +989,26 @@ static bte_status solve_batch_sweep(bte_ctx* ctx, int b0, int nbb, const bte_opt
     if (ctx->nbcell > 0) {
         BTE_LAUNCH(KK_RHS, -1, (double)S * ctx->nbcell * 2 * w, 0,
                    bte::k_bound_rhs<<<dim3((ctx->nbcell + 127) / 128, S), 128, 0, st>>>(
-                       src, ctx->d_bcell.as<int>(), ctx->nbcell, ctx->d_kb.as<double>(), ctx->d_dg.as<double>(),
-                       ctx->d_vo.as<double>(), nbb, b0, ctx->d_bsum.as<double>()));
+                       src, ctx->d_bcell.as<int>(), ctx->nbcell, ctx->d_kb.as<double>(), ctx->p_binvd.as<double>(),
+                       nbb, b0, ctx->d_bsum.as<double>()));
     }
     const bte::SweepSrc ssrc{ctx->d_ebar.as<double>(), ctx->d_bsum.as<double>(), ctx->e_prev, ctx->nbcell};
     bte::SweepPlan sp{ctx->p_cell.as<int>(), ctx->p_bidx.as<int>(), ctx->p_dg.as<double>(), ctx->p_vo.as<double>(), ctx->p_nb.as<int>(),
                       ctx->p_fc.as<double>(), ctx->p_lvl.as<int>(), ctx->p_lvl_off.as<int>(), ctx->n, ctx->F};
     // launch-shape autotuning on the first sweep of this plan (each candidate
-    // computes the same x from the same inputs)
+    // computes the same x from the same inputs); the choice is kept per
+    // process for the same device and plan shape, so a new context on the
+    // same mesh does not time the candidates again
+    const SweepTuneKey tkey{ctx->device, ctx->n, ctx->F, ctx->n_dir, nbb, ctx->plan_levels};
+    if (!ctx->sweep_tuned) {
+        std::lock_guard<std::mutex> lock(g_sweep_tune_mutex);
+        auto hit = g_sweep_tune.find(tkey);
+        if (hit != g_sweep_tune.end()) {
+            ctx->sweep_group = hit->second.first;
+            ctx->sweep_threads = hit->second.second;
+            ctx->sweep_tuned = true;
+        }
+    }
     if (!ctx->sweep_tuned) {
         // (bands per block, threads); k_sweep takes at most 128 threads
         static const int cand[][2] = {{1, 64}, {1, 128}, {2, 64}, {2, 128}, {4, 64}, {4, 128}, {8, 128}, {16, 128}};
@@ -1007,6 +1034,8 @@ static bte_status solve_batch_sweep(bte_ctx* ctx, int b0, int nbb, const bte_opt
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
         ctx->sweep_tuned = true;
+        std::lock_guard<std::mutex> lock(g_sweep_tune_mutex);
+        g_sweep_tune[tkey] = {ctx->sweep_group, ctx->sweep_threads};
     }
     const int G = std::max(1, std::min(ctx->sweep_group, nbb));
     dim3 sgrid((nbb + G - 1) / G, ctx->n_dir);

@@ -103,16 +103,27 @@ struct RhsSrc {
 // cell), for the sweep: bsum[y][i] = RhsSrc::boundary / D for cell bcell[i],
 // with y -> direction y / nbb, band b0 + y % nbb as in FaceFluxOp.
 __global__ void k_bound_rhs(RhsSrc src, const int* __restrict__ bcell, int nbcell, const double* __restrict__ kb,
-                            const double* __restrict__ dg, const double* __restrict__ vo, int nbb, int b0,
-                            double* bsum) {
+                            const double* __restrict__ binvd, int nbb, int b0, double* bsum) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y;
     if (i >= nbcell) return;
     const int d = y / nbb, b = b0 + y % nbb;
-    const int c = bcell[i];
-    const size_t dc = (size_t)d * src.Np + c;
-    // divided by the cell's diagonal k_b dg + vo, as the sweep's other terms
-    bsum[(size_t)y * nbcell + i] = src.boundary(b, d, c, kb[b]) / fma(kb[b], dg[dc], vo[dc]);
+    // scaled by the cell's 1/D, as the sweep's other terms
+    bsum[(size_t)y * nbcell + i] =
+        src.boundary(b, d, bcell[i], kb[b]) * binvd[((size_t)b * src.n_dir + d) * nbcell + i];
+}
+
+// 1/D = 1 / (k_b dg[d][c] + vo[d][c]) of every boundary cell, per (band,
+// direction): binvd[b][d][i] for cell bcell[i] (once per solve).
+__global__ void k_bound_invd(const int* __restrict__ bcell, int nbcell, const double* __restrict__ kb,
+                             const double* __restrict__ dg, const double* __restrict__ vo, int n_band, int n_dir,
+                             size_t Np, double* binvd) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int d = blockIdx.y;
+    if (i >= nbcell) return;
+    const size_t dc = (size_t)d * Np + bcell[i];
+    for (int b = 0; b < n_band; ++b)
+        binvd[((size_t)b * n_dir + d) * nbcell + i] = 1.0 / fma(kb[b], dg[dc], vo[dc]);
 }
 
 // Right-hand sides of one batch for the Krylov forms: rhs[y][c].

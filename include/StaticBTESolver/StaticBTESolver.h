@@ -37,7 +37,11 @@ public:
     void solve(int max_iter);
 
     // ---- Additions
-    void setForm(int form);                 // bte_form (0 plain FP64, 1 mixed)
+    void setForm(int form);                 // bte_form (0 plain FP64, 1 mixed, 2 sweep)
+    // outer-iteration acceleration (bte_options.accel: 0 none, 1 learned, 2 Aitken,
+    // 3 Anderson; every: interval or depth).  Learned needs setMlp first.
+    void setAccel(int accel, int every);
+    void setMlp(const std::vector<float>& params);  // bte_mlp_param_count() values
     void setTolerance(double margin_tol);   // outer stop (reference: 1e-5)
     void setInnerTolerance(double tol);     // inner relative residual (reference: 1e-9)
     void setVerbose(bool verbose);          // print the reference's stdout lines (default true)
@@ -60,6 +64,8 @@ private:
     int DM_ = 3, num_theta_ = 4, num_phi_ = 4;
     double T_ref_ = 300;
     int form_ = 0;
+    int accel_ = 0, accel_every_ = 8;
+    std::vector<float> mlp_;
     double tol_ = 1e-5, inner_tol_ = 1e-9;
     bool verbose_ = true;
     int status_ = 0, n_iter_ = 0;

@@ -1256,6 +1256,19 @@ extern "C" bte_status bte_solve(bte_ctx* ctx, const bte_options* opts, bte_repor
     }
     ctx->history.clear();
     ctx->history_rows = 0;
+    // CUDA graphs of the sweep form's outer iteration (not with the profiler,
+    // which times each launch, nor with lagged edges, whose sweeps repeat
+    // under host control)
+    const bool use_graph = o.form == BTE_FORM_SWEEP && fused_margin && !ctx->profile;
+    cudaGraphExec_t gexec[2] = {nullptr, nullptr};
+    struct GraphGuard {
+        cudaGraphExec_t* g;
+        ~GraphGuard() {
+            for (int k = 0; k < 2; ++k)
+                if (g[k]) cudaGraphExecDestroy(g[k]);
+        }
+    } graph_guard{gexec};
+    long long graph_solves[2] = {0, 0}, graph_inner[2] = {0, 0}, graph_launches[2] = {0, 0};
     for (int it = 0; it < o.max_iter; ++it) {
         std::swap(ctx->e_curr, ctx->e_prev);
         BTE_CUDA(cudaEventRecord(ev[0], st));
@@ -1266,43 +1279,86 @@ extern "C" bte_status bte_solve(bte_ctx* ctx, const bte_options* opts, bte_repor
                        bte::mlp::k_aa_gather<<<(unsigned)((L + 255) / 256), 256, 0, st>>>(
                            as, ctx->d_T.as<double>(), ctx->e_prev, ctx->d_aa_x.as<double>()));
         }
-        if (ctx->ndiff > 0) {
-            const int nt = ctx->ndiff * NB;
-            BTE_LAUNCH(KK_DIFFUSE, -1, (double)nt * (ND + 1) * 8.0, 0,
-                       bte::k_diffuse_wall<<<(nt + 127) / 128, 128, 0, st>>>(
-                           ctx->e_prev, ctx->d_dlist.as<int>(), ctx->d_bf_cell.as<int>(), ctx->d_wdiff.as<double>(),
-                           ctx->d_wden.as<double>(), ctx->ndiff, NB, ND, Np, ctx->nbf, ctx->d_ediff.as<double>()));
-        }
-        if (fused_margin) BTE_CUDA(cudaMemsetAsync(ctx->d_spart.p, 0, sizeof(double) * ND * NB, st));
-        BTE_CUDA(cudaEventRecord(ev[1], st));
-        for (int b0 = 0; b0 < NB; b0 += ctx->nbb) {
-            const int nbb = std::min(ctx->nbb, NB - b0);
-            bte_status s = o.form == BTE_FORM_SWEEP   ? solve_batch_sweep(ctx, b0, nbb, o, rep)
-                           : o.form == BTE_FORM_MIXED ? solve_batch_mixed(ctx, b0, nbb, o, rep)
-                                                      : solve_batch_plain(ctx, b0, nbb, o, rep);
-            if (s != BTE_OK) return s;
-        }
-        BTE_CUDA(cudaEventRecord(ev[2], st));
-        if (fused_margin) {
-            BTE_LAUNCH(KK_REDUCE, -1, (1.0 * NB * ND + NB) * ctx->n * 8.0, 0,
-                       bte::k_reduce<false><<<dim3(nred, NB), bte::THREADS, 0, st>>>(
-                           ctx->e_curr, ctx->e_prev, ctx->d_omega.as<double>(), ctx->d_Cb.as<double>(), ctx->T_ref,
-                           ctx->n, ND, Np, ctx->d_Tb.as<double>(), nullptr));
+        // the kernels of one outer iteration (ev[1], ev[2] mark its phases when
+        // launched one by one; a captured CUDA graph is timed as a whole)
+        auto enqueue_iteration = [&](bool timed) -> bte_status {
+            if (ctx->ndiff > 0) {
+                const int nt = ctx->ndiff * NB;
+                BTE_LAUNCH(KK_DIFFUSE, -1, (double)nt * (ND + 1) * 8.0, 0,
+                           bte::k_diffuse_wall<<<(nt + 127) / 128, 128, 0, st>>>(
+                               ctx->e_prev, ctx->d_dlist.as<int>(), ctx->d_bf_cell.as<int>(), ctx->d_wdiff.as<double>(),
+                               ctx->d_wden.as<double>(), ctx->ndiff, NB, ND, Np, ctx->nbf, ctx->d_ediff.as<double>()));
+            }
+            if (fused_margin) BTE_CUDA(cudaMemsetAsync(ctx->d_spart.p, 0, sizeof(double) * ND * NB, st));
+            if (timed) BTE_CUDA(cudaEventRecord(ev[1], st));
+            for (int b0 = 0; b0 < NB; b0 += ctx->nbb) {
+                const int nbb = std::min(ctx->nbb, NB - b0);
+                bte_status s = o.form == BTE_FORM_SWEEP   ? solve_batch_sweep(ctx, b0, nbb, o, rep)
+                               : o.form == BTE_FORM_MIXED ? solve_batch_mixed(ctx, b0, nbb, o, rep)
+                                                          : solve_batch_plain(ctx, b0, nbb, o, rep);
+                if (s != BTE_OK) return s;
+            }
+            if (timed) BTE_CUDA(cudaEventRecord(ev[2], st));
+            if (fused_margin) {
+                BTE_LAUNCH(KK_REDUCE, -1, (1.0 * NB * ND + NB) * ctx->n * 8.0, 0,
+                           bte::k_reduce<false><<<dim3(nred, NB), bte::THREADS, 0, st>>>(
+                               ctx->e_curr, ctx->e_prev, ctx->d_omega.as<double>(), ctx->d_Cb.as<double>(), ctx->T_ref,
+                               ctx->n, ND, Np, ctx->d_Tb.as<double>(), nullptr));
+            } else {
+                BTE_LAUNCH(KK_REDUCE, -1, (2.0 * NB * ND + NB) * ctx->n * 8.0, 0,
+                           bte::k_reduce<true><<<dim3(nred, NB), bte::THREADS, 0, st>>>(
+                               ctx->e_curr, ctx->e_prev, ctx->d_omega.as<double>(), ctx->d_Cb.as<double>(), ctx->T_ref,
+                               ctx->n, ND, Np, ctx->d_Tb.as<double>(), ctx->d_mpart.as<double>()));
+            }
+            BTE_LAUNCH(KK_REDUCE, -1, (2.0 * NB + 1) * ctx->n * 8.0, 0,
+                       bte::k_recover<<<(ctx->n + 255) / 256, 256, 0, st>>>(
+                           ctx->d_Tb.as<double>(), ctx->d_Cb.as<double>(), ctx->d_Lr.as<double>(), Lr_sum, ctx->T_ref,
+                           ctx->solid_angle, ctx->n, NB, Np, ctx->d_T.as<double>(), ctx->d_ebar.as<double>()));
+            // margin = sum of the partials / (n_band n_cell), fixed order
+            bte::k_margin_final<<<1, bte::THREADS, 0, st>>>(fused_margin ? ctx->d_spart.as<double>() : ctx->d_mpart.as<double>(),
+                                                            fused_margin ? ND * NB : nred * NB, (double)NB * ctx->n,
+                                                            ctx->d_margin.as<double>());
+            BTE_LAUNCHED();
+            return BTE_OK;
+        };
+        if (use_graph && it >= 1) {
+            // from the second outer iteration on (the first times the sweep's
+            // launch shapes), the iteration is one CUDA graph per parity of it
+            // (e_curr and e_prev alternate), captured once and replayed
+            const int par = it & 1;
+            if (!gexec[par]) {
+                const bte_report before = rep;
+                const long long launches_before = ctx->launches;
+                BTE_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+                const bte_status cs = enqueue_iteration(false);
+                cudaGraph_t graph = nullptr;
+                const cudaError_t ce = cudaStreamEndCapture(st, &graph);
+                if (cs != BTE_OK) {
+                    if (graph) cudaGraphDestroy(graph);
+                    return cs;
+                }
+                BTE_CUDA(ce);
+                const cudaError_t ie = cudaGraphInstantiate(&gexec[par], graph, 0);
+                cudaGraphDestroy(graph);
+                BTE_CUDA(ie);
+                // host-side counters the capture advanced: added on every replay instead
+                graph_solves[par] = rep.inner_solves - before.inner_solves;
+                graph_inner[par] = rep.inner_iterations - before.inner_iterations;
+                graph_launches[par] = ctx->launches - launches_before;
+                rep.inner_solves = before.inner_solves;
+                rep.inner_iterations = before.inner_iterations;
+                ctx->launches = launches_before;
+            }
+            BTE_CUDA(cudaEventRecord(ev[1], st));
+            BTE_CUDA(cudaGraphLaunch(gexec[par], st));
+            BTE_CUDA(cudaEventRecord(ev[2], st));
+            rep.inner_solves += graph_solves[par];
+            rep.inner_iterations += graph_inner[par];
+            ctx->launches += graph_launches[par];
         } else {
-            BTE_LAUNCH(KK_REDUCE, -1, (2.0 * NB * ND + NB) * ctx->n * 8.0, 0,
-                       bte::k_reduce<true><<<dim3(nred, NB), bte::THREADS, 0, st>>>(
-                           ctx->e_curr, ctx->e_prev, ctx->d_omega.as<double>(), ctx->d_Cb.as<double>(), ctx->T_ref,
-                           ctx->n, ND, Np, ctx->d_Tb.as<double>(), ctx->d_mpart.as<double>()));
+            bte_status es = enqueue_iteration(true);
+            if (es != BTE_OK) return es;
         }
-        BTE_LAUNCH(KK_REDUCE, -1, (2.0 * NB + 1) * ctx->n * 8.0, 0,
-                   bte::k_recover<<<(ctx->n + 255) / 256, 256, 0, st>>>(
-                       ctx->d_Tb.as<double>(), ctx->d_Cb.as<double>(), ctx->d_Lr.as<double>(), Lr_sum, ctx->T_ref,
-                       ctx->solid_angle, ctx->n, NB, Np, ctx->d_T.as<double>(), ctx->d_ebar.as<double>()));
-        // margin = sum of the partials / (n_band n_cell), fixed order
-        bte::k_margin_final<<<1, bte::THREADS, 0, st>>>(fused_margin ? ctx->d_spart.as<double>() : ctx->d_mpart.as<double>(),
-                                                        fused_margin ? ND * NB : nred * NB, (double)NB * ctx->n,
-                                                        ctx->d_margin.as<double>());
-        BTE_LAUNCHED();
         BTE_CUDA(cudaEventRecord(ev[3], st));
         BTE_CUDA(cudaMemcpyAsync(ctx->h_pinned, ctx->d_margin.p, sizeof(double), cudaMemcpyDeviceToHost, st));
         if (aa_slots)

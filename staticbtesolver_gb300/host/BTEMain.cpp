@@ -4,6 +4,8 @@
 //   --form plain|mixed|sweep   inner-solve form (default plain: FP64 BiCGSTAB as the reference GPU path)
 //   --tol X              outer margin threshold (default 1e-5)
 //   --inner-tol X        inner relative residual (default 1e-9)
+//   --accel none|aitken|anderson, --accel-every N
+//                        outer-iteration acceleration (default none: the reference's iteration)
 //   --tempcell FILE      write the cell temperatures as the reference's Tempcell.dat
 //                        ("x/L_x y/L_y [z/L_z] T" per cell, src/StaticBTESolver.cpp:818-831)
 #include <getopt.h>
@@ -34,8 +36,11 @@ extern "C" int sbte_main(int argc, char** argv) {
                                        {"tol", required_argument, nullptr, 1002},
                                        {"inner-tol", required_argument, nullptr, 1003},
                                        {"tempcell", required_argument, nullptr, 1004},
+                                       {"accel", required_argument, nullptr, 1005},
+                                       {"accel-every", required_argument, nullptr, 1006},
                                        {nullptr, 0, nullptr, 0}};
     std::string geo, bandfile, bcfile, tempcell;
+    int accel = 0, accel_every = 8;
     double L_x = 0, L_y = 0, L_z = 0, T_ref = 300, tol = 1e-5, inner_tol = 1e-9;
     int DM = 3, ntheta = 4, nphi = 4, maxIter = 10000, form = 0;
     bool has_bc = false;
@@ -58,6 +63,16 @@ extern "C" int sbte_main(int argc, char** argv) {
             case 1002: tol = std::stod(optarg); break;
             case 1003: inner_tol = std::stod(optarg); break;
             case 1004: tempcell = optarg; break;
+            case 1005: {
+                const std::string a = optarg;
+                accel = a == "anderson" ? 3 : a == "aitken" ? 2 : a == "none" ? 0 : -1;
+                if (accel < 0) {
+                    std::cerr << "--accel takes none, aitken or anderson" << std::endl;
+                    return 1;
+                }
+                break;
+            }
+            case 1006: accel_every = std::stoi(optarg); break;
             default: std::cerr << "Unknown option " << c << std::endl; return 1;
         }
     }
@@ -96,6 +111,7 @@ extern "C" int sbte_main(int argc, char** argv) {
         solver.setForm(form);
         solver.setTolerance(tol);
         solver.setInnerTolerance(inner_tol);
+        solver.setAccel(accel, accel_every);
         solver.solve(maxIter);
         rc = (solver.status() == 0 || solver.status() == 6) ? 0 : 1;
         if (rc == 0 && !tempcell.empty() && !solver.writeTempcell(tempcell)) {

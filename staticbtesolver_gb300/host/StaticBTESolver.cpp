@@ -36,6 +36,11 @@ void StaticBTESolver::setParam(int DM, int num_theta, int num_phi, double T_ref)
 }
 
 void StaticBTESolver::setForm(int form) { form_ = form; }
+void StaticBTESolver::setAccel(int accel, int every) {
+    accel_ = accel;
+    accel_every_ = every;
+}
+void StaticBTESolver::setMlp(const std::vector<float>& params) { mlp_ = params; }
 void StaticBTESolver::setTolerance(double tol) { tol_ = tol; }
 void StaticBTESolver::setInnerTolerance(double tol) { inner_tol_ = tol; }
 void StaticBTESolver::setVerbose(bool v) { verbose_ = v; }
@@ -74,6 +79,24 @@ void StaticBTESolver::solve(int max_iter) {
     o.max_iter = max_iter;
     o.tol = tol_;
     o.form = form_;
+    o.accel = accel_;
+    o.accel_every = accel_every_;
+    if (accel_ == 1 || accel_ == 2) {  // the per-cell extrapolations use the centroids
+        status_ = bte_set_centroids(ctx_, P.centroid.data());
+        if (status_ == BTE_OK && accel_ == 1) {
+            if ((int)mlp_.size() != bte_mlp_param_count()) {
+                std::cerr << "StaticBTESolver: the learned accelerator needs setMlp with " << bte_mlp_param_count()
+                          << " values" << std::endl;
+                status_ = BTE_ERR_STATE;
+                return;
+            }
+            status_ = bte_set_mlp(ctx_, mlp_.data());
+        }
+        if (status_ != BTE_OK) {
+            std::cerr << "StaticBTESolver: " << bte_last_error(ctx_) << std::endl;
+            return;
+        }
+    }
     o.inner_tol = inner_tol_;
     Printer pr{verbose_};
     o.on_iteration = print_iteration;

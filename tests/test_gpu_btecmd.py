@@ -12,23 +12,26 @@ from conftest import rel_l2
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("form", ["plain", "sweep"])
-def test_btecmd_2dm2dg(sbte, get_case, tmp_path, form):
+@pytest.mark.parametrize("form,accel", [("plain", "none"), ("sweep", "none"), ("sweep", "anderson")])
+def test_btecmd_2dm2dg(sbte, get_case, tmp_path, form, accel):
     from staticbtesolver_gb300 import _build
     c = get_case("2DM2DG")
     out = tmp_path / "Tempcell.dat"
     cmd = [_build.BTECMD, "-g", c.geo, "-m", c.band, "-b", c.bc, "-d", str(c.DM), "-t", str(c.nt), "-p", str(c.np),
            "-T", "300", "-I", str(c.max_iter), "-x", repr(c.L[0]), "-y", repr(c.L[1]), "--form", form,
-           "--tempcell", str(out)]
+           "--accel", accel, "--tempcell", str(out)]
     r = subprocess.run(cmd, capture_output=True, text=True, timeout=300, cwd=tmp_path)
     assert r.returncode == 0, r.stderr
     margins = [float(m) for m in re.findall(r"Iteration #\d+\t Margin per band per cell: (\S+)", r.stdout)]
-    assert len(margins) == int(c.ref["n_iter"])
+    if accel == "none":
+        assert len(margins) == int(c.ref["n_iter"])
+    else:  # the accelerated iteration stops at the same margin, sooner
+        assert len(margins) < int(c.ref["n_iter"]) and margins[-1] <= 1e-5
     q = {int(k): float(v) for k, v in re.findall(r"heat flux of Boundary Condition #(\d+): (\S+)", r.stdout)}
     q = np.array([q[k] for k in sorted(q)])
     big = np.abs(c.ref["q"]) > 1e-3 * np.abs(c.ref["q"]).max()
     # the printed fluxes carry 6 significant digits
-    np.testing.assert_allclose(q[big], c.ref["q"][big], rtol=6e-6)
+    np.testing.assert_allclose(q[big], c.ref["q"][big], rtol=6e-6 if accel == "none" else 1e-4)
     assert re.search(r"N_cell: \d+", r.stdout) and "Time taken by iteration" in r.stdout
     rows = np.loadtxt(out)
     assert rows.shape == (c.ref["T"].size, 3)

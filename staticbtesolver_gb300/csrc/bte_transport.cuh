@@ -312,39 +312,14 @@ __global__ void k_sweep_invd(SweepPlan sp, const double* __restrict__ kb, int n_
 
 // Operands of one sweep item that do not depend on the level being solved.
 struct SweepItem {
-    int c, b, bi;
+    int c, bi;
     int u[4];
     double cf[4];
     double kinv, voi, eb, bs, old;
 };
 
-// Stage A: everything addressed by the position j alone.
-__device__ __forceinline__ void sweep_load_a(const SweepPlan& sp, const double* __restrict__ voi,
-                                             const double* __restrict__ kinv, int d, int j, int b, int n_dir,
-                                             SweepItem& it) {
-    const size_t pj = (size_t)d * sp.n + j;
-    it.b = b;
-    it.c = sp.cell[pj];
-#pragma unroll
-    for (int f = 0; f < 4; ++f) {
-        if (f < sp.F) {
-            const size_t q = ((size_t)d * sp.F + f) * sp.n + j;
-            it.u[f] = sp.nb[q];
-            it.cf[f] = sp.fc[q];
-        } else {
-            it.u[f] = -1;
-            it.cf[f] = 0.0;
-        }
-    }
-    const size_t q = ((size_t)b * n_dir + d) * sp.n + j;
-    it.kinv = kinv[q];
-    it.voi = voi[q];
-    it.bi = sp.bidx[pj];
-}
-
-// Stage B: what is addressed by the cell (ebar, the boundary part of the
-// right-hand side, and with MARGIN the previous iterate), issued a level after
-// stage A so the cell index has arrived and the loads do not stall the sweep.
+// The cell-addressed operands come from SweepSrc (ebar, the boundary part of
+// the right-hand side, and with MARGIN the previous iterate).
 struct SweepSrc {
     const double* ebar;   // [n_band][Np]
     const double* bsum;   // [nbb * n_dir][nbcell] (k_bound_rhs)
@@ -352,12 +327,46 @@ struct SweepSrc {
     int nbcell;
 };
 
+// Row pointers of one thread's (band, direction) system, computed once per
+// block so the per-item work is 32-bit indexing only.
+struct SweepRows {
+    const int* cell;   // [n] level order of direction d
+    const int* bidx;   // [n]
+    const int* nb;     // [F][n]
+    const double* fc;  // [F][n]
+    const double* voi; // [n] this band
+    const double* kinv;
+    const double* eb;  // ebar of this band, by cell
+    const double* bs;  // boundary part of this system, by boundary row
+    const double* xold;
+    int n, F;
+};
+
+// Stage A: everything addressed by the position j alone.
+__device__ __forceinline__ void sweep_load_a(const SweepRows& r, int j, SweepItem& it) {
+    it.c = r.cell[j];
+#pragma unroll
+    for (int f = 0; f < 4; ++f) {
+        if (f < r.F) {
+            it.u[f] = r.nb[f * r.n + j];
+            it.cf[f] = r.fc[f * r.n + j];
+        } else {
+            it.u[f] = -1;
+            it.cf[f] = 0.0;
+        }
+    }
+    it.kinv = r.kinv[j];
+    it.voi = r.voi[j];
+    it.bi = r.bidx[j];
+}
+
+// Stage B: what is addressed by the cell, issued a level after stage A so the
+// cell index has arrived and the loads do not stall the sweep.
 template <bool MARGIN>
-__device__ __forceinline__ void sweep_load_b(const SweepSrc& src, int d, int n_dir, int nbb, int b0, size_t Np,
-                                             SweepItem& it) {
-    it.eb = src.ebar[(size_t)it.b * Np + it.c];
-    it.bs = it.bi >= 0 ? src.bsum[((size_t)d * nbb + (it.b - b0)) * src.nbcell + it.bi] : 0.0;
-    if (MARGIN) it.old = src.x_old[((size_t)it.b * n_dir + d) * Np + it.c];
+__device__ __forceinline__ void sweep_load_b(const SweepRows& r, SweepItem& it) {
+    it.eb = r.eb[it.c];
+    it.bs = it.bi >= 0 ? r.bs[it.bi] : 0.0;
+    if (MARGIN) it.old = r.xold[it.c];
 }
 
 // Fixed-order sum over a block of any whole-warp size (<= 1024 threads); the
@@ -375,14 +384,17 @@ __device__ __forceinline__ double block_sum_any(double v, double* smem /* [32] *
 }
 
 // One block sweeps direction blockIdx.y for bands b0 + blockIdx.x * G .. + G - 1.
-// x and x_old are e_curr / e_prev ([band][n_dir][Np]).  Each thread's first
-// item of the next two levels is loaded ahead (everything but the upstream
-// values), and the block keeps its last W solved positions (for its G bands)
-// in a shared-memory ring, so after a level barrier the upstream values come
-// from shared memory.  A position p is still in the ring during the level
-// [j0, j1) whenever p >= j1 - W: no position written in this level maps to
-// its slot.  W is a power of two.  Older and lagged upstream values are read
-// from global memory.
+// x and x_old are e_curr / e_prev ([band][n_dir][Np]).  Thread t serves band
+// t mod gp (gp = the power of two >= the block's band count, which divides
+// the block size) at positions t / gp, t / gp + blockDim / gp, ... of each
+// level, so each thread's band -- and its row pointers -- are fixed.  Each
+// thread's first item of the next two levels is loaded ahead (everything but
+// the upstream values), and the block keeps its last W solved positions per
+// band in a shared-memory ring, so after a level barrier the upstream values
+// come from shared memory.  A position p is still in the ring during the
+// level [j0, j1) whenever p >= j1 - W: no position written in this level maps
+// to its slot.  W is a power of two.  Older and lagged upstream values are
+// read from global memory.
 // At most 128 threads, 5 blocks per SM (<= 96 registers, no spills): 640
 // blocks of the 40-band, 32-direction workload fit in one wave.
 // MARGIN (acyclic plans: one sweep is the exact solve): the block also sums
@@ -399,36 +411,58 @@ __global__ void __launch_bounds__(128, 5) k_sweep(SweepPlan sp, const double* __
     const int g0 = blockIdx.x * G;
     const int gn = min(G, nbb - g0);
     if (gn <= 0) return;
+    int gp = 1;
+    while (gp < gn) gp <<= 1;
+    const int sh = __ffs(gp) - 1;
+    const int bl = threadIdx.x & (gp - 1);
+    const bool serves = bl < gn;  // threads of a padded band slot only load
+    const int b = b0 + g0 + (serves ? bl : 0);
+    const int n = sp.n;
+    const size_t sys = (size_t)b * n_dir + d;
+    SweepRows rows;
+    rows.cell = sp.cell + (size_t)d * n;
+    rows.bidx = sp.bidx + (size_t)d * n;
+    rows.nb = sp.nb + (size_t)d * sp.F * n;
+    rows.fc = sp.fc + (size_t)d * sp.F * n;
+    rows.voi = voi + sys * n;
+    rows.kinv = kinv + sys * n;
+    rows.eb = src.ebar + (size_t)b * Np;
+    rows.bs = src.bsum + ((size_t)d * nbb + (b - b0)) * src.nbcell;
+    rows.xold = src.x_old + sys * Np;
+    rows.n = n;
+    rows.F = sp.F;
+    double* xb = x + sys * Np;
+    double* rg = ring + (size_t)bl * W;
+    const int* cell_d = rows.cell;
+    const int per_round = blockDim.x >> sh;  // positions per round of the block
+    const int tpos = threadIdx.x >> sh;      // this thread's first position in a level
     const int L0 = sp.lvl_off[d], L1 = sp.lvl_off[d + 1] - 1;  // levels L0 .. L1-1
-    const int* cell_d = sp.cell + (size_t)d * sp.n;
     SweepItem p1, p2;  // this thread's first item of levels l and l+1
     bool h1 = false, h2 = false;
     double msum = 0.0;
     auto pre = [&](int l, SweepItem& dst) -> bool {
         if (l >= L1) return false;
-        const int j0 = sp.lvl[l];
-        if (threadIdx.x >= (sp.lvl[l + 1] - j0) * gn) return false;
-        sweep_load_a(sp, voi, kinv, d, j0 + threadIdx.x / gn, b0 + g0 + threadIdx.x % gn, n_dir, dst);
+        const int j = sp.lvl[l] + tpos;
+        if (j >= sp.lvl[l + 1]) return false;
+        sweep_load_a(rows, j, dst);
         return true;
     };
     h1 = pre(L0, p1);
-    if (h1) sweep_load_b<MARGIN>(src, d, n_dir, nbb, b0, Np, p1);
+    if (h1) sweep_load_b<MARGIN>(rows, p1);
     h2 = pre(L0 + 1, p2);
     for (int l = L0; l < L1; ++l) {
         const int j0 = sp.lvl[l], j1 = sp.lvl[l + 1];
-        const int items = (j1 - j0) * gn;
         const int keep = j1 - W;  // oldest position still readable from the ring
-        for (int it = threadIdx.x; it < items; it += blockDim.x) {
+        bool first = true;
+        for (int j = j0 + tpos; j < j1; j += per_round) {
             SweepItem cur;
-            const int j = j0 + it / gn;
-            const int bl = it % gn;
-            if (it == threadIdx.x && h1) cur = p1;
+            if (first && h1) cur = p1;
             else {
-                sweep_load_a(sp, voi, kinv, d, j, b0 + g0 + bl, n_dir, cur);
-                sweep_load_b<MARGIN>(src, d, n_dir, nbb, b0, Np, cur);
+                sweep_load_a(rows, j, cur);
+                sweep_load_b<MARGIN>(rows, cur);
             }
-            double* xb = x + ((size_t)cur.b * n_dir + d) * Np;
-            double* rg = ring + (size_t)bl * W;
+            first = false;
+            if (!serves) continue;
             double off = 0.0;
 #pragma unroll
             for (int f = 0; f < 4; ++f) {
@@ -438,7 +472,7 @@ __global__ void __launch_bounds__(128, 5) k_sweep(SweepPlan sp, const double* __
                 if (u >= 0) xu = u >= keep ? rg[u & (W - 1)] : xb[cell_d[u]];
                 else {  // lagged (u = -2 - position): previous sweep's value (or the previous outer iterate)
                     const int cu = cell_d[-u - 2];
-                    xu = first_sweep ? src.x_old[((size_t)cur.b * n_dir + d) * Np + cu] : xb[cu];
+                    xu = first_sweep ? rows.xold[cu] : xb[cu];
                 }
                 off = fma(cur.cf[f], xu, off);
             }
@@ -452,7 +486,7 @@ __global__ void __launch_bounds__(128, 5) k_sweep(SweepPlan sp, const double* __
         }
         p1 = p2;
         h1 = h2;
-        if (h1) sweep_load_b<MARGIN>(src, d, n_dir, nbb, b0, Np, p1);
+        if (h1) sweep_load_b<MARGIN>(rows, p1);
         h2 = pre(l + 2, p2);
         __syncthreads();
     }

@@ -970,6 +970,22 @@ static int sweep_ring(int G) {
 }
 static size_t sweep_smem(int G) { return sizeof(double) * (size_t)G * sweep_ring(G); }
 
+// k_sweep for the mesh's faces per cell (2 in 1D, 3 in 2D, 4 in 3D).
+template <bool MARGIN>
+static void launch_sweep(int F, dim3 grid, int threads, size_t smem, cudaStream_t st, const bte::SweepPlan& sp,
+                         const double* voi, const double* kinv, const bte::SweepSrc& src, double* x, int first_sweep,
+                         int G, int W, int nbb, int b0, int n_band, int n_dir, size_t Np, double* mpart) {
+    if (F == 2)
+        bte::k_sweep<MARGIN, 2><<<grid, threads, smem, st>>>(sp, voi, kinv, src, x, first_sweep, G, W, nbb, b0, n_band,
+                                                             n_dir, Np, mpart);
+    else if (F == 3)
+        bte::k_sweep<MARGIN, 3><<<grid, threads, smem, st>>>(sp, voi, kinv, src, x, first_sweep, G, W, nbb, b0, n_band,
+                                                             n_dir, Np, mpart);
+    else
+        bte::k_sweep<MARGIN, 4><<<grid, threads, smem, st>>>(sp, voi, kinv, src, x, first_sweep, G, W, nbb, b0, n_band,
+                                                             n_dir, Np, mpart);
+}
+
 // Solve all systems of one batch by upwind sweeps (exact in one sweep when no
 // edge is lagged; otherwise Gauss-Seidel sweeps until ||R - A x|| <= inner_tol ||R||).
 static bte_status solve_batch_sweep(bte_ctx* ctx, int b0, int nbb, const bte_options& o, bte_report& rep) {
@@ -1020,9 +1036,9 @@ static bte_status solve_batch_sweep(bte_ctx* ctx, int b0, int nbb, const bte_opt
         for (int k = 0; k < ncand; ++k) {
             const int Gk = std::max(1, std::min(cand[k][0], nbb));
             BTE_CUDA(cudaEventRecord(e0, st));
-            bte::k_sweep<false><<<dim3((nbb + Gk - 1) / Gk, ctx->n_dir), cand[k][1], sweep_smem(Gk), st>>>(
-                sp, ctx->p_voi.as<double>(), ctx->p_kinv.as<double>(), ssrc, ctx->e_curr, 1, Gk, sweep_ring(Gk), nbb,
-                b0, ctx->n_band, ctx->n_dir, ctx->Np, nullptr);
+            launch_sweep<false>(ctx->F, dim3((nbb + Gk - 1) / Gk, ctx->n_dir), cand[k][1], sweep_smem(Gk), st, sp,
+                                ctx->p_voi.as<double>(), ctx->p_kinv.as<double>(), ssrc, ctx->e_curr, 1, Gk,
+                                sweep_ring(Gk), nbb, b0, ctx->n_band, ctx->n_dir, ctx->Np, nullptr);
             BTE_LAUNCHED();
             BTE_CUDA(cudaEventRecord(e1, st));
             BTE_CUDA(cudaEventSynchronize(e1));
@@ -1049,14 +1065,16 @@ static bte_status solve_batch_sweep(bte_ctx* ctx, int b0, int nbb, const bte_opt
     for (;;) {
         if (margin) {
             BTE_LAUNCH(KK_SWEEP, -1, sweep_bytes, 0,
-                       bte::k_sweep<true><<<sgrid, ctx->sweep_threads, sweep_smem(G), st>>>(
-                           sp, ctx->p_voi.as<double>(), ctx->p_kinv.as<double>(), ssrc, ctx->e_curr, 1, G,
-                           sweep_ring(G), nbb, b0, ctx->n_band, ctx->n_dir, ctx->Np, ctx->d_spart.as<double>()));
+                       launch_sweep<true>(ctx->F, sgrid, ctx->sweep_threads, sweep_smem(G), st, sp,
+                                          ctx->p_voi.as<double>(), ctx->p_kinv.as<double>(), ssrc, ctx->e_curr, 1, G,
+                                          sweep_ring(G), nbb, b0, ctx->n_band, ctx->n_dir, ctx->Np,
+                                          ctx->d_spart.as<double>()));
         } else {
             BTE_LAUNCH(KK_SWEEP, -1, sweep_bytes, 0,
-                       bte::k_sweep<false><<<sgrid, ctx->sweep_threads, sweep_smem(G), st>>>(
-                           sp, ctx->p_voi.as<double>(), ctx->p_kinv.as<double>(), ssrc, ctx->e_curr, sweeps == 0, G,
-                           sweep_ring(G), nbb, b0, ctx->n_band, ctx->n_dir, ctx->Np, nullptr));
+                       launch_sweep<false>(ctx->F, sgrid, ctx->sweep_threads, sweep_smem(G), st, sp,
+                                           ctx->p_voi.as<double>(), ctx->p_kinv.as<double>(), ssrc, ctx->e_curr,
+                                           sweeps == 0, G, sweep_ring(G), nbb, b0, ctx->n_band, ctx->n_dir, ctx->Np,
+                                           nullptr));
         }
         ++sweeps;
         if (ctx->plan_lagged_dirs == 0) break;

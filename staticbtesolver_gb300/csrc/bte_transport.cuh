@@ -310,11 +310,13 @@ __global__ void k_sweep_invd(SweepPlan sp, const double* __restrict__ kb, int n_
     }
 }
 
-// Operands of one sweep item that do not depend on the level being solved.
+// Operands of one sweep item that do not depend on the level being solved
+// (FM = faces per cell: 2, 3 or 4).
+template <int FM>
 struct SweepItem {
     int c, bi;
-    int u[4];
-    double cf[4];
+    int u[FM];
+    double cf[FM];
     double kinv, voi, eb, bs, old;
 };
 
@@ -343,17 +345,13 @@ struct SweepRows {
 };
 
 // Stage A: everything addressed by the position j alone.
-__device__ __forceinline__ void sweep_load_a(const SweepRows& r, int j, SweepItem& it) {
+template <int FM>
+__device__ __forceinline__ void sweep_load_a(const SweepRows& r, int j, SweepItem<FM>& it) {
     it.c = r.cell[j];
 #pragma unroll
-    for (int f = 0; f < 4; ++f) {
-        if (f < r.F) {
-            it.u[f] = r.nb[f * r.n + j];
-            it.cf[f] = r.fc[f * r.n + j];
-        } else {
-            it.u[f] = -1;
-            it.cf[f] = 0.0;
-        }
+    for (int f = 0; f < FM; ++f) {
+        it.u[f] = r.nb[f * r.n + j];
+        it.cf[f] = r.fc[f * r.n + j];
     }
     it.kinv = r.kinv[j];
     it.voi = r.voi[j];
@@ -362,8 +360,8 @@ __device__ __forceinline__ void sweep_load_a(const SweepRows& r, int j, SweepIte
 
 // Stage B: what is addressed by the cell, issued a level after stage A so the
 // cell index has arrived and the loads do not stall the sweep.
-template <bool MARGIN>
-__device__ __forceinline__ void sweep_load_b(const SweepRows& r, SweepItem& it) {
+template <bool MARGIN, int FM>
+__device__ __forceinline__ void sweep_load_b(const SweepRows& r, SweepItem<FM>& it) {
     it.eb = r.eb[it.c];
     it.bs = it.bi >= 0 ? r.bs[it.bi] : 0.0;
     if (MARGIN) it.old = r.xold[it.c];
@@ -400,7 +398,7 @@ __device__ __forceinline__ double block_sum_any(double v, double* smem /* [32] *
 // MARGIN (acyclic plans: one sweep is the exact solve): the block also sums
 // (x - x_old)^2 over its items, in a fixed order, into
 // mpart[d * n_band + b0 + blockIdx.x * G], the outer iteration's margin partial.
-template <bool MARGIN>
+template <bool MARGIN, int FM>
 __global__ void __launch_bounds__(128, 5) k_sweep(SweepPlan sp, const double* __restrict__ voi,
                                                   const double* __restrict__ kinv, SweepSrc src, double* x,
                                                   int first_sweep, int G, int W, int nbb, int b0, int n_band,
@@ -437,10 +435,10 @@ __global__ void __launch_bounds__(128, 5) k_sweep(SweepPlan sp, const double* __
     const int per_round = blockDim.x >> sh;  // positions per round of the block
     const int tpos = threadIdx.x >> sh;      // this thread's first position in a level
     const int L0 = sp.lvl_off[d], L1 = sp.lvl_off[d + 1] - 1;  // levels L0 .. L1-1
-    SweepItem p1, p2;  // this thread's first item of levels l and l+1
+    SweepItem<FM> p1, p2;  // this thread's first item of levels l and l+1
     bool h1 = false, h2 = false;
     double msum = 0.0;
-    auto pre = [&](int l, SweepItem& dst) -> bool {
+    auto pre = [&](int l, SweepItem<FM>& dst) -> bool {
         if (l >= L1) return false;
         const int j = sp.lvl[l] + tpos;
         if (j >= sp.lvl[l + 1]) return false;
@@ -448,24 +446,24 @@ __global__ void __launch_bounds__(128, 5) k_sweep(SweepPlan sp, const double* __
         return true;
     };
     h1 = pre(L0, p1);
-    if (h1) sweep_load_b<MARGIN>(rows, p1);
+    if (h1) sweep_load_b<MARGIN, FM>(rows, p1);
     h2 = pre(L0 + 1, p2);
     for (int l = L0; l < L1; ++l) {
         const int j0 = sp.lvl[l], j1 = sp.lvl[l + 1];
         const int keep = j1 - W;  // oldest position still readable from the ring
         bool first = true;
         for (int j = j0 + tpos; j < j1; j += per_round) {
-            SweepItem cur;
+            SweepItem<FM> cur;
             if (first && h1) cur = p1;
             else {
                 sweep_load_a(rows, j, cur);
-                sweep_load_b<MARGIN>(rows, cur);
+                sweep_load_b<MARGIN, FM>(rows, cur);
             }
             first = false;
             if (!serves) continue;
             double off = 0.0;
 #pragma unroll
-            for (int f = 0; f < 4; ++f) {
+            for (int f = 0; f < FM; ++f) {
                 const int u = cur.u[f];
                 if (u == -1) continue;
                 double xu;
@@ -486,7 +484,7 @@ __global__ void __launch_bounds__(128, 5) k_sweep(SweepPlan sp, const double* __
         }
         p1 = p2;
         h1 = h2;
-        if (h1) sweep_load_b<MARGIN>(rows, p1);
+        if (h1) sweep_load_b<MARGIN, FM>(rows, p1);
         h2 = pre(l + 2, p2);
         __syncthreads();
     }

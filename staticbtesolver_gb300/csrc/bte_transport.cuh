@@ -438,28 +438,30 @@ __global__ void __launch_bounds__(128, 5) k_sweep(SweepPlan sp, const double* __
     SweepItem<FM> p1, p2;  // this thread's first item of levels l and l+1
     bool h1 = false, h2 = false;
     double msum = 0.0;
-    auto pre = [&](int l, SweepItem<FM>& dst) -> bool {
-        if (l >= L1) return false;
-        const int j = sp.lvl[l] + tpos;
-        if (j >= sp.lvl[l + 1]) return false;
+    // level bounds carried from level to level: lA, lB, lC = starts of levels
+    // l, l+1, l+2 (the last start is n), so a level begins without a load
+    const int* lvl = sp.lvl;
+    int lA = lvl[L0], lB = lvl[L0 + 1], lC = L0 + 2 <= L1 ? lvl[L0 + 2] : lB;
+    auto pre = [&](int j_begin, int j_end, SweepItem<FM>& dst) -> bool {
+        const int j = j_begin + tpos;
+        if (j >= j_end) return false;
         sweep_load_a(rows, j, dst);
         return true;
     };
-    h1 = pre(L0, p1);
+    h1 = pre(lA, lB, p1);
     if (h1) sweep_load_b<MARGIN, FM>(rows, p1);
-    h2 = pre(L0 + 1, p2);
+    h2 = L0 + 1 < L1 && pre(lB, lC, p2);
     for (int l = L0; l < L1; ++l) {
-        const int j0 = sp.lvl[l], j1 = sp.lvl[l + 1];
+        const int j0 = lA, j1 = lB;
+        const int lD = l + 3 <= L1 ? lvl[l + 3] : lC;  // for the prefetch of level l+2, issued now
         const int keep = j1 - W;  // oldest position still readable from the ring
-        bool first = true;
         for (int j = j0 + tpos; j < j1; j += per_round) {
             SweepItem<FM> cur;
-            if (first && h1) cur = p1;
+            if (j == j0 + tpos && h1) cur = p1;
             else {
                 sweep_load_a(rows, j, cur);
                 sweep_load_b<MARGIN, FM>(rows, cur);
             }
-            first = false;
             if (!serves) continue;
             double off = 0.0;
 #pragma unroll
@@ -485,7 +487,10 @@ __global__ void __launch_bounds__(128, 5) k_sweep(SweepPlan sp, const double* __
         p1 = p2;
         h1 = h2;
         if (h1) sweep_load_b<MARGIN, FM>(rows, p1);
-        h2 = pre(l + 2, p2);
+        h2 = l + 2 < L1 && pre(lC, lD, p2);
+        lA = lB;
+        lB = lC;
+        lC = lD;
         __syncthreads();
     }
     if (MARGIN) {

@@ -1329,7 +1329,8 @@ extern "C" bte_status bte_solve(bte_ctx* ctx, const bte_options* opts, bte_repor
                                ctx->n, ND, Np, ctx->d_Tb.as<double>(), ctx->d_mpart.as<double>()));
             }
             BTE_LAUNCH(KK_REDUCE, -1, (2.0 * NB + 1) * ctx->n * 8.0, 0,
-                       bte::k_recover<<<(ctx->n + 255) / 256, 256, 0, st>>>(
+                       bte::k_recover<<<(ctx->n + bte::RC_CELLS - 1) / bte::RC_CELLS, bte::RC_CELLS * bte::RC_SLICES,
+                                        0, st>>>(
                            ctx->d_Tb.as<double>(), ctx->d_Cb.as<double>(), ctx->d_Lr.as<double>(), Lr_sum, ctx->T_ref,
                            ctx->solid_angle, ctx->n, NB, Np, ctx->d_T.as<double>(), ctx->d_ebar.as<double>()));
             // margin = sum of the partials / (n_band n_cell), fixed order

@@ -193,17 +193,35 @@ __global__ void __launch_bounds__(THREADS) k_reduce(const double* __restrict__ e
 }
 
 // src/StaticBTESolver.cpp:106-120: T[c] = sum_b Lr_b Tb[b][c] / sum_b Lr_b and
-// ebar[b][c] = C_b / Omega_tot (T[c] - T_ref).
-__global__ void k_recover(const double* __restrict__ Tb, const double* __restrict__ Cb, const double* __restrict__ Lr,
-                          double Lr_sum, double T_ref, double solid_angle, int n, int n_band, size_t Np, double* T,
-                          double* ebar) {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= n) return;
-    double tacc = 0.0;
-    for (int b = 0; b < n_band; ++b) tacc += Lr[b] * Tb[(size_t)b * Np + c];
-    const double Tc = tacc / Lr_sum;
-    T[c] = Tc;
-    for (int b = 0; b < n_band; ++b) ebar[(size_t)b * Np + c] = Cb[b] / solid_angle * (Tc - T_ref);
+// ebar[b][c] = C_b / Omega_tot (T[c] - T_ref).  A block covers 32 cells with
+// 8 band slices (thread (x, y): cell x, bands y, y + 8, ...), so every load and
+// store is coalesced along the cells and the grid has n / 32 blocks; the 8
+// slice sums are added in slice order.
+constexpr int RC_CELLS = 32, RC_SLICES = 8;
+__global__ void __launch_bounds__(RC_CELLS * RC_SLICES)
+    k_recover(const double* __restrict__ Tb, const double* __restrict__ Cb, const double* __restrict__ Lr,
+              double Lr_sum, double T_ref, double solid_angle, int n, int n_band, size_t Np, double* T,
+              double* ebar) {
+    __shared__ double part[RC_SLICES][RC_CELLS];
+    __shared__ double tc[RC_CELLS];
+    const int x = threadIdx.x % RC_CELLS, y = threadIdx.x / RC_CELLS;
+    const int c = blockIdx.x * RC_CELLS + x;
+    double acc = 0.0;
+    if (c < n)
+        for (int b = y; b < n_band; b += RC_SLICES) acc += Lr[b] * Tb[(size_t)b * Np + c];
+    part[y][x] = acc;
+    __syncthreads();
+    if (y == 0) {
+        double t = 0.0;
+        for (int k = 0; k < RC_SLICES; ++k) t += part[k][x];
+        tc[x] = t / Lr_sum;
+        if (c < n) T[c] = tc[x];
+    }
+    __syncthreads();
+    if (c < n) {
+        const double Tc = tc[x];
+        for (int b = y; b < n_band; b += RC_SLICES) ebar[(size_t)b * Np + c] = Cb[b] / solid_angle * (Tc - T_ref);
+    }
 }
 
 // margin = sum of partials / (n_band n_cell).  One block: thread t sums

@@ -1142,7 +1142,8 @@ static bte_status anderson_step(bte_ctx* ctx, int slots, int& count, int& next, 
                                                            ctx->d_aa_x.as<double>(), L, slot, mx,
                                                            ctx->d_aa_g.as<double>(), ctx->d_aa_f.as<double>(),
                                                            ctx->d_aa_part.as<double>()));
-    M::k_aa_row<<<1, 32, 0, st>>>(ctx->d_aa_part.as<double>(), nblk, slot, mx, ctx->d_aa_gram.as<double>());
+    M::k_aa_row<<<1, 32 * M::AA_MAX, 0, st>>>(ctx->d_aa_part.as<double>(), nblk, slot, mx,
+                                               ctx->d_aa_gram.as<double>());
     BTE_LAUNCHED();
     const int k = count;
     if (k < 2) return BTE_OK;  // nothing to mix yet
@@ -1151,10 +1152,14 @@ static bte_status anderson_step(bte_ctx* ctx, int slots, int& count, int& next, 
     M::k_aa_solve<<<1, 32, 0, st>>>(ctx->d_aa_gram.as<double>(), mx, ctx->d_aa_alpha.as<double>(),
                                    ctx->d_aa_flag.as<double>());
     BTE_LAUNCHED();
-    BTE_LAUNCH(KK_REDUCE, -1, ((double)k + 1) * L * 8.0 + (double)ctx->n_band * n * 8.0, 0,
+    BTE_LAUNCH(KK_REDUCE, -1, ((double)k + 1) * L * 8.0, 0,
                M::k_aa_mix<<<gl, 256, 0, st>>>(as, ctx->d_aa_g.as<double>(), L, mx, ctx->d_aa_alpha.as<double>(),
                                                 ctx->T_ref, ctx->d_T.as<double>(), ctx->d_ebar.as<double>(),
                                                 ctx->e_curr));
+    BTE_LAUNCH(KK_REDUCE, -1, (double)(ctx->n_band + 1) * n * 8.0, 0,
+               M::k_ebar_from_T<<<dim3((n + 255) / 256, ctx->n_band), 256, 0, st>>>(
+                   ctx->d_T.as<double>(), ctx->d_Cb.as<double>(), ctx->solid_angle, ctx->T_ref, n, ctx->Np,
+                   ctx->d_ebar.as<double>()));
     ++rep.accel_steps;
     return BTE_OK;
 }
@@ -1303,7 +1308,7 @@ extern "C" bte_status bte_solve(bte_ctx* ctx, const bte_options* opts, bte_repor
             if (ctx->ndiff > 0) {
                 const int nt = ctx->ndiff * NB;
                 BTE_LAUNCH(KK_DIFFUSE, -1, (double)nt * (ND + 1) * 8.0, 0,
-                           bte::k_diffuse_wall<<<(nt + 127) / 128, 128, 0, st>>>(
+                           bte::k_diffuse_wall<<<(nt + 3) / 4, 128, 0, st>>>(
                                ctx->e_prev, ctx->d_dlist.as<int>(), ctx->d_bf_cell.as<int>(), ctx->d_wdiff.as<double>(),
                                ctx->d_wden.as<double>(), ctx->ndiff, NB, ND, Np, ctx->nbf, ctx->d_ediff.as<double>()));
             }

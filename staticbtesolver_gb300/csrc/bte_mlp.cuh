@@ -545,7 +545,7 @@ struct AaMix {
 // part[i][block] for mx.slot[i].  AA_BLOCKS blocks (a constant, so the order
 // does not depend on the device).  Only the newest row of the Gram matrix is
 // computed: the others do not change.
-constexpr int AA_BLOCKS = 304;
+constexpr int AA_BLOCKS = 1216;
 __global__ void __launch_bounds__(AA_THREADS) k_aa_push(AaState a, const double* __restrict__ T,
                                                         const double* __restrict__ e, const double* __restrict__ x,
                                                         size_t stride, int slot, AaMix mx, double* g, double* f,
@@ -588,75 +588,142 @@ __global__ void __launch_bounds__(AA_THREADS) k_aa_push(AaState a, const double*
     }
 }
 
-// One block: the newest Gram row, G[slot][s] = G[s][slot] = sum over blocks of
-// the partials (block order), into the persistent slot-indexed matrix G.
+// The newest Gram row, G[slot][s] = G[s][slot] = sum over blocks of the
+// partials, into the persistent slot-indexed matrix G.  One warp per stored
+// slot: lane l sums blocks l, l+32, ... in order, then a fixed butterfly.
 __global__ void k_aa_row(const double* __restrict__ part, int nblk, int slot, AaMix mx, double* G) {
-    const int i = threadIdx.x;
+    const int i = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (i >= mx.k) return;
     double t = 0.0;
-    for (int b = 0; b < nblk; ++b) t += part[(size_t)i * nblk + b];
-    G[slot * AA_MAX + mx.slot[i]] = t;
-    G[mx.slot[i] * AA_MAX + slot] = t;
+    for (int b = lane; b < nblk; b += 32) t += part[(size_t)i * nblk + b];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (lane == 0) {
+        G[slot * AA_MAX + mx.slot[i]] = t;
+        G[mx.slot[i] * AA_MAX + slot] = t;
+    }
 }
 
-// One thread: alpha = G^-1 1 / (1^T G^-1 1) over the stored slots (Gram
-// matrix indexed by slot, AA_MAX x AA_MAX), Tikhonov 1e-12 max(diag), Gaussian
-// elimination with partial pivoting.  If the weights are not finite or one
-// exceeds 1e3 the newest iterate is taken alone (alpha = e_k) and *flag = 1
-// asks the host to restart the history.
+// One warp: alpha = G^-1 1 / (1^T G^-1 1) over the stored slots (Gram matrix
+// indexed by slot, AA_MAX x AA_MAX), Tikhonov 1e-12 max(diag), Gaussian
+// elimination with partial pivoting (the first row of largest |pivot|); lane
+// r holds row r.  If the weights are not finite or one exceeds 1e3 the newest
+// iterate is taken alone (alpha = e_k) and *flag = 1 asks the host to restart
+// the history.
 __global__ void k_aa_solve(const double* __restrict__ Gs, AaMix mx, double* alpha, double* flag) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const int lane = threadIdx.x;
+    if (blockIdx.x != 0 || lane >= 32) return;
     const int k = mx.k;
-    double G[AA_MAX][AA_MAX + 1];
-    double dmax = 0.0;
-    for (int i = 0; i < k; ++i)
-        for (int j = 0; j < k; ++j) {
-            G[i][j] = Gs[mx.slot[i] * AA_MAX + mx.slot[j]];
-            if (i == j) dmax = fmax(dmax, G[i][i]);
-        }
+    double row[AA_MAX + 1];
+    double diag = 0.0;
+#pragma unroll
+    for (int j = 0; j <= AA_MAX; ++j) row[j] = 0.0;
+    if (lane < k) {
+#pragma unroll
+        for (int j = 0; j < AA_MAX; ++j)
+            if (j < k) row[j] = Gs[mx.slot[lane] * AA_MAX + mx.slot[j]];
+#pragma unroll
+        for (int j = 0; j < AA_MAX; ++j)
+            if (j == lane) diag = row[j];
+    }
+    double dmax = diag;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) dmax = fmax(dmax, __shfl_xor_sync(0xffffffffu, dmax, o));
     bool ok = dmax > 0.0 && dmax < 1e300;
-    for (int i = 0; i < k; ++i) {
-        G[i][i] += 1e-12 * dmax;
-        G[i][k] = 1.0;
+    if (lane < k) {
+#pragma unroll
+        for (int j = 0; j < AA_MAX; ++j)
+            if (j == lane) row[j] += 1e-12 * dmax;
+#pragma unroll
+        for (int j = 0; j <= AA_MAX; ++j)
+            if (j == k) row[j] = 1.0;
     }
-    for (int c = 0; ok && c < k; ++c) {
-        int piv = c;
-        for (int r = c + 1; r < k; ++r)
-            if (fabs(G[r][c]) > fabs(G[piv][c])) piv = r;
-        if (piv != c)
-            for (int j = 0; j <= k; ++j) {
-                const double t = G[c][j];
-                G[c][j] = G[piv][j];
-                G[piv][j] = t;
-            }
-        if (G[c][c] == 0.0) {
-            ok = false;
-            break;
+#pragma unroll
+    for (int c = 0; c < AA_MAX; ++c) {
+        if (c >= k) break;
+        // pivot: the lowest row r >= c with the largest |G[r][c]|
+        double colv = 0.0;
+#pragma unroll
+        for (int j = 0; j < AA_MAX; ++j)
+            if (j == c) colv = row[j];
+        double best = (lane >= c && lane < k) ? fabs(colv) : -1.0;
+        int piv = lane;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+            const int op = __shfl_xor_sync(0xffffffffu, piv, o);
+            if (ob > best || (ob == best && op < piv)) { best = ob; piv = op; }
         }
-        for (int r = c + 1; r < k; ++r) {
-            const double f = G[r][c] / G[c][c];
-            for (int j = c; j <= k; ++j) G[r][j] -= f * G[c][j];
+        // swap rows c and piv
+#pragma unroll
+        for (int j = 0; j <= AA_MAX; ++j) {
+            const double vc = __shfl_sync(0xffffffffu, row[j], c);
+            const double vp = __shfl_sync(0xffffffffu, row[j], piv);
+            if (lane == c) row[j] = vp;
+            else if (lane == piv) row[j] = vc;
+        }
+        double pr[AA_MAX + 1];
+#pragma unroll
+        for (int j = 0; j <= AA_MAX; ++j) pr[j] = __shfl_sync(0xffffffffu, row[j], c);
+        double pc = 0.0;
+#pragma unroll
+        for (int j = 0; j < AA_MAX; ++j)
+            if (j == c) pc = pr[j];
+        if (pc == 0.0) ok = false;
+        if (ok && lane > c && lane < k) {
+            double rc = 0.0;
+#pragma unroll
+            for (int j = 0; j < AA_MAX; ++j)
+                if (j == c) rc = row[j];
+            const double f = rc / pc;
+#pragma unroll
+            for (int j = 0; j <= AA_MAX; ++j)
+                if (j >= c) row[j] -= f * pr[j];
         }
     }
-    double a[AA_MAX], sum = 0.0;
+    // back substitution, row by row from the last
+    double a[AA_MAX];
+#pragma unroll
+    for (int i = 0; i < AA_MAX; ++i) a[i] = 0.0;
+    double sum = 0.0;
     if (ok) {
-        for (int r = k - 1; r >= 0; --r) {
-            double v = G[r][k];
-            for (int j = r + 1; j < k; ++j) v -= G[r][j] * a[j];
-            a[r] = v / G[r][r];
+#pragma unroll
+        for (int r = AA_MAX - 1; r >= 0; --r) {
+            if (r >= k) continue;
+            double rr[AA_MAX + 1];
+#pragma unroll
+            for (int j = 0; j <= AA_MAX; ++j) rr[j] = __shfl_sync(0xffffffffu, row[j], r);
+            double v = 0.0, rk = 0.0, rd = 0.0;
+#pragma unroll
+            for (int j = 0; j <= AA_MAX; ++j) {
+                if (j == k) rk = rr[j];
+                if (j == r) rd = rr[j];
+            }
+            v = rk;
+#pragma unroll
+            for (int j = 0; j < AA_MAX; ++j)
+                if (j > r && j < k) v -= rr[j] * a[j];
+            a[r] = v / rd;
         }
-        for (int i = 0; i < k; ++i) sum += a[i];
-        for (int i = 0; i < k; ++i) {
-            a[i] /= sum;
-            if (!(fabs(a[i]) <= 1e3)) ok = false;
+#pragma unroll
+        for (int i = 0; i < AA_MAX; ++i)
+            if (i < k) sum += a[i];
+#pragma unroll
+        for (int i = 0; i < AA_MAX; ++i) {
+            if (i < k) {
+                a[i] /= sum;
+                if (!(fabs(a[i]) <= 1e3)) ok = false;
+            }
         }
     }
-    for (int i = 0; i < k; ++i) alpha[i] = ok ? a[i] : (i == k - 1 ? 1.0 : 0.0);
-    *flag = ok ? 0.0 : 1.0;
+    if (lane == 0) {
+        for (int i = 0; i < k; ++i) alpha[i] = ok ? a[i] : (i == k - 1 ? 1.0 : 0.0);
+        *flag = ok ? 0.0 : 1.0;
+    }
 }
 
-// state = sum_i alpha_i g_i: T and ebar[b][c] = C_b / Omega_tot (T - T_ref), and
-// the boundary-cell intensities written back into e (the next iteration's e_prev).
+// state = sum_i alpha_i g_i: T and the boundary-cell intensities written back
+// into e (the next iteration's e_prev).
 __global__ void k_aa_mix(AaState a, const double* __restrict__ g, size_t stride, AaMix mx,
                          const double* __restrict__ alpha, double T_ref, double* __restrict__ T,
                          double* __restrict__ ebar, double* __restrict__ e) {
@@ -665,13 +732,20 @@ __global__ void k_aa_mix(AaState a, const double* __restrict__ g, size_t stride,
     double t = 0.0;
     for (int i = 0; i < mx.k; ++i) t = fma(alpha[i], g[(size_t)mx.slot[i] * stride + j], t);
     if (j < (size_t)a.n) {
-        T[j] = t;
-        for (int b = 0; b < a.n_band; ++b) ebar[(size_t)b * a.Np + j] = a.Cb[b] / a.solid_angle * (t - T_ref);
+        T[j] = t;  // ebar follows in k_ebar_from_T
     } else {
         double sc;
         const size_t k = a.e_index(j, sc);
         e[k] = t / sc;
     }
+}
+
+// ebar[b][c] = C_b / Omega_tot (T[c] - T_ref), coalesced along the cells (grid y = band).
+__global__ void k_ebar_from_T(const double* __restrict__ T, const double* __restrict__ Cb, double solid_angle,
+                              double T_ref, int n, size_t Np, double* __restrict__ ebar) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    const int b = blockIdx.y;
+    if (c < n) ebar[(size_t)b * Np + c] = Cb[b] / solid_angle * (T[c] - T_ref);
 }
 
 }  // namespace mlp

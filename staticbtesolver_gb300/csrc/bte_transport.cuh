@@ -139,11 +139,15 @@ __global__ void __launch_bounds__(THREADS) k_rhs(FaceFluxOp op, RhsSrc src, doub
 // Diffuse wall energy per (band, diffuse face) from the previous iterate
 // (src/StaticBTESolver.cpp:180-204): sum over outgoing directions of
 // e w / sum w, w = (S.n) Omega in 3D, S.n in 2D; 1D: sum e (s.n) Omega / pi.
+// One warp per (band, diffuse face): lane l sums directions l, l+32, ... and
+// the lanes are combined by a fixed butterfly (the order does not depend on
+// timing).
 __global__ void k_diffuse_wall(const double* __restrict__ e_prev, const int* __restrict__ dlist,  // [ndiff] -> bf
                                const int* __restrict__ bf_cell, const double* __restrict__ wdiff,  // [ndiff][n_dir]
                                const double* __restrict__ wden,  // [ndiff]
                                int ndiff, int n_band, int n_dir, size_t Np, int nbf, double* ediff) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;  // warp index: whole warps exit together
+    const int lane = threadIdx.x & 31;
     if (t >= ndiff * n_band) return;
     const int b = t / ndiff, k = t % ndiff;
     const int e = dlist[k];
@@ -151,9 +155,11 @@ __global__ void k_diffuse_wall(const double* __restrict__ e_prev, const int* __r
     const double* ep = e_prev + (size_t)b * n_dir * Np + c;
     const double* w = wdiff + (size_t)k * n_dir;
     double acc = 0.0;
-    for (int d = 0; d < n_dir; ++d)
+    for (int d = lane; d < n_dir; d += 32)
         if (w[d] != 0.0) acc += ep[(size_t)d * Np] * w[d];
-    ediff[(size_t)b * nbf + e] = acc / wden[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) ediff[(size_t)b * nbf + e] = acc / wden[k];
 }
 
 // The reductions that close an outer iteration (src/StaticBTESolver.cpp:96-104

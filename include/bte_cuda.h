@@ -76,7 +76,8 @@ typedef struct bte_options {
                              (bte_get_kernel_stats); adds event records between launches */
     int accel;            /* outer-iteration acceleration: 0 none (the reference), 1 learned
                              (the MLP set by bte_set_mlp), 2 Aitken per cell (non-learned),
-                             3 Anderson mixing of T (non-learned) */
+                             3 Anderson mixing of T and the boundary-cell intensities
+                             (non-learned) */
     int accel_every;      /* 1, 2: outer iterations between extrapolations (>= 4);
                              3: Anderson depth (1..8) */
     int keep_history;     /* nonzero: keep T after every outer iteration (bte_get_history) */
@@ -98,14 +99,15 @@ typedef struct bte_report {
     long long inner_iterations;/* BiCGSTAB iterations summed over systems */
     long long inner_unconverged;
     long long refinements;     /* FP64 refinement cycles (mixed form) */
-    double ms_total;           /* device time of the outer loop */
+    double ms_total;           /* device time of the outer loop (accelerator included) */
     double ms_rhs;             /* right-hand-side assembly */
-    double ms_inner;           /* inner solves */
-    double ms_reduce;          /* temperature / margin reductions */
+    double ms_inner;           /* inner solves (sweep form from its second iteration on: the
+                                  whole iteration, replayed as a CUDA graph) */
+    double ms_reduce;          /* temperature / margin reductions and the accelerator */
     long long kernel_launches; /* kernels this library launched during the solve */
     int sweep_group;           /* sweep form: bands per block and threads per block */
     int sweep_threads;         /* chosen by timing candidate shapes on a plan's first sweep */
-    int accel_steps;           /* outer-iteration extrapolations applied */
+    int accel_steps;           /* outer-iteration extrapolations (accel 1, 2) or mixes (3) applied */
     int accel_reverts;         /* extrapolations undone (state restored) */
 } bte_report;
 

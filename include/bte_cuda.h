@@ -109,6 +109,9 @@ typedef struct bte_report {
     int sweep_threads;         /* chosen by timing candidate shapes on a plan's first sweep */
     int accel_steps;           /* outer-iteration extrapolations (accel 1, 2) or mixes (3) applied */
     int accel_reverts;         /* extrapolations undone (state restored) */
+    int sweep_ring;            /* sweep form: solved positions kept in shared memory per band */
+    int sweep_margin;          /* sweep form, acyclic plan: 1 the sweep sums the margin, 0 the reduction
+                                  does (timed against each other with the launch shape) */
 } bte_report;
 
 /* Fill opts with the reference's defaults (max_iter 10000 as BTEcmd's -I default,
@@ -212,6 +215,13 @@ bte_status bte_mlp_train(const float* X, const float* Y, int M, int steps, int b
 
 /* Kernel statistics of the last solve run with opts->profile set; *n = entries. */
 bte_status bte_get_kernel_stats(bte_ctx* ctx, bte_kernel_stat* stats, int cap, int* n);
+
+/* The sweep autotuner's table from the first sweep of the current plan (empty
+ * when the choice came from the per-process cache): candidate k ran with
+ * group[k] bands and threads[k] threads per block and ring[k] positions per
+ * band, in ms[k] milliseconds.  Entries are written up to cap (arrays may be
+ * NULL when cap is 0); *n = candidates timed. */
+bte_status bte_get_sweep_tuning(bte_ctx* ctx, int* group, int* threads, int* ring, float* ms, int cap, int* n);
 
 /* The reference's inner-solve operator boundary (src/bicgstab.hpp:65,96,138):
  * BICGSTAB(n, maxit, tol); init(rowptr, colind, val, nnz, b); solve(x) --

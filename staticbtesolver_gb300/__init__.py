@@ -61,7 +61,8 @@ class Report(C.Structure):
                 ("inner_unconverged", C.c_longlong), ("refinements", C.c_longlong), ("ms_total", C.c_double),
                 ("ms_rhs", C.c_double), ("ms_inner", C.c_double), ("ms_reduce", C.c_double),
                 ("kernel_launches", C.c_longlong), ("sweep_group", C.c_int), ("sweep_threads", C.c_int),
-                ("accel_steps", C.c_int), ("accel_reverts", C.c_int)]
+                ("accel_steps", C.c_int), ("accel_reverts", C.c_int), ("sweep_ring", C.c_int),
+                ("sweep_margin", C.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -118,6 +119,9 @@ def _load():
     L.bte_mlp_param_count.restype = C.c_int
     L.bte_get_kernel_stats.argtypes = [vp, C.c_void_p, C.c_int, C.POINTER(C.c_int)]
     L.bte_get_kernel_stats.restype = C.c_int
+    L.bte_get_sweep_tuning.argtypes = [vp, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
+                                       C.POINTER(C.c_int)]
+    L.bte_get_sweep_tuning.restype = C.c_int
     L.bte_bicgstab_csr.argtypes = [C.c_int, _ip, _ip, _dp, C.c_int, _dp, _dp, C.c_int, C.c_double,
                                    C.POINTER(C.c_int), C.POINTER(C.c_int)]
     for fn in ("bte_create", "bte_destroy", "bte_set_geometry", "bte_set_quadrature", "bte_set_bands",
@@ -337,6 +341,19 @@ class Context:
         self._check(_cuda.bte_get_kernel_stats(self._h, C.cast(arr, C.c_void_p), 32, C.byref(n)))
         return {arr[i].name.decode(): dict(launches=arr[i].launches, ms=arr[i].ms, bytes=arr[i].bytes)
                 for i in range(n.value)}
+
+    def sweep_tuning(self):
+        """The sweep autotuner's candidates on this context's plan, as dicts
+        (bands and threads per block, ring positions per band, milliseconds);
+        empty when the shape came from the per-process cache."""
+        n = C.c_int(0)
+        self._check(_cuda.bte_get_sweep_tuning(self._h, None, None, None, None, 0, C.byref(n)))
+        m = n.value
+        cols = [np.zeros(max(m, 1), np.int32) for _ in range(3)] + [np.zeros(max(m, 1), np.float32)]
+        self._check(_cuda.bte_get_sweep_tuning(self._h, *[c.ctypes.data_as(C.c_void_p) for c in cols], m,
+                                               C.byref(n)))
+        return [dict(group=int(cols[0][k]), threads=int(cols[1][k]), ring=int(cols[2][k]), ms=float(cols[3][k]))
+                for k in range(m)]
 
     def margins(self):
         k = C.c_int(0)

@@ -12,6 +12,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -65,6 +66,14 @@ const char* kKindNames[kNumKinds] = {"bicg_p_update", "bicg_spmv1",   "bicg_s_up
 
 }  // namespace
 
+// Launch shape of the upwind sweep: bands per block, threads per block, ring
+// positions per band, dynamic shared memory.
+struct SweepShape {
+    int G = 2, threads = 128, W = 2048;
+    size_t smem = 0;
+    bool margin = false;  // acyclic plans: the sweep sums the margin partials (else k_reduce does)
+};
+
 struct bte_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -115,7 +124,7 @@ struct bte_ctx {
     // upwind sweep plan (form BTE_FORM_SWEEP)
     bool plan_ready = false;
     int plan_lagged_dirs = 0;
-    bool sweep_margin = false;  // acyclic plan: the sweep sums the margin partials (d_spart)
+    bool sweep_margin = false;  // the sweep sums the margin partials (d_spart), chosen with the launch shape
     long long plan_levels = 0;
     DevBuf p_cell, p_dg, p_vo, p_nb, p_fc, p_lvl, p_lvl_off, p_part, p_bad, p_voi, p_kinv, d_spart, p_bidx, p_binvd;
     DevBuf d_bcell, d_bidx, d_bsum;
@@ -123,11 +132,15 @@ struct bte_ctx {
     DevBuf d_aa_x, d_aa_g, d_aa_f, d_aa_part, d_aa_gram, d_aa_alpha, d_aa_flag;  // Anderson mixing
     double aa_prev_margin = 0.0;  // cells with boundary faces, cell -> row, boundary rhs per (system, row)
     int nbcell = 0;
-    // sweep launch shape (bands per block, threads per block) picked by timing
-    // the candidates on the first sweep of a plan
-    int sweep_group = 2, sweep_threads = 128;
+    // inflow faces per cell at most (the sweep's face slots)
+    int plan_fm = 2;
+    // sweep kernel and launch shape picked by timing the candidates on the
+    // first sweep of a plan
+    SweepShape sweep_shape{};
     bool sweep_tuned = false;
-    float sweep_tune_ms[16] = {};
+    std::vector<SweepShape> sweep_tune_cand;
+    std::vector<float> sweep_tune_ms;
+    float sweep_margin_ms[4] = {};  // sweep without / with the margin, k_reduce without / with it
     // profiling (opts->profile): events around each launch, resolved after a sync
     bool profile = false;
     std::vector<cudaEvent_t> ev_pool;
@@ -618,6 +631,15 @@ static bte_status setup_mixed(bte_ctx* ctx) {
     return BTE_OK;
 }
 
+// Face slots the sweep is instantiated for (2 in 1D and 2D, 3 in 3D).
+static int sweep_slots(const bte_ctx* ctx) { return std::max(2, std::min(ctx->plan_fm, 4)); }
+
+static int inflow_count(uint8_t m) {
+    int k = 0;
+    for (; m; m >>= 1) k += m & 1;
+    return k;
+}
+
 // Level order of one direction's upwind graph (Kahn's algorithm in waves).
 // mask[c] bit f: face f of c is an inflow face with a neighbour.  When no cell
 // is free the unprocessed cell with the fewest unresolved inflow edges (lowest
@@ -692,6 +714,10 @@ static bte_status build_sweep_plan(bte_ctx* ctx) {
                 level_order(n, F, &mask[(size_t)d * n], ctx->nbr.data(), perm[d], lvl[d], lag[d]);
         });
     for (auto& th : pool) th.join();
+    // the sweep's face slots: the largest inflow count of a cell
+    int fm = 0;
+    for (uint8_t m : mask) fm = std::max(fm, inflow_count(m));
+    ctx->plan_fm = fm;
     std::vector<int> h_perm((size_t)ND * n), h_pos((size_t)ND * n), h_lag((size_t)ND * F * n), h_lvl, h_off(ND + 1, 0);
     int lagged_dirs = 0;
     long long levels = 0;
@@ -744,8 +770,11 @@ static bte_status build_sweep_plan(bte_ctx* ctx) {
     }
     BTE_CUDA(cudaStreamSynchronize(st));  // d_perm / d_lag go out of scope
     ctx->sweep_tuned = false;
+    ctx->sweep_tune_cand.clear();
+    ctx->sweep_tune_ms.clear();
+    std::fill(ctx->sweep_margin_ms, ctx->sweep_margin_ms + 4, 0.f);
     ctx->plan_lagged_dirs = lagged_dirs;
-    ctx->sweep_margin = lagged_dirs == 0;
+    ctx->sweep_margin = false;  // decided with the launch shape on the first sweep
     BTE_CUDA(ctx->d_spart.alloc(sizeof(double) * ND * ctx->n_band));
     ctx->plan_levels = levels;
     ctx->plan_ready = true;
@@ -957,33 +986,61 @@ static bte_status solve_batch_mixed(bte_ctx* ctx, int b0, int nbb, const bte_opt
 }
 
 // Launch shapes chosen by the sweep's autotuner, per (device, cells, faces,
-// directions, bands per batch, levels).
-using SweepTuneKey = std::tuple<int, int, int, int, int, long long>;
-static std::mutex g_sweep_tune_mutex;
-static std::map<SweepTuneKey, std::pair<int, int>> g_sweep_tune;
+// directions, bands per batch, levels, margin restriction).
+using SweepTuneKey = std::tuple<int, int, int, int, int, long long, int>;
 
-// Shared-memory ring of the sweep: W (a power of two) positions per band, 32 KB per block.
+// BTE_SWEEP_MARGIN=1 (in the sweep) or 0 (in k_reduce) fixes where the margin
+// of an acyclic plan is summed instead of timing both (the temperatures are
+// the same to the bit either way; the margins differ by summation order).
+static int sweep_margin_restriction() {
+    const char* v = std::getenv("BTE_SWEEP_MARGIN");
+    if (!v || !*v) return -1;
+    return v[0] == '0' ? 0 : v[0] == '1' ? 1 : -1;
+}
+static std::mutex g_sweep_tune_mutex;
+static std::map<SweepTuneKey, SweepShape> g_sweep_tune;
+
+// Shared-memory ring of k_sweep: W (a power of two) positions per band, 32 KB per block.
 static int sweep_ring(int G) {
     int w = 4096;
     while (w > 256 && w * std::max(G, 1) > 4096) w >>= 1;
     return w;
 }
-static size_t sweep_smem(int G) { return sizeof(double) * (size_t)G * sweep_ring(G); }
 
-// k_sweep for the mesh's faces per cell (2 in 1D, 3 in 2D, 4 in 3D).
+// Candidates of the autotuner for batches of nbb bands: (bands per block,
+// threads); k_sweep takes at most 128 threads.
+static std::vector<SweepShape> sweep_candidates(int nbb) {
+    static const int cand[][2] = {{1, 64}, {1, 128}, {2, 64}, {2, 128}, {4, 64}, {4, 128}, {8, 128}, {16, 128}};
+    std::vector<SweepShape> out;
+    for (const auto& c : cand) {
+        SweepShape sh;
+        sh.G = std::max(1, std::min(c[0], nbb));
+        sh.threads = c[1];
+        sh.W = sweep_ring(sh.G);
+        sh.smem = sizeof(double) * (size_t)sh.G * sh.W;
+        bool dup = false;
+        for (const SweepShape& o : out) dup |= o.G == sh.G && o.threads == sh.threads;
+        if (!dup) out.push_back(sh);
+    }
+    return out;
+}
+
+// One sweep of bands b0 .. b0+nbb-1 in every direction with shape sh, for the
+// plan's face slots (2 in 1D and 2D, 3 in 3D).
 template <bool MARGIN>
-static void launch_sweep(int F, dim3 grid, int threads, size_t smem, cudaStream_t st, const bte::SweepPlan& sp,
-                         const double* voi, const double* kinv, const bte::SweepSrc& src, double* x, int first_sweep,
-                         int G, int W, int nbb, int b0, int n_band, int n_dir, size_t Np, double* mpart) {
-    if (F == 2)
-        bte::k_sweep<MARGIN, 2><<<grid, threads, smem, st>>>(sp, voi, kinv, src, x, first_sweep, G, W, nbb, b0, n_band,
-                                                             n_dir, Np, mpart);
-    else if (F == 3)
-        bte::k_sweep<MARGIN, 3><<<grid, threads, smem, st>>>(sp, voi, kinv, src, x, first_sweep, G, W, nbb, b0, n_band,
-                                                             n_dir, Np, mpart);
-    else
-        bte::k_sweep<MARGIN, 4><<<grid, threads, smem, st>>>(sp, voi, kinv, src, x, first_sweep, G, W, nbb, b0, n_band,
-                                                             n_dir, Np, mpart);
+static void launch_sweep(const bte_ctx* ctx, const SweepShape& sh, int nbb, int b0, cudaStream_t st,
+                         const bte::SweepPlan& sp, const bte::SweepSrc& src, int first_sweep, double* mpart) {
+    const dim3 grid((nbb + sh.G - 1) / sh.G, ctx->n_dir);
+    const double* voi = ctx->p_voi.as<double>();
+    const double* kinv = ctx->p_kinv.as<double>();
+    const int fm = sweep_slots(ctx);
+#define BTE_SWEEP_FM(FM)                                                                                         \
+    bte::k_sweep<MARGIN, FM><<<grid, sh.threads, sh.smem, st>>>(sp, voi, kinv, src, ctx->e_curr, first_sweep, sh.G, \
+                                                                sh.W, nbb, b0, ctx->n_band, ctx->n_dir, ctx->Np, mpart)
+    if (fm == 2) BTE_SWEEP_FM(2);
+    else if (fm == 3) BTE_SWEEP_FM(3);
+    else BTE_SWEEP_FM(4);
+#undef BTE_SWEEP_FM
 }
 
 // Solve all systems of one batch by upwind sweeps (exact in one sweep when no
@@ -1015,46 +1072,90 @@ static bte_status solve_batch_sweep(bte_ctx* ctx, int b0, int nbb, const bte_opt
     // computes the same x from the same inputs); the choice is kept per
     // process for the same device and plan shape, so a new context on the
     // same mesh does not time the candidates again
-    const SweepTuneKey tkey{ctx->device, ctx->n, ctx->F, ctx->n_dir, nbb, ctx->plan_levels};
+    const int only_margin = sweep_margin_restriction();
+    const SweepTuneKey tkey{ctx->device, ctx->n, ctx->F, ctx->n_dir, nbb, ctx->plan_levels, only_margin};
     if (!ctx->sweep_tuned) {
         std::lock_guard<std::mutex> lock(g_sweep_tune_mutex);
         auto hit = g_sweep_tune.find(tkey);
         if (hit != g_sweep_tune.end()) {
-            ctx->sweep_group = hit->second.first;
-            ctx->sweep_threads = hit->second.second;
+            ctx->sweep_shape = hit->second;
             ctx->sweep_tuned = true;
         }
     }
     if (!ctx->sweep_tuned) {
-        // (bands per block, threads); k_sweep takes at most 128 threads
-        static const int cand[][2] = {{1, 64}, {1, 128}, {2, 64}, {2, 128}, {4, 64}, {4, 128}, {8, 128}, {16, 128}};
-        const int ncand = (int)(sizeof(cand) / sizeof(cand[0]));
+        const std::vector<SweepShape> cand = sweep_candidates(nbb);
+        ctx->sweep_tune_cand = cand;
+        ctx->sweep_tune_ms.assign(cand.size(), 0.f);
         cudaEvent_t e0, e1;
         BTE_CUDA(cudaEventCreate(&e0));
         BTE_CUDA(cudaEventCreate(&e1));
         float best = 1e30f;
-        for (int k = 0; k < ncand; ++k) {
-            const int Gk = std::max(1, std::min(cand[k][0], nbb));
+        for (size_t k = 0; k < cand.size(); ++k) {
             BTE_CUDA(cudaEventRecord(e0, st));
-            launch_sweep<false>(ctx->F, dim3((nbb + Gk - 1) / Gk, ctx->n_dir), cand[k][1], sweep_smem(Gk), st, sp,
-                                ctx->p_voi.as<double>(), ctx->p_kinv.as<double>(), ssrc, ctx->e_curr, 1, Gk,
-                                sweep_ring(Gk), nbb, b0, ctx->n_band, ctx->n_dir, ctx->Np, nullptr);
+            launch_sweep<false>(ctx, cand[k], nbb, b0, st, sp, ssrc, 1, nullptr);
             BTE_LAUNCHED();
             BTE_CUDA(cudaEventRecord(e1, st));
             BTE_CUDA(cudaEventSynchronize(e1));
             float ms = 0;
             cudaEventElapsedTime(&ms, e0, e1);
             ctx->sweep_tune_ms[k] = ms;
-            if (ms < best) { best = ms; ctx->sweep_group = cand[k][0]; ctx->sweep_threads = cand[k][1]; }
+            if (ms < best) { best = ms; ctx->sweep_shape = cand[k]; }
         }
+        // where an acyclic plan sums the margin: in the sweep (one more load
+        // and two FP64 operations per cell-system, k_reduce<false>) or in
+        // k_reduce<true> (e_prev read again).  Both are timed with the chosen
+        // shape -- best of two launches each -- and the cheaper per outer
+        // iteration (batches x sweep difference against reduce difference) is kept.
+        bool fuse = false;
+        if (ctx->plan_lagged_dirs == 0) {
+            if (only_margin >= 0) fuse = only_margin == 1;
+            else {
+                auto time_best = [&](auto&& launch) -> float {
+                    float t = 1e30f;
+                    for (int r = 0; r < 2; ++r) {
+                        cudaEventRecord(e0, st);
+                        launch();
+                        cudaEventRecord(e1, st);
+                        cudaEventSynchronize(e1);
+                        float ms = 0;
+                        cudaEventElapsedTime(&ms, e0, e1);
+                        t = std::min(t, ms);
+                    }
+                    return t;
+                };
+                const SweepShape sh = ctx->sweep_shape;
+                const int NB = ctx->n_band, nred = (int)(ctx->Np / bte::THREADS);
+                const float sf = time_best([&] { launch_sweep<false>(ctx, sh, nbb, b0, st, sp, ssrc, 1, nullptr); });
+                const float sm = time_best(
+                    [&] { launch_sweep<true>(ctx, sh, nbb, b0, st, sp, ssrc, 1, ctx->d_spart.as<double>()); });
+                auto reduce = [&](bool with_margin) {
+                    if (with_margin)
+                        bte::k_reduce<true><<<dim3(nred, NB), bte::THREADS, 0, st>>>(
+                            ctx->e_curr, ctx->e_prev, ctx->d_omega.as<double>(), ctx->d_Cb.as<double>(), ctx->T_ref,
+                            ctx->n, ctx->n_dir, ctx->Np, ctx->d_Tb.as<double>(), ctx->d_mpart.as<double>());
+                    else
+                        bte::k_reduce<false><<<dim3(nred, NB), bte::THREADS, 0, st>>>(
+                            ctx->e_curr, ctx->e_prev, ctx->d_omega.as<double>(), ctx->d_Cb.as<double>(), ctx->T_ref,
+                            ctx->n, ctx->n_dir, ctx->Np, ctx->d_Tb.as<double>(), nullptr);
+                };
+                const float rm = time_best([&] { reduce(true); });
+                const float rf = time_best([&] { reduce(false); });
+                BTE_LAUNCHED();
+                const int batches = (NB + ctx->nbb - 1) / ctx->nbb;
+                fuse = batches * (sm - sf) < rm - rf;
+                ctx->sweep_margin_ms[0] = sf; ctx->sweep_margin_ms[1] = sm;
+                ctx->sweep_margin_ms[2] = rf; ctx->sweep_margin_ms[3] = rm;
+            }
+        }
+        ctx->sweep_shape.margin = fuse;
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
         ctx->sweep_tuned = true;
         std::lock_guard<std::mutex> lock(g_sweep_tune_mutex);
-        g_sweep_tune[tkey] = {ctx->sweep_group, ctx->sweep_threads};
+        g_sweep_tune[tkey] = ctx->sweep_shape;
     }
-    const int G = std::max(1, std::min(ctx->sweep_group, nbb));
-    dim3 sgrid((nbb + G - 1) / G, ctx->n_dir);
+    const SweepShape shape = ctx->sweep_shape;
+    ctx->sweep_margin = shape.margin && ctx->plan_lagged_dirs == 0;
     // algorithmic HBM bytes of a sweep per system and cell: V Omega / D and
     // k / D read, x written (and, with the fused margin, the previous iterate
     // read), plus the level-ordered geometry per direction; ebar and the
@@ -1065,16 +1166,10 @@ static bte_status solve_batch_sweep(bte_ctx* ctx, int b0, int nbb, const bte_opt
     for (;;) {
         if (margin) {
             BTE_LAUNCH(KK_SWEEP, -1, sweep_bytes, 0,
-                       launch_sweep<true>(ctx->F, sgrid, ctx->sweep_threads, sweep_smem(G), st, sp,
-                                          ctx->p_voi.as<double>(), ctx->p_kinv.as<double>(), ssrc, ctx->e_curr, 1, G,
-                                          sweep_ring(G), nbb, b0, ctx->n_band, ctx->n_dir, ctx->Np,
-                                          ctx->d_spart.as<double>()));
+                       launch_sweep<true>(ctx, shape, nbb, b0, st, sp, ssrc, 1, ctx->d_spart.as<double>()));
         } else {
             BTE_LAUNCH(KK_SWEEP, -1, sweep_bytes, 0,
-                       launch_sweep<false>(ctx->F, sgrid, ctx->sweep_threads, sweep_smem(G), st, sp,
-                                           ctx->p_voi.as<double>(), ctx->p_kinv.as<double>(), ssrc, ctx->e_curr,
-                                           sweeps == 0, G, sweep_ring(G), nbb, b0, ctx->n_band, ctx->n_dir, ctx->Np,
-                                           nullptr));
+                       launch_sweep<false>(ctx, shape, nbb, b0, st, sp, ssrc, sweeps == 0, nullptr));
         }
         ++sweeps;
         if (ctx->plan_lagged_dirs == 0) break;
@@ -1223,8 +1318,11 @@ extern "C" bte_status bte_solve(bte_ctx* ctx, const bte_options* opts, bte_repor
     };
     bte_status result = BTE_ERR_NOT_CONVERGED;
     const int nred = (int)(Np / bte::THREADS);
-    // the sweep of an acyclic plan sums the margin itself; k_reduce then reads e_curr only
-    const bool fused_margin = o.form == BTE_FORM_SWEEP && ctx->sweep_margin;
+    // the sweep of an acyclic plan may sum the margin itself (k_reduce then
+    // reads e_curr only); the choice is made with the launch shape, on the
+    // first sweep, so it is read after the sweeps of an iteration
+    auto fused_margin = [&]() { return o.form == BTE_FORM_SWEEP && ctx->sweep_margin; };
+    const bool acyclic_sweep = o.form == BTE_FORM_SWEEP && ctx->plan_lagged_dirs == 0;
     // accelerator set-up
     bool accel_on = o.accel != 0;
     int accel_last = -1;
@@ -1282,7 +1380,7 @@ extern "C" bte_status bte_solve(bte_ctx* ctx, const bte_options* opts, bte_repor
     // CUDA graphs of the sweep form's outer iteration (not with the profiler,
     // which times each launch, nor with lagged edges, whose sweeps repeat
     // under host control)
-    const bool use_graph = o.form == BTE_FORM_SWEEP && fused_margin && !ctx->profile;
+    const bool use_graph = o.form == BTE_FORM_SWEEP && ctx->plan_lagged_dirs == 0 && !ctx->profile;
     cudaGraphExec_t gexec[2] = {nullptr, nullptr};
     struct GraphGuard {
         cudaGraphExec_t* g;
@@ -1312,7 +1410,7 @@ extern "C" bte_status bte_solve(bte_ctx* ctx, const bte_options* opts, bte_repor
                                ctx->e_prev, ctx->d_dlist.as<int>(), ctx->d_bf_cell.as<int>(), ctx->d_wdiff.as<double>(),
                                ctx->d_wden.as<double>(), ctx->ndiff, NB, ND, Np, ctx->nbf, ctx->d_ediff.as<double>()));
             }
-            if (fused_margin) BTE_CUDA(cudaMemsetAsync(ctx->d_spart.p, 0, sizeof(double) * ND * NB, st));
+            if (acyclic_sweep) BTE_CUDA(cudaMemsetAsync(ctx->d_spart.p, 0, sizeof(double) * ND * NB, st));
             if (timed) BTE_CUDA(cudaEventRecord(ev[1], st));
             for (int b0 = 0; b0 < NB; b0 += ctx->nbb) {
                 const int nbb = std::min(ctx->nbb, NB - b0);
@@ -1322,7 +1420,8 @@ extern "C" bte_status bte_solve(bte_ctx* ctx, const bte_options* opts, bte_repor
                 if (s != BTE_OK) return s;
             }
             if (timed) BTE_CUDA(cudaEventRecord(ev[2], st));
-            if (fused_margin) {
+            const bool fused = fused_margin();
+            if (fused) {
                 BTE_LAUNCH(KK_REDUCE, -1, (1.0 * NB * ND + NB) * ctx->n * 8.0, 0,
                            bte::k_reduce<false><<<dim3(nred, NB), bte::THREADS, 0, st>>>(
                                ctx->e_curr, ctx->e_prev, ctx->d_omega.as<double>(), ctx->d_Cb.as<double>(), ctx->T_ref,
@@ -1339,8 +1438,8 @@ extern "C" bte_status bte_solve(bte_ctx* ctx, const bte_options* opts, bte_repor
                            ctx->d_Tb.as<double>(), ctx->d_Cb.as<double>(), ctx->d_Lr.as<double>(), Lr_sum, ctx->T_ref,
                            ctx->solid_angle, ctx->n, NB, Np, ctx->d_T.as<double>(), ctx->d_ebar.as<double>()));
             // margin = sum of the partials / (n_band n_cell), fixed order
-            bte::k_margin_final<<<1, bte::THREADS, 0, st>>>(fused_margin ? ctx->d_spart.as<double>() : ctx->d_mpart.as<double>(),
-                                                            fused_margin ? ND * NB : nred * NB, (double)NB * ctx->n,
+            bte::k_margin_final<<<1, bte::THREADS, 0, st>>>(fused ? ctx->d_spart.as<double>() : ctx->d_mpart.as<double>(),
+                                                            fused ? ND * NB : nred * NB, (double)NB * ctx->n,
                                                             ctx->d_margin.as<double>());
             BTE_LAUNCHED();
             return BTE_OK;
@@ -1506,8 +1605,10 @@ extern "C" bte_status bte_solve(bte_ctx* ctx, const bte_options* opts, bte_repor
     BTE_CUDA(cudaStreamSynchronize(st));
     if (ctx->profile) prof_resolve(ctx, nullptr, 0);
     rep.kernel_launches = ctx->launches;
-    rep.sweep_group = o.form == BTE_FORM_SWEEP ? ctx->sweep_group : 0;
-    rep.sweep_threads = o.form == BTE_FORM_SWEEP ? ctx->sweep_threads : 0;
+    rep.sweep_group = o.form == BTE_FORM_SWEEP ? ctx->sweep_shape.G : 0;
+    rep.sweep_threads = o.form == BTE_FORM_SWEEP ? ctx->sweep_shape.threads : 0;
+    rep.sweep_ring = o.form == BTE_FORM_SWEEP ? ctx->sweep_shape.W : 0;
+    rep.sweep_margin = o.form == BTE_FORM_SWEEP && ctx->sweep_margin ? 1 : 0;
     ctx->solved = true;
     if (report) *report = rep;
     if (result == BTE_ERR_NOT_CONVERGED && ctx->err.empty()) ctx->err = "max_iter reached";
@@ -1575,6 +1676,21 @@ bte_status bte_get_kernel_stats(bte_ctx* ctx, bte_kernel_stat* stats, int cap, i
     if (!ctx) return BTE_ERR_INVALID_ARGUMENT;
     for (int k = 0; k < kNumKinds && k < cap && stats; ++k) stats[k] = ctx->stats[k];
     if (n) *n = kNumKinds;
+    return BTE_OK;
+}
+
+bte_status bte_get_sweep_tuning(bte_ctx* ctx, int* group, int* threads, int* ring, float* ms, int cap, int* n) {
+    if (!ctx || cap < 0) return BTE_ERR_INVALID_ARGUMENT;
+    const int m = (int)ctx->sweep_tune_cand.size();
+    if (cap > 0 && (!group || !threads || !ring || !ms)) return BTE_ERR_INVALID_ARGUMENT;
+    for (int k = 0; k < m && k < cap; ++k) {
+        const SweepShape& c = ctx->sweep_tune_cand[k];
+        group[k] = c.G;
+        threads[k] = c.threads;
+        ring[k] = c.W;
+        ms[k] = ctx->sweep_tune_ms[k];
+    }
+    if (n) *n = m;
     return BTE_OK;
 }
 

@@ -297,10 +297,11 @@ namespace bte {
 // residual test passes.
 //
 // Sweep-ordered arrays, direction-major, position j in level order:
-//   sw_cell[d][j], sw_dg[d][j], sw_vo[d][j], sw_fc[d][f][j], and sw_nb[d][f][j]
+//   sw_cell[d][j], sw_dg[d][j], sw_vo[d][j], sw_fc[d][k][j], and sw_nb[d][k][j]
 //   = the upstream cell's POSITION in this direction's order (-1 none,
-//   -2-position for a lagged edge); levels lvl[lvl_off[d] .. lvl_off[d+1]] are
-//   start positions (the last entry is n).
+//   -2-position for a lagged edge) for the k-th inflow face of the cell (slots
+//   k = 0 .. F-1, inflow faces first in face order, the rest -1); levels
+//   lvl[lvl_off[d] .. lvl_off[d+1]] are start positions (the last entry is n).
 struct SweepPlan {
     const int* cell;
     const int* bidx;  // [n_dir][n] row of the cell in the boundary-cell list, -1 interior
@@ -422,6 +423,7 @@ __device__ __forceinline__ double block_sum_any(double v, double* smem /* [32] *
 // MARGIN (acyclic plans: one sweep is the exact solve): the block also sums
 // (x - x_old)^2 over its items, in a fixed order, into
 // mpart[d * n_band + b0 + blockIdx.x * G], the outer iteration's margin partial.
+// FM = the plan's face slots (inflow faces first).
 template <bool MARGIN, int FM>
 __global__ void __launch_bounds__(128, 5) k_sweep(SweepPlan sp, const double* __restrict__ voi,
                                                   const double* __restrict__ kinv, SweepSrc src, double* x,
@@ -592,15 +594,24 @@ __global__ void k_sweep_layout(const int* __restrict__ perm, const int* __restri
     sbidx[pj] = bidx[c];
     sdg[pj] = dg[(size_t)d * Np + c];
     svo[pj] = vo[(size_t)d * Np + c];
+    // inflow faces first, in face order (the sweep adds their terms in the
+    // same order, so the compaction does not change a bit of x); the slots
+    // after them hold -1 / 0 and the sweep is instantiated for the largest
+    // inflow count (2D triangles: 2 of 3 faces, 3D tetrahedra: 3 of 4)
+    int k = 0;
     for (int f = 0; f < F; ++f) {
         const double v = fc[((size_t)d * F + f) * Np + c];
-        const size_t q = ((size_t)d * F + f) * n + j;
+        if (v == 0.0) continue;
+        const size_t q = ((size_t)d * F + k) * n + j;
+        const int pu = pos[(size_t)d * n + nbr[(size_t)c * F + f]];
         sfc[q] = v;
-        if (v == 0.0) snb[q] = -1;
-        else {
-            const int pu = pos[(size_t)d * n + nbr[(size_t)c * F + f]];
-            snb[q] = lagged[((size_t)d * F + f) * n + c] ? -2 - pu : pu;
-        }
+        snb[q] = lagged[((size_t)d * F + f) * n + c] ? -2 - pu : pu;
+        ++k;
+    }
+    for (; k < F; ++k) {
+        const size_t q = ((size_t)d * F + k) * n + j;
+        sfc[q] = 0.0;
+        snb[q] = -1;
     }
 }
 

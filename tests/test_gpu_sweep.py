@@ -98,3 +98,35 @@ def test_sweep_with_cycles_matches_bicgstab(sbte, get_case):
     assert rs["inner_unconverged"] == 0
     assert rs["n_iter"] == rp["n_iter"]
     assert rel_l2(Ts - 300, Tp - 300) < 1e-6
+
+
+@pytest.mark.parametrize("name", ["square16_b8", "3DM2DG", "square16_b8/cycles"])
+def test_sweep_margin_placements_agree(sbte, get_case, monkeypatch, name):
+    """The margin of an acyclic plan is summed either by the sweep (one more
+    load and two FP64 operations per cell-system) or by k_reduce (e_prev read
+    again); the autotuner times both.  Forced either way the temperatures agree
+    to the bit, on 2D and 3D plans (two and three face slots), and the margins
+    to rounding (the partials are grouped differently).  With lagged edges the
+    reduction always sums it."""
+    c = get_case(name.split("/")[0])
+    runs = {}
+    for placement in ("0", "1"):
+        monkeypatch.setenv("BTE_SWEEP_MARGIN", placement)
+        if name.endswith("/cycles"):
+            ctx = sbte.Context(0).set_arrays(_rewired(sbte, c, n_swaps=10))
+            st, rep = ctx.solve(max_iter=3000, tol=1e-5, form=sbte.FORM_SWEEP)
+        else:
+            ctx = sbte.Context(0).load(sbte.Problem(*c.args()))
+            st, rep = ctx.solve(max_iter=c.max_iter, tol=1e-5, form=sbte.FORM_SWEEP)
+        runs[placement] = (st, ctx.temperature(), ctx.margins(), rep.as_dict(), ctx.sweep_tuning())
+        ctx.close()
+    (s0, T0, m0, r0, t0), (s1, T1, m1, r1, t1) = runs["0"], runs["1"]
+    assert s0 == 0 and s1 == 0
+    assert r0["sweep_margin"] == 0 and r1["sweep_margin"] == (0 if name.endswith("/cycles") else 1), (r0, r1)
+    # the autotuner's table (empty when the shape came from the per-process cache)
+    for t in t0 + t1:
+        assert t["ms"] > 0 and t["threads"] in (64, 128) and t["ring"] * t["group"] <= 4096
+    assert r0["n_iter"] == r1["n_iter"] and r0["inner_iterations"] == r1["inner_iterations"]
+    assert np.array_equal(T0, T1)
+    np.testing.assert_allclose(m0, m1, rtol=1e-12, atol=0)
+

@@ -1104,8 +1104,10 @@ static bte_status solve_batch_sweep(bte_ctx* ctx, int b0, int nbb, const bte_opt
         // where an acyclic plan sums the margin: in the sweep (one more load
         // and two FP64 operations per cell-system, k_reduce<false>) or in
         // k_reduce<true> (e_prev read again).  Both are timed with the chosen
-        // shape -- best of two launches each -- and the cheaper per outer
-        // iteration (batches x sweep difference against reduce difference) is kept.
+        // shape -- best of two launches each -- per outer iteration (batches x
+        // sweep difference against reduce difference); the sweep takes the
+        // margin only when that saves 3 % of the sweeps and reduction, so a
+        // near tie (2D meshes) does not flip between runs.
         bool fuse = false;
         if (ctx->plan_lagged_dirs == 0) {
             if (only_margin >= 0) fuse = only_margin == 1;
@@ -1142,7 +1144,7 @@ static bte_status solve_batch_sweep(bte_ctx* ctx, int b0, int nbb, const bte_opt
                 const float rf = time_best([&] { reduce(false); });
                 BTE_LAUNCHED();
                 const int batches = (NB + ctx->nbb - 1) / ctx->nbb;
-                fuse = batches * (sm - sf) < rm - rf;
+                fuse = batches * (sm - sf) < (rm - rf) - 0.03f * (batches * sf + rf);
                 ctx->sweep_margin_ms[0] = sf; ctx->sweep_margin_ms[1] = sm;
                 ctx->sweep_margin_ms[2] = rf; ctx->sweep_margin_ms[3] = rm;
             }

@@ -141,7 +141,6 @@ struct bte_ctx {
     bool sweep_tuned = false;
     std::vector<SweepShape> sweep_tune_cand;
     std::vector<float> sweep_tune_ms;
-    float sweep_margin_ms[4] = {};  // sweep without / with the margin, k_reduce without / with it
     // profiling (opts->profile): events around each launch, resolved after a sync
     bool profile = false;
     std::vector<cudaEvent_t> ev_pool;
@@ -715,7 +714,6 @@ static bte_status build_sweep_plan(bte_ctx* ctx) {
     ctx->sweep_tuned = false;
     ctx->sweep_tune_cand.clear();
     ctx->sweep_tune_ms.clear();
-    std::fill(ctx->sweep_margin_ms, ctx->sweep_margin_ms + 4, 0.f);
     ctx->plan_lagged_dirs = lagged_dirs;
     ctx->sweep_margin = false;  // decided with the launch shape on the first sweep
     BTE_CUDA(ctx->d_spart.alloc(sizeof(double) * ND * ctx->n_band));
@@ -1088,8 +1086,6 @@ static bte_status solve_batch_sweep(bte_ctx* ctx, int b0, int nbb, const bte_opt
                 BTE_LAUNCHED();
                 const int batches = (NB + ctx->nbb - 1) / ctx->nbb;
                 fuse = batches * (sm - sf) < (rm - rf) - 0.03f * (batches * sf + rf);
-                ctx->sweep_margin_ms[0] = sf; ctx->sweep_margin_ms[1] = sm;
-                ctx->sweep_margin_ms[2] = rf; ctx->sweep_margin_ms[3] = rm;
             }
         }
         ctx->sweep_shape.margin = fuse;

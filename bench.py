@@ -54,7 +54,7 @@ sys.path.insert(0, ROOT)
 METRIC = "s to converged T (<=1e-5 rel L2 vs FP64): chosen form vs plain FP64 GPU; HBM GB/s"
 UNIT = "s"
 # Outer iterations of the square20k solve to margin <= 1e-5 (same for the
-# oracle and the plain GPU form, see tests/test_gpu_full.py); the CPU legs run
+# oracle and the plain GPU form, see tests/test_full_square20k.py); the CPU legs run
 # a 2-iteration sample and scale by it.
 OUTER_ITERS = {"square20k": 198}
 
@@ -396,7 +396,9 @@ def run_ours(args, rank, world, local):
                        "T_min": float(T.min()), "T_max": float(T.max()), "kernels": per_kernel,
                        "plain_fp64_form": plain,
                        "mixed_fp32_fp64_form": mixed,
-                       "sweep_shape": {"bands_per_block": last["sweep_group"], "threads": last["sweep_threads"]},
+                       "sweep_shape": {"bands_per_block": last["sweep_group"], "threads": last["sweep_threads"],
+                                       "ring": last["sweep_ring"],
+                                       "margin_summed_in": "sweep" if last["sweep_margin"] else "k_reduce"},
                        "speedup_vs_plain_fp64": (plain["s_extrapolated"] / t_step) if plain and "s_extrapolated" in plain else None},
             "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": round(achieved, 1), "peak": peak,
                          "peak_source": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),

@@ -81,6 +81,9 @@ typedef struct bte_options {
     int accel_every;      /* 1, 2: outer iterations between extrapolations (>= 4);
                              3: Anderson depth (1..8) */
     int keep_history;     /* nonzero: keep T after every outer iteration (bte_get_history) */
+    int dsa;              /* nonzero: diffusion-synthetic acceleration of the outer iteration (below) */
+    double dsa_tol;       /* relative residual of its low-order solve (0: 1e-3) */
+    int dsa_maxit;        /* iteration limit of its low-order solve (0: 4000) */
 } bte_options;
 
 /* Per-kernel totals of the last profiled bte_solve. */
@@ -112,6 +115,9 @@ typedef struct bte_report {
     int sweep_ring;            /* sweep form: solved positions kept in shared memory per band */
     int sweep_margin;          /* sweep form, acyclic plan: 1 the sweep sums the margin, 0 the reduction
                                   does (timed against each other with the launch shape) */
+    int dsa_solves;            /* low-order corrections applied (dsa) */
+    long long dsa_iterations;  /* conjugate-gradient iterations summed over them */
+    double ms_dsa;             /* device time of the corrections (included in ms_reduce and ms_total) */
 } bte_report;
 
 /* Fill opts with the reference's defaults (max_iter 10000 as BTEcmd's -I default,
@@ -196,6 +202,23 @@ bte_status bte_get_margins(bte_ctx* ctx, double* margins, int cap, int* n);
  * small system on the host); the history restarts when the margin grows
  * tenfold or a weight exceeds 1e3.  The plain iteration's margin still
  * decides convergence. */
+/* dsa != 0 (diffusion-synthetic acceleration, no counterpart in the reference;
+ * any form, combinable with accel): after each outer iteration that has not
+ * met the tolerance, the change r = T_new - T_old of the equilibrium
+ * temperature drives one low-order diffusion solve on the same cells,
+ *   sum_f W_f (x_c - x_nb) + sum_{isothermal wall faces} W_f x_c = V_c r_c,
+ *   W_f = (A_f / Omega_tot) sum_b Lr_b L_b (G_f + L_b q_f / (4 delta_f)) / sum_b Lr_b,
+ * L_b = v_b tau_b, G_f = 1/2 sum_d |g_df| (the upwind scheme's own numerical
+ * diffusion, g = S.n), q_f = sum_d g_df (s_d.n_f), delta_f the centroid
+ * distance across the face; diffuse and specular walls are adiabatic.  The
+ * next iteration's source is T_new + x (the boundary cells' intensities,
+ * which the walls reflect, shift by C_b / Omega_tot x).  In the diffusive
+ * regime, where the source iteration's error shrinks by ~1e-6 per outer
+ * iteration, this shrinks it by ~5-10x per iteration.  The low-order solve is
+ * conjugate gradients (FP32 vectors, FP64 dot products) in one cooperative
+ * kernel; it needs at least one isothermal wall (otherwise dsa is ignored).
+ * Convergence is still the reference's margin between consecutive transport
+ * iterates, and the returned fields are the last transport iterate's. */
 int bte_mlp_param_count(void);
 bte_status bte_set_mlp(bte_ctx* ctx, const float* params);
 /* Cell centroids [n_cell][3] (used only for the accelerator's features). */
@@ -231,6 +254,16 @@ bte_status bte_bicgstab_csr(int n, const int* rowptr, const int* colind, const d
                             int nnz, const double* b, double* x, int maxit, double tol,
                             int* iterations, int* converged);
 
+/* The low-order solve of dsa on host buffers: n cells with n_face face slots,
+ * nb[f*n+c] the cell coupled to c through slot f (-1: none, or a wall held at
+ * x = 0 when W[f*n+c] > 0), W[f*n+c] >= 0 the coupling (the operator must be
+ * symmetric: W of (c, f) equals W of the slot of nb that names c).  Solves
+ * sum_f W[f][c] (x_c - x_nb) = b_c (x_nb = 0 for walls) to a relative
+ * residual tol of the Jacobi-scaled system within maxit iterations, on the
+ * current device.  iterations and relres may be NULL. */
+bte_status bte_dsa_solve(int n, int n_face, const int* nb, const double* W, const double* b, double* x,
+                         double tol, int maxit, int* iterations, double* relres);
+
 /* Allocation-free variant of bte_bicgstab_csr.  No counterpart in the
  * reference: it exists for callers that cannot allocate device memory -- code
  * whose device memory belongs to another allocator with a fixed budget, or
@@ -242,9 +275,12 @@ bte_status bte_bicgstab_csr(int n, const int* rowptr, const int* colind, const d
  * keeps until exit; it calls no cudaMalloc, cudaFree or allocating library
  * routine.  Limits: n <= 262144 unknowns, maxit <= 10000; larger values and a
  * malformed CSR return BTE_ERR_INVALID_ARGUMENT (message in bte_last_error(NULL)).
- * The first call on a device looks up the array's device address and should
+ * Every call looks up the array's device address in the current device's
+ * context (so a context recreated after cudaDeviceReset is followed); the
+ * first call on a device also loads the library's device code there and should
  * come before any stream capture.  Calls share the array: calls that overlap
- * on the GPU race.  The call returns after the solve has finished. */
+ * on the GPU race.  The call returns after the solve has finished, and after
+ * any of its kernels still queued when it fails. */
 bte_status bte_bicgstab_csr_noalloc(int n, const int* rowptr, const int* colind, const double* val,
                                     int nnz, const double* b, double* x, int maxit, double tol,
                                     void* stream, int* iterations, int* converged);

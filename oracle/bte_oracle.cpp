@@ -675,6 +675,62 @@ int oracle_run(oracle_session* s, int max_iter, double outer_tol, int inner, dou
     return it;
 }
 
+// One outer iteration (the loop body of src/StaticBTESolver.cpp:707-788) from
+// a given state: the previous energy density e_prev_in[n_band][n_dir][n_cell]
+// and the equilibrium temperature T_in[n_cell] of the source (ebar = C_b /
+// Omega_tot (T_in - T_ref), as _recover_temperature :114-118 sets it).  Writes
+// the new e (e_out, may be NULL), T (T_out) and returns the margin against
+// e_prev_in.  Used to check that a field is a fixed point of the reference's
+// iteration and to drive accelerated solves on the CPU.
+double oracle_step(oracle_session* s, const double* e_prev_in, const double* T_in, int inner, double inner_tol,
+                   int threads, double* e_out, double* T_out) {
+    const int NC = s->N_cell, NF = s->N_face;
+    const size_t ne = (size_t)s->N_band * s->N_dir * NC;
+    s->e_prev.assign(e_prev_in, e_prev_in + ne);
+    s->e_curr.assign(ne, 0.0);
+    s->Tb.assign((size_t)NC * s->N_band, 0.0);
+    s->ebar.assign((size_t)NC * s->N_band, 0.0);
+    for (int c = 0; c < NC; ++c)
+        for (int b = 0; b < s->N_band; ++b)
+            s->ebar[(size_t)c * s->N_band + b] = s->bands[b].C / s->solid_angle * (T_in[c] - s->T_ref);
+    s->T.assign(NC, 0.0);
+#ifdef _OPENMP
+    if (threads > 0) omp_set_num_threads(threads);
+#else
+    (void)threads;
+#endif
+    const int nsys = s->N_band * s->N_dir;
+    long long iters = 0, unconv = 0;
+#pragma omp parallel for schedule(dynamic, 1) reduction(+ : iters, unconv)
+    for (int k = 0; k < nsys; ++k) {
+        int b = k / s->N_dir, d = k % s->N_dir;
+        std::vector<int> rowptr(NC + 1), col((size_t)NF * NC + 1);
+        std::vector<double> val((size_t)NF * NC + 1), Re(NC);
+        s->get_Ke(b, d, rowptr.data(), col.data(), val.data());
+        s->get_Re(b, d, s->e_prev.data(), s->ebar.data(), Re.data());
+        oracle::Csr A;
+        A.n = NC;
+        A.rowptr = rowptr;
+        A.col.assign(col.begin(), col.begin() + rowptr[NC]);
+        A.val.assign(val.begin(), val.begin() + rowptr[NC]);
+        double* x = &s->e_curr[s->eidx(b, d, 0)];
+        oracle::KrylovResult r = inner == ORACLE_INNER_BICGSTAB
+                                     ? oracle::bicgstab_jacobi(A, Re.data(), x, inner_tol, 1000)
+                                     : oracle::gmres_ilu0(A, Re.data(), x, inner_tol, 1e-50, 1e5, 1000);
+        iters += r.iterations;
+        if (!r.converged) ++unconv;
+    }
+    s->solves += nsys;
+    s->inner_iters += iters;
+    s->unconverged += unconv;
+    s->reductions();
+    const double m = s->margin();
+    if (e_out) std::memcpy(e_out, s->e_curr.data(), sizeof(double) * ne);
+    std::memcpy(T_out, s->T.data(), sizeof(double) * NC);
+    s->heat_flux();
+    return m;
+}
+
 void oracle_temperature(const oracle_session* s, double* T) {
     std::memcpy(T, s->T.data(), sizeof(double) * s->T.size());
 }

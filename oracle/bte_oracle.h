@@ -52,6 +52,13 @@ void oracle_geometry(const oracle_session* s, double* volume, double* centroid, 
 int oracle_run(oracle_session* s, int max_iter, double outer_tol, int inner, double inner_tol,
                int threads, long long max_systems);
 
+// One outer iteration from a given state (e_prev_in [n_band][n_dir][n_cell], the
+// source temperature T_in [n_cell]): writes e_out (may be NULL) and T_out,
+// returns the margin against e_prev_in.  The results getters below then
+// describe this iteration.
+double oracle_step(oracle_session* s, const double* e_prev_in, const double* T_in, int inner, double inner_tol,
+                   int threads, double* e_out, double* T_out);
+
 // Results after oracle_run.
 void oracle_temperature(const oracle_session* s, double* T);          // [n_cell]
 void oracle_band_temperature(const oracle_session* s, double* Tb);    // [n_cell*n_band]

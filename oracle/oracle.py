@@ -64,6 +64,8 @@ def lib():
         L.oracle_run.restype = C.c_int
         L.oracle_run.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_int, C.c_double, C.c_int,
                                  C.c_longlong]
+        L.oracle_step.restype = C.c_double
+        L.oracle_step.argtypes = [C.c_void_p, _dp, _dp, C.c_int, C.c_double, C.c_int, C.c_void_p, _dp]
         L.oracle_temperature.argtypes = [C.c_void_p, _dp]
         L.oracle_band_temperature.argtypes = [C.c_void_p, _dp]
         L.oracle_heat_flux.argtypes = [C.c_void_p, _dp, _dp]
@@ -156,6 +158,26 @@ class Oracle:
                       Tb=Tb.reshape(self.n_cell, self.n_band), e=e,
                       inner=dict(solves=int(st[0]), iterations=int(st[1]), unconverged=int(st[2]),
                                  seconds=float(sec[0])))
+
+    def step(self, e_prev, T_src, inner=INNER_GMRES_ILU0, inner_tol=1e-9, threads=0, want_energy=True):
+        """One outer iteration of the reference's source iteration from a given
+        state (e_prev [n_band][n_dir][n_cell], source temperature T_src [n_cell]).
+        Returns (e, T, margin); e is None unless want_energy."""
+        e_prev = np.ascontiguousarray(e_prev, np.float64).reshape(-1)
+        T_src = np.ascontiguousarray(T_src, np.float64)
+        T = np.zeros(self.n_cell)
+        e = np.zeros(self.n_band * self.n_dir * self.n_cell) if want_energy else None
+        m = lib().oracle_step(self._h, e_prev, T_src, inner, inner_tol, threads,
+                              e.ctypes.data_as(C.c_void_p) if e is not None else None, T)
+        if e is not None:
+            e = e.reshape(self.n_band, self.n_dir, self.n_cell)
+        return e, T, float(m)
+
+    def heat_flux(self):
+        """Heat flux of the last run or step."""
+        q, qb = np.zeros(self.n_bc), np.zeros(self.n_bc * self.n_band)
+        lib().oracle_heat_flux(self._h, q, qb)
+        return q, qb.reshape(self.n_bc, self.n_band)
 
     def assemble(self, band, direction, e_prev, ebar):
         n, nf = self.n_cell, self.n_face

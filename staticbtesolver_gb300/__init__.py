@@ -21,7 +21,7 @@ import numpy as np
 
 from . import _build
 
-__all__ = ["build", "Problem", "Context", "Options", "Report", "StaticBTESolver", "bicgstab_csr",
+__all__ = ["build", "Problem", "Context", "Options", "Report", "StaticBTESolver", "bicgstab_csr", "dsa_solve",
            "FORM_PLAIN", "FORM_MIXED", "FORM_SWEEP", "BteError", "lib_paths"]
 
 FORM_PLAIN = 0
@@ -48,7 +48,7 @@ class Options(C.Structure):
     _fields_ = [("max_iter", C.c_int), ("tol", C.c_double), ("form", C.c_int), ("inner_tol", C.c_double),
                 ("inner_maxit", C.c_int), ("batch_systems", C.c_int), ("on_iteration", ITER_CB),
                 ("user", C.c_void_p), ("profile", C.c_int), ("accel", C.c_int), ("accel_every", C.c_int),
-                ("keep_history", C.c_int)]
+                ("keep_history", C.c_int), ("dsa", C.c_int), ("dsa_tol", C.c_double), ("dsa_maxit", C.c_int)]
 
 
 class KernelStat(C.Structure):
@@ -62,7 +62,8 @@ class Report(C.Structure):
                 ("ms_rhs", C.c_double), ("ms_inner", C.c_double), ("ms_reduce", C.c_double),
                 ("kernel_launches", C.c_longlong), ("sweep_group", C.c_int), ("sweep_threads", C.c_int),
                 ("accel_steps", C.c_int), ("accel_reverts", C.c_int), ("sweep_ring", C.c_int),
-                ("sweep_margin", C.c_int)]
+                ("sweep_margin", C.c_int), ("dsa_solves", C.c_int), ("dsa_iterations", C.c_longlong),
+                ("ms_dsa", C.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -124,9 +125,11 @@ def _load():
     L.bte_get_sweep_tuning.restype = C.c_int
     L.bte_bicgstab_csr.argtypes = [C.c_int, _ip, _ip, _dp, C.c_int, _dp, _dp, C.c_int, C.c_double,
                                    C.POINTER(C.c_int), C.POINTER(C.c_int)]
+    L.bte_dsa_solve.argtypes = [C.c_int, C.c_int, _ip, _dp, _dp, _dp, C.c_double, C.c_int, C.POINTER(C.c_int),
+                                C.POINTER(C.c_double)]
     for fn in ("bte_create", "bte_destroy", "bte_set_geometry", "bte_set_quadrature", "bte_set_bands",
                "bte_set_bcs", "bte_solve", "bte_get_temperature", "bte_get_band_temperature", "bte_get_heat_flux",
-               "bte_get_energy", "bte_get_margins", "bte_bicgstab_csr"):
+               "bte_get_energy", "bte_get_margins", "bte_bicgstab_csr", "bte_dsa_solve"):
         getattr(L, fn).restype = C.c_int
     H = C.CDLL(_build.LIB_HOST)
     H.sbte_open.restype = vp
@@ -298,10 +301,11 @@ class Context:
 
     def solve(self, max_iter=1000, tol=1e-5, form=FORM_PLAIN, inner_tol=1e-9, inner_maxit=1000,
               batch_systems=0, on_iteration=None, raise_on_not_converged=False, profile=False, accel=0,
-              accel_every=8, keep_history=False):
+              accel_every=8, keep_history=False, dsa=False, dsa_tol=0.0, dsa_maxit=0):
         o = default_options(max_iter=int(max_iter), tol=float(tol), form=int(form), inner_tol=float(inner_tol),
                             inner_maxit=int(inner_maxit), batch_systems=int(batch_systems), profile=int(profile),
-                            accel=int(accel), accel_every=int(accel_every), keep_history=int(bool(keep_history)))
+                            accel=int(accel), accel_every=int(accel_every), keep_history=int(bool(keep_history)),
+                            dsa=int(bool(dsa)), dsa_tol=float(dsa_tol), dsa_maxit=int(dsa_maxit))
         cb = None
         if on_iteration is not None:
             cb = ITER_CB(lambda _u, it, m, ms: on_iteration(it, m, ms))
@@ -408,6 +412,23 @@ class StaticBTESolver:
         if self.result is None:
             raise BteError(2, "writeTempcell: solve first")
         write_tempcell(path, self._geometry[0], self.result.T, self._geometry[1], self._L)
+
+
+def dsa_solve(nb, W, b, tol=1e-6, maxit=4000):
+    """The low-order diffusion solve of the dsa option on the GPU (bte_dsa_solve):
+    nb[f][c] neighbour (-1 none / wall), W[f][c] >= 0 symmetric couplings, b[n];
+    returns (x, iterations, relative residual of the Jacobi-scaled system)."""
+    L, _ = _load()
+    nb = np.ascontiguousarray(nb, np.int32)
+    W = np.ascontiguousarray(W, np.float64)
+    F, n = nb.shape
+    x = np.zeros(n)
+    it, rr = C.c_int(0), C.c_double(0.0)
+    st = L.bte_dsa_solve(n, F, nb.ravel(), W.ravel(), np.ascontiguousarray(b, np.float64), x, float(tol), int(maxit),
+                         C.byref(it), C.byref(rr))
+    if st != 0:
+        raise BteError(st, L.bte_last_error(None).decode())
+    return x, it.value, rr.value
 
 
 def bicgstab_csr(rowptr, col, val, b, maxit=1000, tol=1e-9):

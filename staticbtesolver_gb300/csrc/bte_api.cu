@@ -25,6 +25,8 @@
 #include "bte_kernels.cuh"
 #include "bte_transport.cuh"
 #include "bte_mlp.cuh"
+#include "bte_dsa.cuh"
+#include "dsa_setup.h"
 #include "sweep_order.h"
 #include <random>
 
@@ -60,10 +62,11 @@ struct DevBuf {
 constexpr int kGroup = 8;  // BiCGSTAB iterations launched between host checks
 
 enum KernelKind { KK_P, KK_SPMV1, KK_S, KK_SPMV2, KK_X, KK_INIT, KK_RHS, KK_REDUCE, KK_DIFFUSE, KK_HEAT, KK_SWEEP,
-                  KK_SWEEP_RES, kNumKinds };
+                  KK_SWEEP_RES, KK_DSA, kNumKinds };
 const char* kKindNames[kNumKinds] = {"bicg_p_update", "bicg_spmv1",   "bicg_s_update", "bicg_spmv2",
                                      "bicg_x_update", "bicg_init",    "rhs_assembly",  "reduce_margin",
-                                     "diffuse_wall",  "heat_flux",    "upwind_sweep",  "sweep_residual"};
+                                     "diffuse_wall",  "heat_flux",    "upwind_sweep",  "sweep_residual",
+                                     "dsa_correction"};
 
 }  // namespace
 
@@ -149,6 +152,14 @@ struct bte_ctx {
     size_t ev_next = 0;
     bte_kernel_stat stats[kNumKinds];
     std::vector<int> h_active;
+    // diffusion-synthetic acceleration: the scaled low-order operator and its
+    // conjugate-gradient work (bte_dsa.cuh), the source temperature of the
+    // running outer iteration, the right-hand side and the correction
+    bool dsa_ready = false;
+    int dsa_walls = 0;   // wall faces held at a fixed temperature
+    int dsa_blocks = 0;  // cooperative grid of k_dsa_cg
+    DevBuf d_lo_nb, d_lo_w, d_lo_dsc, d_Tsrc, d_dsa_b, d_dsa_x;
+    DevBuf cg_r, cg_aw, cg_s, cg_x, cg_p, cg_part, cg_bar, cg_stat, cg_relres;
     // results
     double* e_curr = nullptr;
     double* e_prev = nullptr;
@@ -595,6 +606,7 @@ static bte_status setup(bte_ctx* ctx, int batch_systems) {
     ctx->h_iters.resize(S);
     ctx->plan_ready = false;
     ctx->mixed_ready = false;
+    ctx->dsa_ready = false;
     ctx->dirty = false;
     return BTE_OK;
 }
@@ -628,6 +640,108 @@ static bte_status setup_mixed(bte_ctx* ctx) {
     BTE_CUDA(ctx->m_skip.alloc(sizeof(int) * S));
     BTE_CUDA(ctx->m_active.alloc(sizeof(int)));
     ctx->mixed_ready = true;
+    return BTE_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Diffusion-synthetic acceleration: the low-order operator and its solve.
+
+// Weight of the physical second-moment term in the low-order face coefficient
+// (0 keeps only the upwind scheme's numerical diffusion).  1/4 came out best
+// on 2D squares from thick (Lambda/h ~ 1e-3) to mixed (Lambda/h up to ~8)
+// cells: 0.17-0.29 error reduction per outer iteration.
+constexpr double kDsaBeta = 0.25;
+constexpr int kDsaThreads = bte::dsa::THREADS;
+
+// Upload a low-order operator (nb, W as bte_dsa_solve takes them) in its
+// symmetrically scaled form and size the conjugate-gradient work for n cells.
+static bte_status dsa_prepare(bte_ctx* ctx, int n, int F, const int* nb, const double* W) {
+    cudaStream_t st = ctx->stream;
+    std::vector<double> diag(n, 0.0), dsc(n, 0.0);
+    for (int f = 0; f < F; ++f)
+        for (int c = 0; c < n; ++c) diag[c] += W[(size_t)f * n + c];
+    for (int c = 0; c < n; ++c) dsc[c] = diag[c] > 0.0 ? 1.0 / std::sqrt(diag[c]) : 0.0;
+    std::vector<float> w((size_t)F * n, 0.0f);
+    std::vector<int> nbv((size_t)F * n, -1);
+    for (int f = 0; f < F; ++f)
+        for (int c = 0; c < n; ++c) {
+            const size_t q = (size_t)f * n + c;
+            const int o = nb[q];
+            if (o >= 0 && W[q] > 0.0) {
+                w[q] = (float)(W[q] * dsc[c] * dsc[o]);
+                nbv[q] = o;
+            }
+        }
+    BTE_CUDA(upload(ctx->d_lo_nb, nbv, st));
+    BTE_CUDA(upload(ctx->d_lo_w, w, st));
+    BTE_CUDA(upload(ctx->d_lo_dsc, dsc, st));
+    int coop = 0, sms = 0, occ = 0;
+    BTE_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, ctx->device));
+    if (!coop) return fail(ctx, BTE_ERR_CUDA, "dsa: the device does not support cooperative launches");
+    BTE_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
+    BTE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, bte::dsa::k_dsa_cg, kDsaThreads, 0));
+    if (occ < 1) return fail(ctx, BTE_ERR_CUDA, "dsa: the low-order kernel cannot be resident");
+    // at most one block per SM: enough threads for the cells, few blocks at each barrier
+    const int want = std::max(1, std::min(sms, (n + kDsaThreads - 1) / kDsaThreads));
+    ctx->dsa_blocks = std::min(want, occ * sms);
+    const size_t nn = (size_t)n;
+    BTE_CUDA(ctx->cg_r.alloc(sizeof(float) * 2 * nn));
+    BTE_CUDA(ctx->cg_aw.alloc(sizeof(float) * 2 * nn));
+    BTE_CUDA(ctx->cg_s.alloc(sizeof(float) * 2 * nn));
+    BTE_CUDA(ctx->cg_x.alloc(sizeof(float) * nn));
+    BTE_CUDA(ctx->cg_p.alloc(sizeof(float) * nn));
+    BTE_CUDA(ctx->cg_part.alloc(sizeof(double) * (2 * (size_t)ctx->dsa_blocks + 2)));
+    BTE_CUDA(ctx->cg_bar.alloc(sizeof(unsigned) * 2));
+    BTE_CUDA(ctx->cg_stat.alloc(sizeof(int) * 4));
+    BTE_CUDA(ctx->cg_relres.alloc(sizeof(double)));
+    BTE_CUDA(ctx->d_dsa_b.alloc(sizeof(double) * nn));
+    BTE_CUDA(ctx->d_dsa_x.alloc(sizeof(double) * nn));
+    BTE_CUDA(cudaMemsetAsync(ctx->cg_stat.p, 0, sizeof(int) * 4, st));
+    return BTE_OK;
+}
+
+// One low-order solve of d_dsa_b into d_dsa_x (cooperative launch, every block resident).
+static bte_status dsa_launch(bte_ctx* ctx, int n, int F, double tol, int maxit) {
+    cudaStream_t st = ctx->stream;
+    BTE_CUDA(cudaMemsetAsync(ctx->cg_bar.p, 0, sizeof(unsigned) * 2, st));
+    bte::dsa::Lo lo{n, F, ctx->d_lo_nb.as<int>(), ctx->d_lo_w.as<float>(), ctx->d_lo_dsc.as<double>()};
+    bte::dsa::CgWork wk{ctx->cg_r.as<float>(), ctx->cg_aw.as<float>(), ctx->cg_s.as<float>(), ctx->cg_x.as<float>(),
+                        ctx->cg_p.as<float>(), ctx->cg_part.as<double>(), ctx->cg_bar.as<unsigned>(),
+                        ctx->cg_stat.as<int>(), ctx->cg_relres.as<double>()};
+    const double* b = ctx->d_dsa_b.as<double>();
+    double* x = ctx->d_dsa_x.as<double>();
+    void* args[] = {&lo, &wk, &b, &tol, &maxit, &x};
+    BTE_CUDA(cudaLaunchCooperativeKernel((const void*)bte::dsa::k_dsa_cg, dim3(ctx->dsa_blocks), dim3(kDsaThreads),
+                                         args, 0, st));
+    BTE_LAUNCHED();
+    return BTE_OK;
+}
+
+// The low-order operator of the mesh, bands and walls of ctx.
+static bte_status setup_dsa(bte_ctx* ctx) {
+    const int n = ctx->n, F = ctx->F;
+    // walls held at a fixed temperature: isothermal rows, and boundary faces
+    // that no row names (their wall energy stays 0 in the reference)
+    std::vector<char> fixed((size_t)n * F, 0);
+    for (size_t cf = 0; cf < (size_t)n * F; ++cf) {
+        const int code = ctx->nbr[cf];
+        if (code >= 0) continue;
+        int row = -1;
+        for (int i = 0; i < ctx->n_bc; ++i)
+            if (ctx->bc_index[i] == code) { row = i; break; }
+        fixed[cf] = row < 0 || ctx->bc_type[row] == 1;
+    }
+    bte::DsaCoefficients co;
+    bte::dsa_coefficients(ctx->dim, n, F, ctx->nbr.data(), ctx->area.data(), ctx->normal.data(), ctx->volume.data(),
+                          ctx->n_dir, ctx->s.data(), ctx->S.data(), ctx->solid_angle, ctx->n_band, ctx->vg.data(),
+                          ctx->tau.data(), ctx->Lr.data(), fixed, kDsaBeta, co);
+    ctx->dsa_walls = co.n_dirichlet;
+    if (co.n_dirichlet > 0) {
+        bte_status s = dsa_prepare(ctx, n, F, co.nb.data(), co.W.data());
+        if (s != BTE_OK) return s;
+        BTE_CUDA(ctx->d_Tsrc.alloc(sizeof(double) * ctx->Np));
+    }
+    ctx->dsa_ready = true;
     return BTE_OK;
 }
 
@@ -1212,6 +1326,11 @@ extern "C" bte_status bte_solve(bte_ctx* ctx, const bte_options* opts, bte_repor
     if (o.form != BTE_FORM_PLAIN && o.form != BTE_FORM_SWEEP && o.form != BTE_FORM_MIXED)
         return fail(ctx, BTE_ERR_INVALID_ARGUMENT, "bte_solve: unknown form");
     if (ctx->dim == 1 && ctx->F != 2) return fail(ctx, BTE_ERR_INVALID_ARGUMENT, "1D mesh needs 2 faces");
+    if (o.dsa && ctx->dim == 1) return fail(ctx, BTE_ERR_INVALID_ARGUMENT, "bte_solve: dsa needs a 2D or 3D mesh");
+    if (o.dsa && (o.dsa_tol < 0 || o.dsa_maxit < 0))
+        return fail(ctx, BTE_ERR_INVALID_ARGUMENT, "bte_solve: bad dsa_tol / dsa_maxit");
+    const double dsa_tol = o.dsa_tol > 0 ? o.dsa_tol : 1e-3;
+    const int dsa_maxit = o.dsa_maxit > 0 ? o.dsa_maxit : 4000;
     BTE_CUDA(cudaSetDevice(ctx->device));
     bte_report rep;
     std::memset(&rep, 0, sizeof(rep));
@@ -1235,6 +1354,12 @@ extern "C" bte_status bte_solve(bte_ctx* ctx, const bte_options* opts, bte_repor
         bte_status s = setup_mixed(ctx);
         if (s != BTE_OK) return s;
     }
+    if (o.dsa && !ctx->dsa_ready) {
+        bte_status s = setup_dsa(ctx);
+        if (s != BTE_OK) return s;
+    }
+    // without a wall held at a fixed temperature the low-order operator is singular: dsa is ignored
+    const bool dsa_on = o.dsa && ctx->dsa_walls > 0;
     cudaStream_t st = ctx->stream;
     const int NB = ctx->n_band, ND = ctx->n_dir;
     const size_t Np = ctx->Np;
@@ -1242,14 +1367,29 @@ extern "C" bte_status bte_solve(bte_ctx* ctx, const bte_options* opts, bte_repor
     ctx->e_prev = ctx->d_e1.as<double>();
     BTE_CUDA(cudaMemsetAsync(ctx->e_curr, 0, sizeof(double) * NB * ND * Np, st));
     BTE_CUDA(cudaMemsetAsync(ctx->d_ebar.p, 0, sizeof(double) * NB * Np, st));  // cell_band_density = 0 (:92)
+    if (dsa_on) {
+        // the source of the first outer iteration is ebar = 0, i.e. T = T_ref
+        bte::dsa::k_fill<<<(unsigned)((Np + 255) / 256), 256, 0, st>>>(ctx->d_T.as<double>(), ctx->T_ref, (int)Np);
+        BTE_LAUNCHED();
+        BTE_CUDA(cudaMemsetAsync(ctx->cg_stat.p, 0, sizeof(int) * 4, st));
+    }
     ctx->margins.clear();
     double Lr_sum = 0;
     for (int b = 0; b < NB; ++b) Lr_sum += ctx->Lr[b];
-    cudaEvent_t ev[7];  // [0..3] the phases of an outer iteration, [5..6] the accelerator step after it
+    // [0..3] the phases of an outer iteration, [5..6] the accelerator step
+    // after it (the dsa correction included), [7..8] the dsa correction
+    cudaEvent_t ev[9];
     for (auto& e : ev) BTE_CUDA(cudaEventCreate(&e));
-    struct EvGuard { cudaEvent_t* e; ~EvGuard() { for (int k = 0; k < 7; ++k) cudaEventDestroy(e[k]); } } guard{ev};
+    struct EvGuard { cudaEvent_t* e; ~EvGuard() { for (int k = 0; k < 9; ++k) cudaEventDestroy(e[k]); } } guard{ev};
     bool accel_timed = false;  // ev[5..6] hold an accelerator step not yet added to the report
+    bool dsa_timed = false;    // ev[7..8] hold a dsa correction not yet added
     auto add_accel_time = [&]() {
+        if (dsa_timed) {
+            float t = 0;
+            cudaEventElapsedTime(&t, ev[7], ev[8]);
+            rep.ms_dsa += t;
+            dsa_timed = false;
+        }
         if (!accel_timed) return;
         float t = 0;
         cudaEventElapsedTime(&t, ev[5], ev[6]);
@@ -1257,6 +1397,7 @@ extern "C" bte_status bte_solve(bte_ctx* ctx, const bte_options* opts, bte_repor
         rep.ms_total += t;
         accel_timed = false;
     };
+    const bool post_step = o.accel != 0 || dsa_on;  // kernels after the margin read-back
     bte_status result = BTE_ERR_NOT_CONVERGED;
     const int nred = (int)(Np / bte::THREADS);
     // the sweep of an acyclic plan may sum the margin itself (k_reduce then
@@ -1334,6 +1475,8 @@ extern "C" bte_status bte_solve(bte_ctx* ctx, const bte_options* opts, bte_repor
     for (int it = 0; it < o.max_iter; ++it) {
         std::swap(ctx->e_curr, ctx->e_prev);
         BTE_CUDA(cudaEventRecord(ev[0], st));
+        if (dsa_on)  // the temperature this iteration's source comes from
+            BTE_CUDA(cudaMemcpyAsync(ctx->d_Tsrc.p, ctx->d_T.p, sizeof(double) * ctx->n, cudaMemcpyDeviceToDevice, st));
         if (aa_slots && it > 0) {  // the state this iteration starts from (iteration 0 starts from T_ref, e = 0)
             const bte::mlp::AaState as = aa_state(ctx);
             const size_t L = aa_len(ctx);
@@ -1476,9 +1619,42 @@ extern "C" bte_status bte_solve(bte_ctx* ctx, const bte_options* opts, bte_repor
         // the margin at the jump (right after a jump the margin rises while the
         // intensities follow the new source, so it is judged once they have);
         // otherwise restore the state before the jump and stop extrapolating
-        if (o.accel) {
+        if (post_step) {
             BTE_CUDA(cudaEventRecord(ev[5], st));
             accel_timed = true;
+        }
+        if (dsa_on) {
+            // low-order correction: solve for the remaining error x of T from
+            // this iteration's change, then T += x (and ebar, and the boundary
+            // cells' intensities the walls reflect next)
+            const int n = ctx->n;
+            BTE_CUDA(cudaEventRecord(ev[7], st));
+            BTE_LAUNCH(KK_DSA, -1, 3.0 * n * 8.0, 0,
+                       bte::dsa::k_dsa_rhs<<<(n + 255) / 256, 256, 0, st>>>(ctx->d_T.as<double>(),
+                                                                            ctx->d_Tsrc.as<double>(),
+                                                                            ctx->d_volume.as<double>(), n,
+                                                                            ctx->d_dsa_b.as<double>()));
+            {
+                size_t slot = 0;
+                BTE_CUDA(prof_begin(ctx, &slot));
+                bte_status ls = dsa_launch(ctx, n, ctx->F, dsa_tol, dsa_maxit);
+                if (ls != BTE_OK) return ls;
+                BTE_CUDA(prof_end(ctx, slot, KK_DSA, -1, 0, 0));
+            }
+            BTE_LAUNCH(KK_DSA, -1, (2.0 + NB) * n * 8.0, 0,
+                       bte::dsa::k_dsa_apply<<<(n + 255) / 256, 256, 0, st>>>(
+                           ctx->d_dsa_x.as<double>(), ctx->d_Cb.as<double>(), ctx->solid_angle, ctx->T_ref, n, NB,
+                           Np, ctx->d_T.as<double>(), ctx->d_ebar.as<double>()));
+            if (ctx->nbcell > 0) {
+                const int nt = ctx->nbcell * ND;
+                BTE_LAUNCH(KK_DSA, -1, 2.0 * nt * NB * 8.0, 0,
+                           bte::dsa::k_dsa_shift_boundary<<<dim3((nt + 255) / 256, NB), 256, 0, st>>>(
+                               ctx->d_dsa_x.as<double>(), ctx->d_bcell.as<int>(), ctx->nbcell, ctx->d_Cb.as<double>(),
+                               ctx->solid_angle, ND, Np, ctx->e_curr));
+            }
+            BTE_CUDA(cudaEventRecord(ev[8], st));
+            dsa_timed = true;
+            ++rep.dsa_solves;
         }
         if (aa_slots && it > 0) {
             bte_status s = anderson_step(ctx, aa_slots, aa_count, aa_next, aa_order, m, rep);
@@ -1524,7 +1700,7 @@ extern "C" bte_status bte_solve(bte_ctx* ctx, const bte_options* opts, bte_repor
         }
         // the accelerator's kernels and copies run after ev[3]: timed by
         // ev[5..6], read after the next synchronisation
-        if (o.accel) BTE_CUDA(cudaEventRecord(ev[6], st));
+        if (post_step) BTE_CUDA(cudaEventRecord(ev[6], st));
     }
     if (accel_timed) {
         BTE_CUDA(cudaEventSynchronize(ev[6]));
@@ -1543,8 +1719,17 @@ extern "C" bte_status bte_solve(bte_ctx* ctx, const bte_options* opts, bte_repor
                                         ctx->d_bf_area.as<double>(), ctx->d_vg.as<double>(), ctx->nbf, NB,
                                         ctx->n_bc, ctx->dim, ctx->d_qband.as<double>(), ctx->d_q.as<double>());
     BTE_LAUNCHED();
+    int dsa_stat[4] = {0, 0, 0, 0};
+    if (dsa_on) BTE_CUDA(cudaMemcpyAsync(dsa_stat, ctx->cg_stat.p, sizeof(dsa_stat), cudaMemcpyDeviceToHost, st));
     BTE_CUDA(cudaStreamSynchronize(st));
     if (ctx->profile) prof_resolve(ctx, nullptr, 0);
+    if (dsa_on) {
+        rep.dsa_iterations = dsa_stat[2];
+        if (dsa_stat[1]) {
+            if (report) *report = rep;
+            return fail(ctx, BTE_ERR_CUDA, "dsa: a grid barrier of the low-order solve timed out");
+        }
+    }
     rep.kernel_launches = ctx->launches;
     rep.sweep_group = o.form == BTE_FORM_SWEEP ? ctx->sweep_shape.G : 0;
     rep.sweep_threads = o.form == BTE_FORM_SWEEP ? ctx->sweep_shape.threads : 0;
@@ -1726,6 +1911,67 @@ bte_status bte_bicgstab_csr(int n, const int* rowptr, const int* colind, const d
     return BTE_OK;
 }
 
+static bte_status dsa_solve_impl(bte_ctx* ctx, int n, int F, const int* nb, const double* W, const double* b,
+                                 double* x, double tol, int maxit, int* iterations, double* relres) {
+    BTE_CUDA(cudaGetDevice(&ctx->device));
+    BTE_CUDA(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+    bte_status s = dsa_prepare(ctx, n, F, nb, W);
+    if (s != BTE_OK) return s;
+    BTE_CUDA(cudaMemcpyAsync(ctx->d_dsa_b.p, b, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+    s = dsa_launch(ctx, n, F, tol, maxit);
+    if (s != BTE_OK) return s;
+    int stat[4] = {0, 0, 0, 0};
+    double rr = 0.0;
+    BTE_CUDA(cudaMemcpyAsync(x, ctx->d_dsa_x.p, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    BTE_CUDA(cudaMemcpyAsync(stat, ctx->cg_stat.p, sizeof(stat), cudaMemcpyDeviceToHost, ctx->stream));
+    BTE_CUDA(cudaMemcpyAsync(&rr, ctx->cg_relres.p, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    BTE_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (stat[1]) return fail(ctx, BTE_ERR_CUDA, "a grid barrier of the low-order solve timed out");
+    if (iterations) *iterations = stat[0];
+    if (relres) *relres = rr;
+    return BTE_OK;
+}
+
+bte_status bte_dsa_solve(int n, int n_face, const int* nb, const double* W, const double* b, double* x, double tol,
+                         int maxit, int* iterations, double* relres) {
+    if (n <= 0 || n_face <= 0 || !nb || !W || !b || !x || !(tol > 0) || maxit <= 0) {
+        g_create_error = "bte_dsa_solve: bad size, tolerance, iteration limit or null pointer";
+        return BTE_ERR_INVALID_ARGUMENT;
+    }
+    const size_t nf = (size_t)n * n_face;
+    for (size_t q = 0; q < nf; ++q) {
+        if (nb[q] < -1 || nb[q] >= n || !(W[q] >= 0.0) || !std::isfinite(W[q]) || !std::isfinite(b[q % n])) {
+            g_create_error = "bte_dsa_solve: neighbour index out of range or negative / non-finite value";
+            return BTE_ERR_INVALID_ARGUMENT;
+        }
+    }
+    for (int f = 0; f < n_face; ++f)
+        for (int c = 0; c < n; ++c) {
+            const size_t q = (size_t)f * n + c;
+            const int o = nb[q];
+            if (o < 0 || W[q] == 0.0) continue;
+            bool back = false;
+            for (int g = 0; g < n_face && !back; ++g) back = nb[(size_t)g * n + o] == c && W[(size_t)g * n + o] == W[q];
+            if (!back || o == c) {
+                g_create_error = "bte_dsa_solve: the operator is not symmetric (no matching slot in the neighbour)";
+                return BTE_ERR_INVALID_ARGUMENT;
+            }
+        }
+    bte_ctx tmp;
+    struct StreamGuard {
+        bte_ctx* c;
+        ~StreamGuard() {
+            if (c->stream) {
+                cudaStreamSynchronize(c->stream);
+                cudaStreamDestroy(c->stream);
+            }
+        }
+    } guard{&tmp};
+    const bte_status s = dsa_solve_impl(&tmp, n, n_face, nb, W, b, x, tol, maxit, iterations, relres);
+    if (s != BTE_OK) g_create_error = "bte_dsa_solve: " + tmp.err;
+    return s;
+}
+
 }  // extern "C"
 
 // ---------------------------------------------------------------------------
@@ -1741,12 +1987,14 @@ bte_status bte_bicgstab_csr(int n, const int* rowptr, const int* colind, const d
 // the process exits (kNoAllocScratchBytes, about 21 MB).
 //
 // Host code must not pass g_noalloc_scratch itself to a kernel: in host code
-// the name is a host-side stand-in, not a device address.  The device address
-// is looked up once per device with cudaGetSymbolAddress (with that device
-// current) on the first call made on it; that first call should therefore come
-// before any stream capture.  All calls share the one array and leave their
-// contents in it: each call clears what must start at zero, and calls that
-// overlap on the GPU (different streams or threads at the same time) race.
+// the name is a host-side stand-in, not a device address.  Every call looks up
+// the device address with cudaGetSymbolAddress on the current device, so a
+// context that was torn down and created again (cudaDeviceReset) is followed;
+// the first call on a device also loads this module's device code there and
+// should therefore come before any stream capture.  All calls share the one
+// array and leave their contents in it: each call clears what must start at
+// zero, and calls that overlap on the GPU (different streams or threads at the
+// same time) race.
 namespace {
 constexpr int kNoAllocMaxN = 1 << 18;     // unknowns
 constexpr int kNoAllocMaxIt = 10000;      // BiCGSTAB iterations
@@ -1774,29 +2022,25 @@ __global__ void k_noalloc_check_csr(const int* __restrict__ rowptr, const int* _
         if (col[k] < 0 || col[k] >= n) atomicOr(bad, 1);
 }
 
-static std::mutex g_noalloc_mutex;
-static double* g_noalloc_dev[256] = {};
-
-// Device address of g_noalloc_scratch on the current device (looked up once per device).
-static cudaError_t noalloc_scratch_address(int device, double** out) {
-    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-    if (device < 0 || device >= 256) return cudaErrorInvalidDevice;
-    if (!g_noalloc_dev[device]) {
-        void* p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess) return e;
-        g_noalloc_dev[device] = static_cast<double*>(p);
-    }
-    *out = g_noalloc_dev[device];
+// Device address of g_noalloc_scratch in the current device's context.
+static cudaError_t noalloc_scratch_address(double** out) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return e;
+    *out = static_cast<double*>(p);
     return cudaSuccess;
 }
 
+// On a failure after kernels were queued on the caller's stream, wait for them
+// (ignoring the status) so that no kernel of this call still uses the shared
+// array when the call returns.
 #define NOALLOC_CUDA(call)                                                            \
     do {                                                                              \
         cudaError_t _e = (call);                                                      \
         if (_e != cudaSuccess) {                                                      \
             g_create_error = std::string("bte_bicgstab_csr_noalloc: ") + #call + ": " + \
                              cudaGetErrorString(_e);                                  \
+            if (launched) cudaStreamSynchronize(st);                                  \
             return BTE_ERR_CUDA;                                                      \
         }                                                                             \
     } while (0)
@@ -1817,10 +2061,9 @@ extern "C" bte_status bte_bicgstab_csr_noalloc(int n, const int* rowptr, const i
         return BTE_ERR_INVALID_ARGUMENT;
     }
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    int dev = 0;
-    NOALLOC_CUDA(cudaGetDevice(&dev));
+    bool launched = false;  // work of this call is queued on st
     double* base = nullptr;
-    NOALLOC_CUDA(noalloc_scratch_address(dev, &base));
+    NOALLOC_CUDA(noalloc_scratch_address(&base));
     const size_t Np = (size_t)((n + bte::CH - 1) / bte::CH) * bte::CH;
     const int nchunk = (int)(Np / bte::CH);
     double* vec[10];
@@ -1836,6 +2079,7 @@ extern "C" bte_status bte_bicgstab_csr_noalloc(int n, const int* rowptr, const i
     int* active = iv + 8;
     // what must start at zero: the error flag, the per-iteration counters and
     // the right-hand side padding (the kernels rewrite everything else)
+    launched = true;
     NOALLOC_CUDA(cudaMemsetAsync(iv, 0, sizeof(int) * (8 + (size_t)maxit + 2), st));
     NOALLOC_CUDA(cudaMemsetAsync(vec[7], 0, sizeof(double) * Np, st));
     k_noalloc_check_csr<<<(n + 255) / 256, 256, 0, st>>>(rowptr, colind, n, nnz, bad);

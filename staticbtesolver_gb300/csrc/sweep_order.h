@@ -4,6 +4,9 @@
 
 #include <algorithm>
 #include <cstdint>
+#include <functional>
+#include <queue>
+#include <utility>
 #include <vector>
 
 namespace bte {
@@ -18,6 +21,10 @@ inline int inflow_count(uint8_t m) {
 // mask[c] bit f: face f of c is an inflow face with a neighbour.  When no cell
 // is free the unprocessed cell with the fewest unresolved inflow edges (lowest
 // index on ties) starts the next level alone and those edges become lagged.
+// That cell is found in a min-heap of (unresolved inflow edges, cell), built at
+// the first such break and kept current lazily (a decrement pushes a new entry;
+// stale entries are skipped), so a graph with many cycles costs O(n log n),
+// not O(n) per break; acyclic graphs never build it.
 inline void level_order(int n, int F, const uint8_t* mask, const int* nbr, std::vector<int>& perm,
                         std::vector<int>& lvl, std::vector<int>& lagged /* [F][n] */) {
     std::vector<int> indeg(n), dptr(n + 1, 0), down;
@@ -40,12 +47,23 @@ inline void level_order(int n, int F, const uint8_t* mask, const int* nbr, std::
     perm.clear();
     lvl.clear();
     lagged.assign((size_t)F * n, 0);
+    using Entry = std::pair<int, int>;  // (unresolved inflow edges, cell)
+    std::priority_queue<Entry, std::vector<Entry>, std::greater<Entry>> heap;
+    bool heap_on = false;
     int processed = 0;
     while (processed < n) {
         if (wave.empty()) {
+            if (!heap_on) {
+                for (int c = 0; c < n; ++c)
+                    if (!done[c]) heap.push({indeg[c], c});
+                heap_on = true;
+            }
             int best = -1;
-            for (int c = 0; c < n; ++c)
-                if (!done[c] && (best < 0 || indeg[c] < indeg[best])) best = c;
+            while (best < 0) {
+                const Entry top = heap.top();
+                heap.pop();
+                if (!done[top.second] && indeg[top.second] == top.first) best = top.second;
+            }
             for (int f = 0; f < F; ++f)
                 if ((mask[best] >> f & 1) && !done[nbr[(size_t)best * F + f]]) lagged[(size_t)f * n + best] = 1;
             wave.push_back(best);
@@ -60,6 +78,7 @@ inline void level_order(int n, int F, const uint8_t* mask, const int* nbr, std::
                 const int c2 = down[k];
                 if (done[c2]) continue;
                 if (--indeg[c2] == 0) next.push_back(c2);
+                else if (heap_on) heap.push({indeg[c2], c2});
             }
         wave.swap(next);
     }

@@ -1,0 +1,128 @@
+"""The low-order operator of the diffusion-synthetic acceleration
+(staticbtesolver_gb300/csrc/dsa_setup.h), on the CPU.
+
+The header is plain C++; it is compiled here into a small shared library and
+checked against a NumPy restatement of the same face coefficients on meshes
+read by the oracle (the reference's geometry and quadrature):
+  W_f = (A_f / Omega_tot) sum_b Lr_b L_b (G_f + beta L_b q_f / delta_f) / sum_b Lr_b,
+G_f = 1/2 sum_d |S_d.n_f|, q_f = sum_d (S_d.n_f)(s_d.n_f), delta_f the
+centroid distance across the face (dim/(dim+1) (V_c + V_nb) / A_f; a wall
+face uses V_c alone).  The operator must be symmetric, hold exactly the
+isothermal (and unnamed) wall faces, and have zero row sums away from them.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+HEADER = os.path.join(ROOT, "staticbtesolver_gb300", "csrc", "dsa_setup.h")
+
+SRC = r'''
+#include "%s"
+extern "C" int dsa_c(int dim, int n, int F, const int* nbr, const double* area, const double* normal,
+                     const double* volume, int nd, const double* s, const double* S, double om, int nb,
+                     const double* vg, const double* tau, const double* Lr, const char* fixed, double beta,
+                     double* W, int* nbo, double* diag) {
+    std::vector<char> fx(fixed, fixed + (size_t)n * F);
+    bte::DsaCoefficients co;
+    bte::dsa_coefficients(dim, n, F, nbr, area, normal, volume, nd, s, S, om, nb, vg, tau, Lr, fx, beta, co);
+    std::copy(co.W.begin(), co.W.end(), W);
+    std::copy(co.nb.begin(), co.nb.end(), nbo);
+    std::copy(co.diag.begin(), co.diag.end(), diag);
+    return co.n_dirichlet;
+}
+'''
+
+
+@pytest.fixture(scope="module")
+def lib(tmp_path_factory):
+    d = tmp_path_factory.mktemp("dsa_setup")
+    src = d / "dsa.cpp"
+    src.write_text(SRC % HEADER)
+    out = d / "libdsa.so"
+    subprocess.run(["g++", "-O2", "-std=c++17", "-shared", "-fPIC", "-o", str(out), str(src)], check=True)
+    L = C.CDLL(str(out))
+    L.dsa_c.restype = C.c_int
+    return L
+
+
+from oracle.dsa import coefficients, fixed_faces, read_bands as bands_of, read_bc_rows as bc_rows  # noqa: E402
+
+
+def restated(g, q, bands, fixed, dim, beta):
+    return coefficients(g, q, bands, fixed, dim, beta)
+
+
+def run(lib, o, bands, rows, beta=0.25):
+    g, q = o.geometry(), o.quadrature()
+    n, F = g["nbr"].shape
+    fixed = fixed_faces(g["nbr"], rows)
+    W, nbo, diag = np.zeros(F * n), np.zeros(F * n, np.int32), np.zeros(n)
+    f64 = lambda a: np.ascontiguousarray(a, np.float64).ctypes.data_as(C.c_void_p)
+    nbr = np.ascontiguousarray(g["nbr"], np.int32)
+    fx = np.ascontiguousarray(fixed, np.int8)
+    nd = lib.dsa_c(o.dim, n, F, nbr.ctypes.data_as(C.c_void_p), f64(g["area"]), f64(g["normal"]), f64(g["volume"]),
+                   o.n_dir, f64(q["s"]), f64(q["S"]), C.c_double(q["solid_angle"]), len(bands["vg"]),
+                   f64(bands["vg"]), f64(bands["tau"]), f64(bands["Lr"]), fx.ctypes.data_as(C.c_void_p),
+                   C.c_double(beta), W.ctypes.data_as(C.c_void_p), nbo.ctypes.data_as(C.c_void_p),
+                   diag.ctypes.data_as(C.c_void_p))
+    return g, q, fixed, W.reshape(F, n), nbo.reshape(F, n), diag, nd
+
+
+@pytest.mark.parametrize("name", ["square10_b40", "2DM2DG", "cube4_b2"])
+def test_coefficients_match_restatement(lib, oracle_mod, get_case, name):
+    case = get_case(name)
+    o = oracle_mod.Oracle(*case.args())
+    bands, rows = bands_of(case.band), bc_rows(case.bc)
+    for beta in (0.0, 0.25):
+        g, q, fixed, W, nbo, diag, nd = run(lib, o, bands, rows, beta)
+        ref = restated(g, q, bands, fixed, o.dim, beta).T  # [F][n]
+        np.testing.assert_allclose(W, ref, rtol=1e-12, atol=0)
+        assert nd == int(fixed.sum())
+        # couplings only through interior faces, to the face's neighbour
+        nbr = g["nbr"].T
+        assert np.array_equal(nbo, np.where(nbr >= 0, nbr, -1))
+        np.testing.assert_allclose(diag, W.sum(0), rtol=1e-14)
+
+
+@pytest.mark.parametrize("name", ["square10_b40", "cube4_b2"])
+def test_operator_is_symmetric_and_conservative(lib, oracle_mod, get_case, name):
+    import scipy.sparse as sp
+
+    case = get_case(name)
+    o = oracle_mod.Oracle(*case.args())
+    g, q, fixed, W, nbo, diag, nd = run(lib, o, bands_of(case.band), bc_rows(case.bc))
+    F, n = W.shape
+    m = nbo >= 0
+    cols = np.where(m, nbo, 0)
+    rows = np.broadcast_to(np.arange(n), (F, n))
+    A = sp.csr_matrix((-W[m], (rows[m], cols[m])), shape=(n, n)) + sp.diags(diag)
+    assert abs(A - A.T).max() == 0.0  # each face evaluated once, stored on both sides
+    # zero row sums except in cells with a fixed-temperature wall face
+    walls = (np.where(nbo < 0, W, 0.0)).sum(0)
+    np.testing.assert_allclose(np.asarray(A.sum(1)).ravel(), walls, atol=1e-12 * diag.max())
+    assert nd > 0 and (walls > 0).sum() > 0
+    # positive definite with at least one wall held fixed
+    ev = np.linalg.eigvalsh(A.toarray()) if n <= 2000 else None
+    if ev is not None:
+        assert ev.min() > 0
+
+
+def test_adiabatic_walls_carry_no_term(lib, oracle_mod, get_case):
+    """Diffuse (2) and specular (31) walls are adiabatic: no wall coefficient."""
+    case = get_case("2DM2DG")
+    o = oracle_mod.Oracle(*case.args())
+    rows = bc_rows(case.bc)
+    g, q, fixed, W, nbo, diag, nd = run(lib, o, bands_of(case.band), rows)
+    nbr = g["nbr"].T
+    types = {-e - 1: t for e, t, _ in rows}
+    for code, t in types.items():
+        sel = nbr == code
+        if t == 1:
+            assert (W[sel] > 0).all()
+        else:
+            assert (W[sel] == 0).all()

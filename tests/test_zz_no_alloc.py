@@ -35,7 +35,10 @@ def _bidiagonal(n, seed):
     return rp, cols, vals, rng.uniform(-1, 1, n)
 
 
-def _noalloc(sbte, rp, ci, v, b, maxit=1000, tol=1e-9):
+def _noalloc(sbte, rp, ci, v, b, maxit=1000, tol=1e-9, free_memory=None):
+    """One call through the C ABI on torch-owned device buffers.  free_memory
+    (a list) receives the device's free bytes right before and right after
+    the call itself."""
     import torch
 
     L, _ = sbte._load()
@@ -49,9 +52,14 @@ def _noalloc(sbte, rp, ci, v, b, maxit=1000, tol=1e-9):
     t_x = torch.full((len(b),), float("nan"), dtype=torch.float64, device=dev)
     stream = torch.cuda.current_stream(dev).cuda_stream
     it, conv = C.c_int(0), C.c_int(0)
+    torch.cuda.synchronize(dev)
+    if free_memory is not None:
+        free_memory.append(torch.cuda.mem_get_info(dev)[0])
     st = f(len(b), t_rp.data_ptr(), t_ci.data_ptr(), t_v.data_ptr(), len(ci), t_b.data_ptr(), t_x.data_ptr(),
            maxit, tol, C.c_void_p(stream), C.byref(it), C.byref(conv))
     torch.cuda.synchronize(dev)
+    if free_memory is not None:
+        free_memory.append(torch.cuda.mem_get_info(dev)[0])
     return st, t_x.cpu().numpy(), it.value, bool(conv.value)
 
 
@@ -66,6 +74,15 @@ def test_noalloc_matches_allocating_entry_on_two_calls(sbte):
         assert np.linalg.norm(x_na - x_ref) <= 1e-12 * np.linalg.norm(x_ref)
 
 
+def test_noalloc_call_allocates_no_device_memory(sbte):
+    rp, ci, v, b = _bidiagonal(4000, 4)
+    _noalloc(sbte, rp, ci, v, b)  # the first call on the device loads the module
+    free = []
+    st, x, _, conv = _noalloc(sbte, rp, ci, v, b, free_memory=free)
+    assert st == 0 and conv
+    assert free[0] == free[1], free
+
+
 def test_noalloc_rejects_oversize_and_bad_csr(sbte):
     L, _ = sbte._load()
     rp, ci, v, b = _bidiagonal(100, 3)
@@ -75,6 +92,19 @@ def test_noalloc_rejects_oversize_and_bad_csr(sbte):
     bad[5] = 100  # column out of range
     st, _, _, _ = _noalloc(sbte, rp, bad, v, b)
     assert st == 1 and b"malformed" in L.bte_last_error(None)
+    dec = rp.copy()
+    dec[10], dec[11] = dec[11], dec[10]  # row pointers decrease
+    assert dec[11] < dec[10]
+    st, _, _, _ = _noalloc(sbte, dec, ci, v, b)
+    assert st == 1 and b"malformed" in L.bte_last_error(None)
+    short = rp.copy()
+    short[-1] -= 1  # rowptr[n] != nnz
+    st, _, _, _ = _noalloc(sbte, short, ci, v, b)
+    assert st == 1 and b"malformed" in L.bte_last_error(None)
+    # a good call after the rejected ones still matches the allocating entry
+    st, x_na, _, _ = _noalloc(sbte, rp, ci, v, b)
+    x_ref, _, _ = sbte.bicgstab_csr(rp, ci, v, b)
+    assert st == 0 and np.linalg.norm(x_na - x_ref) <= 1e-12 * np.linalg.norm(x_ref)
     big = 1 << 18
     f = L.bte_bicgstab_csr_noalloc
     st = f(big + 1, None, None, None, 0, None, None, 10, 1e-9, None, None, None)

@@ -30,16 +30,17 @@ typedef enum bte_status {
     BTE_ERR_OUT_OF_MEMORY = 4,
     BTE_ERR_UNSUPPORTED_BC = 5,   /* boundary type the reference aborts on (:218, :244, :254) */
     BTE_ERR_NOT_CONVERGED = 6,    /* outer iteration hit max_iter (results are still valid) */
-    BTE_ERR_NUMERICAL = 7,        /* NaN/Inf in the outer iterate */
+    BTE_ERR_NUMERICAL = 7,        /* NaN/Inf in the outer iterate or in band data */
     BTE_ERR_NO_DEVICE = 8
 } bte_status;
 
 /* How each (band, direction) system is solved inside one outer iteration. */
 typedef enum bte_form {
     /* FP64 right-Jacobi BiCGSTAB, x0 = 0, ||r||/||r0|| < inner_tol, at most
-     * inner_maxit iterations, breakdown restart with r_hat = 6.8 b + 0.6:
-     * the reference GPU inner solve (src/bicgstab.hpp:138-300), all systems of
-     * an outer iteration batched into one launch per BiCGSTAB phase. */
+     * inner_maxit iterations (then the last iterate), breakdown restart with
+     * r_hat = 6.8 b + 0.6: the reference GPU inner solve
+     * (src/bicgstab.hpp:138-300), all systems of an outer iteration batched
+     * into one launch per BiCGSTAB phase (see bte_options.plain_cycles). */
     BTE_FORM_PLAIN = 0,
     /* FP32 BiCGSTAB inside FP64 iterative refinement: x starts from the
      * previous outer iterate; each cycle computes the FP64 residual b - A x,
@@ -84,6 +85,10 @@ typedef struct bte_options {
     int dsa;              /* nonzero: diffusion-synthetic acceleration of the outer iteration (below) */
     double dsa_tol;       /* relative residual of its low-order solve (0: 1e-3) */
     int dsa_maxit;        /* iteration limit of its low-order solve (0: 4000) */
+    int plain_cycles;     /* BTE_FORM_PLAIN: 0 or 1 = the reference's semantics (a system stops at
+                             inner_maxit and keeps its last iterate); k > 1 = an unconverged system
+                             goes on to k x inner_maxit iterations and keeps the iterate with the
+                             smallest residual seen after inner_maxit / 2 */
 } bte_options;
 
 /* Per-kernel totals of the last profiled bte_solve. */
@@ -149,7 +154,9 @@ bte_status bte_set_quadrature(bte_ctx* ctx, int n_dir, const double* s, const do
                               const double* omega, int DM, int num_theta, int num_phi,
                               double solid_angle, double T_ref);
 
-/* Bands (src/BTEBand.cpp:8-26): group velocity, relaxation time, Ctot, Lr. */
+/* Bands (src/BTEBand.cpp:8-26): group velocity, relaxation time, Ctot, Lr.
+ * A NaN or infinite value returns BTE_ERR_NUMERICAL (the reference would carry
+ * it into every outer iterate). */
 bte_status bte_set_bands(bte_ctx* ctx, int n_band, const double* vg, const double* tau,
                          const double* C, const double* Lr);
 

@@ -20,6 +20,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
 REF_LIB_PATH = os.path.join(HERE, "_ref", "libbte_ref.so")
 REF_BIN_PATH = os.path.join(HERE, "_ref", "BTEcmd_ref")
+# Where the reference's sources are mounted, when they are (the recipes that
+# compile them read it from STATICBTESOLVER_REFERENCE; the GPU hosts have none).
+REFERENCE_ROOT = os.environ.get("STATICBTESOLVER_REFERENCE", "/root/reference")
 
 INNER_GMRES_ILU0 = 0
 INNER_BICGSTAB = 1
@@ -38,7 +41,7 @@ def build(quiet: bool = True) -> None:
         raise RuntimeError("oracle build failed:\n" + out.stdout + out.stderr)
 
 
-def build_reference(ref_root: str = "/root/reference") -> bool:
+def build_reference(ref_root: str = REFERENCE_ROOT) -> bool:
     """Compile the reference's own CPU solver into oracle/_ref (if its sources exist)."""
     if not os.path.isdir(os.path.join(ref_root, "src")):
         return False

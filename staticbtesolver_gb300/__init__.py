@@ -48,7 +48,8 @@ class Options(C.Structure):
     _fields_ = [("max_iter", C.c_int), ("tol", C.c_double), ("form", C.c_int), ("inner_tol", C.c_double),
                 ("inner_maxit", C.c_int), ("batch_systems", C.c_int), ("on_iteration", ITER_CB),
                 ("user", C.c_void_p), ("profile", C.c_int), ("accel", C.c_int), ("accel_every", C.c_int),
-                ("keep_history", C.c_int), ("dsa", C.c_int), ("dsa_tol", C.c_double), ("dsa_maxit", C.c_int)]
+                ("keep_history", C.c_int), ("dsa", C.c_int), ("dsa_tol", C.c_double), ("dsa_maxit", C.c_int),
+                ("plain_cycles", C.c_int)]
 
 
 class KernelStat(C.Structure):
@@ -301,11 +302,12 @@ class Context:
 
     def solve(self, max_iter=1000, tol=1e-5, form=FORM_PLAIN, inner_tol=1e-9, inner_maxit=1000,
               batch_systems=0, on_iteration=None, raise_on_not_converged=False, profile=False, accel=0,
-              accel_every=8, keep_history=False, dsa=False, dsa_tol=0.0, dsa_maxit=0):
+              accel_every=8, keep_history=False, dsa=False, dsa_tol=0.0, dsa_maxit=0, plain_cycles=0):
         o = default_options(max_iter=int(max_iter), tol=float(tol), form=int(form), inner_tol=float(inner_tol),
                             inner_maxit=int(inner_maxit), batch_systems=int(batch_systems), profile=int(profile),
                             accel=int(accel), accel_every=int(accel_every), keep_history=int(bool(keep_history)),
-                            dsa=int(bool(dsa)), dsa_tol=float(dsa_tol), dsa_maxit=int(dsa_maxit))
+                            dsa=int(bool(dsa)), dsa_tol=float(dsa_tol), dsa_maxit=int(dsa_maxit),
+                            plain_cycles=int(plain_cycles))
         cb = None
         if on_iteration is not None:
             cb = ITER_CB(lambda _u, it, m, ms: on_iteration(it, m, ms))

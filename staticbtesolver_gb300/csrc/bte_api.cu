@@ -158,8 +158,13 @@ struct bte_ctx {
     bool dsa_ready = false;
     int dsa_walls = 0;   // wall faces held at a fixed temperature
     int dsa_blocks = 0;  // cooperative grid of k_dsa_cg
-    DevBuf d_lo_nb, d_lo_w, d_lo_dsc, d_Tsrc, d_dsa_b, d_dsa_x;
-    DevBuf cg_r, cg_aw, cg_s, cg_x, cg_p, cg_part, cg_bar, cg_stat, cg_relres;
+    DevBuf d_lo_nb, d_lo_w, d_lo_dsc, d_Tsrc, d_dsa_b, d_dsa_x, d_dsa_xc, d_dsa_order, d_dsa_pos;
+    DevBuf d_co_ainv, d_co_need_ptr, d_co_need, d_co_sums, d_co_sums0;
+    DevBuf cg_r, cg_aw, cg_s, cg_x, cg_p, cg_u, cg_part, cg_bar, cg_stat, cg_relres;
+    std::vector<int> dsa_order;  // position -> cell of the low-order solve's numbering
+    int dsa_chunk = 0, dsa_seg = 0, dsa_n_agg = 0;
+    bool dsa_stage = false;  // rows of the coarse inverse staged in shared memory
+    size_t dsa_smem = 0;     // dynamic shared memory of k_dsa_pcg
     // results
     double* e_curr = nullptr;
     double* e_prev = nullptr;
@@ -360,6 +365,10 @@ bte_status bte_set_bands(bte_ctx* ctx, int n_band, const double* vg, const doubl
     if (!ctx) return BTE_ERR_INVALID_ARGUMENT;
     if (n_band <= 0 || !vg || !tau || !C || !Lr)
         return fail(ctx, BTE_ERR_INVALID_ARGUMENT, "bte_set_bands: n_band <= 0 or null array");
+    for (int b = 0; b < n_band; ++b)
+        if (!std::isfinite(vg[b]) || !std::isfinite(tau[b]) || !std::isfinite(C[b]) || !std::isfinite(Lr[b]))
+            return fail(ctx, BTE_ERR_NUMERICAL, "bte_set_bands: non-finite group velocity, relaxation time, "
+                                                "heat capacity or Lr in band " + std::to_string(b));
     ctx->n_band = n_band;
     ctx->vg.assign(vg, vg + n_band);
     ctx->tau.assign(tau, tau + n_band);
@@ -654,65 +663,114 @@ constexpr double kDsaBeta = 0.25;
 constexpr int kDsaThreads = bte::dsa::THREADS;
 
 // Upload a low-order operator (nb, W as bte_dsa_solve takes them) in its
-// symmetrically scaled form and size the conjugate-gradient work for n cells.
+// symmetrically scaled form, in a locality order of the cells with the
+// two-level preconditioner's coarse operator, and size the conjugate-gradient
+// work for n cells.
 static bte_status dsa_prepare(bte_ctx* ctx, int n, int F, const int* nb, const double* W) {
     cudaStream_t st = ctx->stream;
-    std::vector<double> diag(n, 0.0), dsc(n, 0.0);
-    for (int f = 0; f < F; ++f)
-        for (int c = 0; c < n; ++c) diag[c] += W[(size_t)f * n + c];
-    for (int c = 0; c < n; ++c) dsc[c] = diag[c] > 0.0 ? 1.0 / std::sqrt(diag[c]) : 0.0;
-    std::vector<float> w((size_t)F * n, 0.0f);
-    std::vector<int> nbv((size_t)F * n, -1);
-    for (int f = 0; f < F; ++f)
-        for (int c = 0; c < n; ++c) {
-            const size_t q = (size_t)f * n + c;
-            const int o = nb[q];
-            if (o >= 0 && W[q] > 0.0) {
-                w[q] = (float)(W[q] * dsc[c] * dsc[o]);
-                nbv[q] = o;
-            }
-        }
-    BTE_CUDA(upload(ctx->d_lo_nb, nbv, st));
-    BTE_CUDA(upload(ctx->d_lo_w, w, st));
-    BTE_CUDA(upload(ctx->d_lo_dsc, dsc, st));
     int coop = 0, sms = 0, occ = 0;
     BTE_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, ctx->device));
     if (!coop) return fail(ctx, BTE_ERR_CUDA, "dsa: the device does not support cooperative launches");
     BTE_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
-    BTE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, bte::dsa::k_dsa_cg, kDsaThreads, 0));
-    if (occ < 1) return fail(ctx, BTE_ERR_CUDA, "dsa: the low-order kernel cannot be resident");
     // at most one block per SM: enough threads for the cells, few blocks at each barrier
-    const int want = std::max(1, std::min(sms, (n + kDsaThreads - 1) / kDsaThreads));
-    ctx->dsa_blocks = std::min(want, occ * sms);
+    const int nblk = std::max(1, std::min(sms, (n + kDsaThreads - 1) / kDsaThreads));
+    ctx->dsa_blocks = nblk;
+    std::vector<double> diag(n, 0.0), dsc(n, 0.0);
+    for (int f = 0; f < F; ++f)
+        for (int c = 0; c < n; ++c) diag[c] += W[(size_t)f * n + c];
+    for (int c = 0; c < n; ++c) dsc[c] = diag[c] > 0.0 ? 1.0 / std::sqrt(diag[c]) : 0.0;
+    // locality order: contiguous position ranges are compact groups of cells
+    std::vector<int> cm((size_t)n * F);
+    for (int f = 0; f < F; ++f)
+        for (int c = 0; c < n; ++c) cm[(size_t)c * F + f] = W[(size_t)f * n + c] > 0.0 ? nb[(size_t)f * n + c] : -1;
+    const int agg_cells = std::max(1, n / (nblk * bte::dsa::AGG));
+    bte::locality_order(n, F, cm.data(), std::max(8, agg_cells / 2), ctx->dsa_order);
+    const std::vector<int>& order = ctx->dsa_order;
+    std::vector<int> pos(n);
+    for (int k = 0; k < n; ++k) pos[order[k]] = k;
+    std::vector<double> wd((size_t)F * n, 0.0), dscp(n);
+    std::vector<float> w((size_t)F * n, 0.0f);
+    std::vector<int> nbv((size_t)F * n, -1);
+    for (int k = 0; k < n; ++k) {
+        const int c = order[k];
+        dscp[k] = dsc[c];
+        for (int f = 0; f < F; ++f) {
+            const size_t q = (size_t)f * n + c;
+            const int o = nb[q];
+            if (o >= 0 && W[q] > 0.0) {
+                const size_t qk = (size_t)f * n + k;
+                wd[qk] = W[q] * dsc[c] * dsc[o];
+                w[qk] = (float)wd[qk];
+                nbv[qk] = pos[o];
+            }
+        }
+    }
+    bte::DsaCoarse co;
+    if (!bte::dsa_coarse(n, F, nbv.data(), wd.data(), nblk, bte::dsa::AGG, co))
+        return fail(ctx, BTE_ERR_INVALID_ARGUMENT,
+                    "dsa: the low-order operator is singular (no wall held at a fixed temperature)");
+    ctx->dsa_chunk = co.chunk;
+    ctx->dsa_seg = co.seg;
+    ctx->dsa_n_agg = co.n_agg;
+    // the block's rows of the coarse inverse live in shared memory when they fit
+    int rows = 0, smem_max = 0;
+    for (int k = 0; k < nblk; ++k) rows = std::max(rows, co.need_ptr[k + 1] - co.need_ptr[k]);
+    BTE_CUDA(cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device));
+    const size_t staged = sizeof(float) * (2 + (size_t)rows) * co.n_agg;
+    ctx->dsa_stage = staged + 16384 <= (size_t)smem_max;
+    ctx->dsa_smem = ctx->dsa_stage ? staged : sizeof(float) * 2 * (size_t)co.n_agg;
+    BTE_CUDA(cudaFuncSetAttribute(bte::dsa::k_dsa_pcg, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)ctx->dsa_smem));
+    BTE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, bte::dsa::k_dsa_pcg, kDsaThreads, ctx->dsa_smem));
+    if (occ < 1 || nblk > occ * sms) return fail(ctx, BTE_ERR_CUDA, "dsa: the low-order kernel cannot be resident");
+    BTE_CUDA(upload(ctx->d_lo_nb, nbv, st));
+    BTE_CUDA(upload(ctx->d_lo_w, w, st));
+    BTE_CUDA(upload(ctx->d_lo_dsc, dscp, st));
+    BTE_CUDA(upload(ctx->d_dsa_order, order, st));
+    BTE_CUDA(upload(ctx->d_dsa_pos, pos, st));
+    BTE_CUDA(upload(ctx->d_co_ainv, co.ainv, st));
+    BTE_CUDA(upload(ctx->d_co_need_ptr, co.need_ptr, st));
+    BTE_CUDA(upload(ctx->d_co_need, co.need, st));
+    BTE_CUDA(ctx->d_co_sums.alloc(sizeof(float) * 6 * (size_t)co.n_agg));
+    BTE_CUDA(ctx->d_co_sums0.alloc(sizeof(double) * (size_t)co.n_agg));
+    BTE_CUDA(cudaMemsetAsync(ctx->d_co_sums.p, 0, ctx->d_co_sums.bytes, st));
+    BTE_CUDA(cudaMemsetAsync(ctx->d_co_sums0.p, 0, ctx->d_co_sums0.bytes, st));
     const size_t nn = (size_t)n;
     BTE_CUDA(ctx->cg_r.alloc(sizeof(float) * 2 * nn));
     BTE_CUDA(ctx->cg_aw.alloc(sizeof(float) * 2 * nn));
     BTE_CUDA(ctx->cg_s.alloc(sizeof(float) * 2 * nn));
     BTE_CUDA(ctx->cg_x.alloc(sizeof(float) * nn));
     BTE_CUDA(ctx->cg_p.alloc(sizeof(float) * nn));
-    BTE_CUDA(ctx->cg_part.alloc(sizeof(double) * (2 * (size_t)ctx->dsa_blocks + 2)));
+    BTE_CUDA(ctx->cg_u.alloc(sizeof(float) * nn));
+    BTE_CUDA(ctx->cg_part.alloc(sizeof(double) * (2 * (size_t)nblk + 2)));
     BTE_CUDA(ctx->cg_bar.alloc(sizeof(unsigned) * 2));
     BTE_CUDA(ctx->cg_stat.alloc(sizeof(int) * 4));
     BTE_CUDA(ctx->cg_relres.alloc(sizeof(double)));
     BTE_CUDA(ctx->d_dsa_b.alloc(sizeof(double) * nn));
     BTE_CUDA(ctx->d_dsa_x.alloc(sizeof(double) * nn));
+    BTE_CUDA(ctx->d_dsa_xc.alloc(sizeof(double) * nn));
     BTE_CUDA(cudaMemsetAsync(ctx->cg_stat.p, 0, sizeof(int) * 4, st));
     return BTE_OK;
 }
 
-// One low-order solve of d_dsa_b into d_dsa_x (cooperative launch, every block resident).
+// One low-order solve of d_dsa_b into d_dsa_x, both in the solve's numbering
+// (cooperative launch, every block resident).
 static bte_status dsa_launch(bte_ctx* ctx, int n, int F, double tol, int maxit) {
     cudaStream_t st = ctx->stream;
     BTE_CUDA(cudaMemsetAsync(ctx->cg_bar.p, 0, sizeof(unsigned) * 2, st));
     bte::dsa::Lo lo{n, F, ctx->d_lo_nb.as<int>(), ctx->d_lo_w.as<float>(), ctx->d_lo_dsc.as<double>()};
+    bte::dsa::Coarse co{ctx->dsa_chunk, ctx->dsa_seg, ctx->dsa_n_agg, ctx->dsa_stage ? 1 : 0,
+                        ctx->d_co_ainv.as<float>(),
+                        ctx->d_co_need_ptr.as<int>(), ctx->d_co_need.as<int>(), ctx->d_co_sums.as<float>(),
+                        ctx->d_co_sums0.as<double>()};
     bte::dsa::CgWork wk{ctx->cg_r.as<float>(), ctx->cg_aw.as<float>(), ctx->cg_s.as<float>(), ctx->cg_x.as<float>(),
-                        ctx->cg_p.as<float>(), ctx->cg_part.as<double>(), ctx->cg_bar.as<unsigned>(),
-                        ctx->cg_stat.as<int>(), ctx->cg_relres.as<double>()};
+                        ctx->cg_p.as<float>(), ctx->cg_u.as<float>(), ctx->cg_part.as<double>(),
+                        ctx->cg_bar.as<unsigned>(), ctx->cg_stat.as<int>(), ctx->cg_relres.as<double>()};
     const double* b = ctx->d_dsa_b.as<double>();
     double* x = ctx->d_dsa_x.as<double>();
-    void* args[] = {&lo, &wk, &b, &tol, &maxit, &x};
-    BTE_CUDA(cudaLaunchCooperativeKernel((const void*)bte::dsa::k_dsa_cg, dim3(ctx->dsa_blocks), dim3(kDsaThreads),
-                                         args, 0, st));
+    void* args[] = {&lo, &co, &wk, &b, &tol, &maxit, &x};
+    BTE_CUDA(cudaLaunchCooperativeKernel((const void*)bte::dsa::k_dsa_pcg, dim3(ctx->dsa_blocks), dim3(kDsaThreads),
+                                         args, ctx->dsa_smem, st));
     BTE_LAUNCHED();
     return BTE_OK;
 }
@@ -848,7 +906,6 @@ static bte_status build_sweep_plan(bte_ctx* ctx) {
 
 // Solve all systems of one batch (bands b0 .. b0+nbb-1, every direction) with
 // the plain FP64 BiCGSTAB; x lands in e_curr.
-constexpr int kPlainCycles = 3;
 
 static bte_status solve_batch_plain(bte_ctx* ctx, int b0, int nbb, const bte_options& o, bte_report& rep) {
     {
@@ -877,14 +934,12 @@ static bte_status solve_batch_plain(bte_ctx* ctx, int b0, int nbb, const bte_opt
                    ctx->w_b.as<double>(), ctx->n));
 
     const int maxit = o.inner_maxit;
-    // a system not converged after maxit iterations goes on up to
-    // kPlainCycles x maxit and returns its best iterate if it still has not
-    // (the reference stops at maxit and returns its last iterate).  On
-    // 78,190-cell 2D meshes (the reference's 2Dcase5) the residual of this
-    // right-Jacobi BiCGSTAB stays at 1e1..1e5 |b| for 600-900 iterations and
-    // then drops to 1e-10 within ~50, so whether it lands before 1000 is
-    // decided by rounding.
-    const int total = maxit * kPlainCycles;
+    // The reference stops a system at maxit and keeps its last iterate
+    // (cycles = 1, no best-iterate copy).  With plain_cycles = k > 1 a system
+    // not converged after maxit iterations goes on up to k x maxit and keeps
+    // its best iterate if it still has not.
+    const int cycles = std::max(1, o.plain_cycles);
+    const int total = maxit * cycles;
     if (ctx->active_cap < total + 2) {
         BTE_CUDA(ctx->s_active.alloc(sizeof(int) * (total + 2)));
         ctx->active_cap = total + 2;
@@ -897,9 +952,11 @@ static bte_status solve_batch_plain(bte_ctx* ctx, int b0, int nbb, const bte_opt
     bte::BicgVecs<double> v{ctx->w_r.as<double>(), ctx->w_rw.as<double>(), ctx->w_p.as<double>(),
                             ctx->w_ph.as<double>(), ctx->w_q.as<double>(), ctx->w_z.as<double>(),
                             ctx->w_t.as<double>(), ctx->w_b.as<double>(), ctx->w_invD.as<double>(), ctx->Np};
-    v.xb = ctx->w_xb.as<double>();  // the best iterate is kept and returned
-    bs.cycles = kPlainCycles;
-    bs.track_from = maxit / 2;  // systems converging before that never copy x
+    if (cycles > 1) {
+        v.xb = ctx->w_xb.as<double>();  // the best iterate is kept and returned
+        bs.cycles = cycles;
+        bs.track_from = maxit / 2;  // systems converging before that never copy x
+    }
     BTE_LAUNCH(KK_INIT, -1, S * N * 7 * w + geo / 2, 0, bte::k_bicg_init<<<grid, bte::THREADS, 0, st>>>(op, v, bs));
     BTE_LAUNCH(KK_INIT, -1, 0, 0, bte::k_bicg_init_scalars<<<(S + 127) / 128, 128, 0, st>>>(bs, nullptr));
     int i = 1;
@@ -1630,10 +1687,9 @@ extern "C" bte_status bte_solve(bte_ctx* ctx, const bte_options* opts, bte_repor
             const int n = ctx->n;
             BTE_CUDA(cudaEventRecord(ev[7], st));
             BTE_LAUNCH(KK_DSA, -1, 3.0 * n * 8.0, 0,
-                       bte::dsa::k_dsa_rhs<<<(n + 255) / 256, 256, 0, st>>>(ctx->d_T.as<double>(),
-                                                                            ctx->d_Tsrc.as<double>(),
-                                                                            ctx->d_volume.as<double>(), n,
-                                                                            ctx->d_dsa_b.as<double>()));
+                       bte::dsa::k_dsa_rhs<<<(n + 255) / 256, 256, 0, st>>>(
+                           ctx->d_T.as<double>(), ctx->d_Tsrc.as<double>(), ctx->d_volume.as<double>(),
+                           ctx->d_dsa_order.as<int>(), n, ctx->d_dsa_b.as<double>()));
             {
                 size_t slot = 0;
                 BTE_CUDA(prof_begin(ctx, &slot));
@@ -1643,13 +1699,14 @@ extern "C" bte_status bte_solve(bte_ctx* ctx, const bte_options* opts, bte_repor
             }
             BTE_LAUNCH(KK_DSA, -1, (2.0 + NB) * n * 8.0, 0,
                        bte::dsa::k_dsa_apply<<<(n + 255) / 256, 256, 0, st>>>(
-                           ctx->d_dsa_x.as<double>(), ctx->d_Cb.as<double>(), ctx->solid_angle, ctx->T_ref, n, NB,
-                           Np, ctx->d_T.as<double>(), ctx->d_ebar.as<double>()));
+                           ctx->d_dsa_x.as<double>(), ctx->d_dsa_pos.as<int>(), ctx->d_Cb.as<double>(),
+                           ctx->solid_angle, ctx->T_ref, n, NB, Np, ctx->d_T.as<double>(), ctx->d_ebar.as<double>(),
+                           ctx->d_dsa_xc.as<double>()));
             if (ctx->nbcell > 0) {
                 const int nt = ctx->nbcell * ND;
                 BTE_LAUNCH(KK_DSA, -1, 2.0 * nt * NB * 8.0, 0,
                            bte::dsa::k_dsa_shift_boundary<<<dim3((nt + 255) / 256, NB), 256, 0, st>>>(
-                               ctx->d_dsa_x.as<double>(), ctx->d_bcell.as<int>(), ctx->nbcell, ctx->d_Cb.as<double>(),
+                               ctx->d_dsa_xc.as<double>(), ctx->d_bcell.as<int>(), ctx->nbcell, ctx->d_Cb.as<double>(),
                                ctx->solid_angle, ND, Np, ctx->e_curr));
             }
             BTE_CUDA(cudaEventRecord(ev[8], st));
@@ -1917,16 +1974,19 @@ static bte_status dsa_solve_impl(bte_ctx* ctx, int n, int F, const int* nb, cons
     BTE_CUDA(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
     bte_status s = dsa_prepare(ctx, n, F, nb, W);
     if (s != BTE_OK) return s;
-    BTE_CUDA(cudaMemcpyAsync(ctx->d_dsa_b.p, b, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+    std::vector<double> bp(n), xp(n);
+    for (int k = 0; k < n; ++k) bp[k] = b[ctx->dsa_order[k]];
+    BTE_CUDA(cudaMemcpyAsync(ctx->d_dsa_b.p, bp.data(), sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
     s = dsa_launch(ctx, n, F, tol, maxit);
     if (s != BTE_OK) return s;
     int stat[4] = {0, 0, 0, 0};
     double rr = 0.0;
-    BTE_CUDA(cudaMemcpyAsync(x, ctx->d_dsa_x.p, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    BTE_CUDA(cudaMemcpyAsync(xp.data(), ctx->d_dsa_x.p, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
     BTE_CUDA(cudaMemcpyAsync(stat, ctx->cg_stat.p, sizeof(stat), cudaMemcpyDeviceToHost, ctx->stream));
     BTE_CUDA(cudaMemcpyAsync(&rr, ctx->cg_relres.p, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     BTE_CUDA(cudaStreamSynchronize(ctx->stream));
     if (stat[1]) return fail(ctx, BTE_ERR_CUDA, "a grid barrier of the low-order solve timed out");
+    for (int k = 0; k < n; ++k) x[ctx->dsa_order[k]] = xp[k];
     if (iterations) *iterations = stat[0];
     if (relres) *relres = rr;
     return BTE_OK;

@@ -11,15 +11,17 @@
 // transport iterates still decides convergence, and the result is the last
 // transport iterate, never a corrected field.
 //
-// The diffusion solve is one persistent cooperative kernel: conjugate
-// gradients in the Chronopoulos-Gear form on the symmetrically Jacobi-scaled
-// operator (unit diagonal), FP32 vectors, FP64 dot products, with one grid
-// barrier per iteration, which also completes the iteration's two dot
-// products.  One barrier suffices because r, w = A r and s are kept in two
-// parity copies: after a barrier every block recomputes the new residual of
-// its cells' neighbours from the previous iteration's r, w and s with the same
-// fused operations as the neighbours' owners, so the values agree to the bit
-// and the product A r_new needs no second barrier.
+// The diffusion solve is one persistent cooperative kernel: preconditioned
+// conjugate gradients in the Chronopoulos-Gear form on the symmetrically
+// Jacobi-scaled operator (unit diagonal), with a two-level preconditioner
+// (the identity plus a coarse correction on aggregates of cells), FP32
+// vectors, FP64 dot products, and one grid barrier per iteration, which also
+// completes the iteration's two dot products.  One barrier suffices because r,
+// w = A u and s are kept in two parity copies: after a barrier every block
+// recomputes the new residual of its cells' neighbours from the previous
+// iteration's r, w and s with the same fused operations as the neighbours'
+// owners, so the values agree to the bit, and the coarse correction of the
+// new residual follows from aggregate sums published with the dot products.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -32,9 +34,10 @@ constexpr int THREADS = 512;
 // polls of the barrier flag before a block gives up (~a second)
 constexpr long long kBarrierPolls = 1ll << 22;
 
-// The low-order operator, symmetrically scaled: unit diagonal, off-diagonal
-// -w[f][c] coupling c to nb[f][c]; dsc[c] = 1 / sqrt(diagonal) (0 for a cell
-// with no coupling at all).
+// The low-order operator in the solve's cell numbering (a locality order of
+// the mesh's cells, dsa_setup.h), symmetrically scaled: unit diagonal,
+// off-diagonal -w[f][c] coupling c to nb[f][c]; dsc[c] = 1 / sqrt(diagonal)
+// (0 for a cell with no coupling at all).
 struct Lo {
     int n, F;
     const int* nb;     // [F][n]
@@ -42,18 +45,38 @@ struct Lo {
     const double* dsc; // [n]
 };
 
+// Aggregates per block of the coarse correction (dsa_setup.h dsa_coarse).
+constexpr int AGG = 4;
+
+// The coarse correction of the preconditioner M^-1 = I + P A_c^-1 P^T: block
+// k owns cells [k chunk, (k+1) chunk), split into AGG aggregates of seg cells.
+struct Coarse {
+    int chunk, seg, n_agg;
+    int stage;             // nonzero: the block's rows of ainv are copied to shared memory once
+    const float* ainv;     // [n_agg][n_agg]
+    const int* need_ptr;   // [nblk+1]
+    const int* need;       // aggregates of a block's cells and of their neighbours
+    float* sums;           // [2][n_agg][3] published aggregate sums of (r, A u, s), two parity copies
+    double* sums0;         // [n_agg] aggregate sums of the scaled right-hand side
+    __device__ __forceinline__ int agg_of(int c) const {
+        const int k = c / chunk;
+        return k * AGG + (c - k * chunk) / seg;
+    }
+};
+
 // Work and control of one solve (all device memory, 16-byte aligned).
 struct CgWork {
     float* r;          // [2][n] residual, two parity copies
-    float* aw;         // [2][n] A r
+    float* aw;         // [2][n] A u
     float* s;          // [2][n] A p
     float* x;          // [n]
     float* p;          // [n]
+    float* u;          // [n] preconditioned residual
     double* part;      // [nblk][2] per-block partial dot products, then [2] the grid's sums
     unsigned* bar;     // [2] barrier arrival count and generation (zero before the launch)
     int* stat;         // [0] iterations of the last solve, [1] error flag (barrier timeout),
                        // [2] iterations summed over solves
-    double* relres;    // [1] final sqrt(r.r / r0.r0)
+    double* relres;    // [1] final sqrt(r.M r / r0.M r0)
 };
 
 __device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
@@ -160,24 +183,116 @@ __device__ __forceinline__ float next_residual(const CgWork& wk, int P, int c, f
     return __fmaf_rn(malpha, __fmaf_rn(beta, so, wi), ri);
 }
 
-// Solve A x = b (A = the low-order operator before scaling) for b[n] (FP64)
-// into xout[n] (FP64), relative tolerance tol on ||r|| of the scaled system,
-// at most maxit iterations.  Launched cooperatively with every block resident.
-__global__ void __launch_bounds__(THREADS) k_dsa_cg(Lo lo, CgWork wk, const double* __restrict__ b, double tol,
-                                                   int maxit, double* __restrict__ xout) {
+// Block sum of the per-thread aggregate partials acc[AGG][3] in a fixed
+// order; thread t < 3 AGG holds sum number t afterwards (in out).
+__device__ __forceinline__ float block_sum_aggs(const float (&acc)[AGG][3], float* red /* [32][3 AGG] */) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int a = 0; a < AGG; ++a)
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            float v = acc[a][q];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+            if (lane == 0) red[warp * 3 * AGG + a * 3 + q] = v;
+        }
+    __syncthreads();
+    float t = 0.0f;
+    if (threadIdx.x < 3 * AGG)
+        for (int w = 0; w < nw; ++w) t += red[w * 3 * AGG + threadIdx.x];
+    __syncthreads();
+    return t;
+}
+
+// sX[J] = (A_c^-1 R)[J] for the aggregates J this block needs, R = sR (all
+// aggregates): one warp per row, lanes over the columns (four running sums
+// per lane, added in a fixed order), fixed butterfly.  rows: the block's rows
+// of A_c^-1 in shared memory (stage) or in global memory.
+__device__ __forceinline__ void coarse_rows(const Coarse& co, const float* rows, const float* sR, float* sX) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int j0 = co.need_ptr[blockIdx.x], j1 = co.need_ptr[blockIdx.x + 1];
+    const int m = co.n_agg;
+    for (int j = j0 + warp; j < j1; j += nw) {
+        const int J = co.need[j];
+        const float* row = co.stage ? rows + (size_t)(j - j0) * m : co.ainv + (size_t)J * m;
+        float v0 = 0.0f, v1 = 0.0f, v2 = 0.0f, v3 = 0.0f;
+        int K = lane;
+        for (; K + 96 < m; K += 128) {
+            v0 = __fmaf_rn(row[K], sR[K], v0);
+            v1 = __fmaf_rn(row[K + 32], sR[K + 32], v1);
+            v2 = __fmaf_rn(row[K + 64], sR[K + 64], v2);
+            v3 = __fmaf_rn(row[K + 96], sR[K + 96], v3);
+        }
+        for (; K < m; K += 32) v0 = __fmaf_rn(row[K], sR[K], v0);
+        float v = (v0 + v1) + (v2 + v3);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) sX[J] = v;
+    }
+}
+
+// Solve A x = b (A = the low-order operator before scaling, both in the
+// solve's numbering) for b[n] (FP64) into xout[n] (FP64): preconditioned
+// conjugate gradients, M^-1 = I + P A_c^-1 P^T on the scaled operator,
+// relative tolerance tol on sqrt(r.M r), at most maxit iterations.  Launched
+// cooperatively with one block per cell range of the coarse set-up, every
+// block resident.  Dynamic shared memory: (2 + rows) n_agg floats, rows = the
+// longest need list when co.stage, else 0.
+//
+// The coarse correction needs P^T r_{i+1} of every aggregate before any block
+// can form u_{i+1} = M^-1 r_{i+1}; it follows without another barrier from
+// the aggregate sums the owners published with the last dot products:
+//   P^T r_{i+1} = P^T r_i - alpha_i (P^T w_i + beta_i P^T s_{i-1}).
+__global__ void __launch_bounds__(THREADS) k_dsa_pcg(Lo lo, Coarse co, CgWork wk, const double* __restrict__ b,
+                                                    double tol, int maxit, double* __restrict__ xout) {
+    extern __shared__ float smem[];
+    float* sR = smem;              // [n_agg] P^T r of every aggregate
+    float* sX = smem + co.n_agg;   // [n_agg] coarse solution (the needed entries)
+    float* sA = smem + 2 * co.n_agg;  // the block's rows of A_c^-1 (stage)
+    if (co.stage) {
+        const int j0 = co.need_ptr[blockIdx.x], j1 = co.need_ptr[blockIdx.x + 1];
+        for (int q = threadIdx.x; q < (j1 - j0) * co.n_agg; q += blockDim.x) {
+            const int j = q / co.n_agg, K = q - j * co.n_agg;
+            sA[q] = co.ainv[(size_t)co.need[j0 + j] * co.n_agg + K];
+        }
+    }
+    __shared__ float red[32 * 3 * AGG];
     const int n = lo.n, F = lo.F;
     const unsigned nblk = gridDim.x;
-    const int stride = gridDim.x * blockDim.x;
-    const int c0 = blockIdx.x * blockDim.x + threadIdx.x;
-    // phase 0: ||D^-1/2 b||
+    const int c_lo = blockIdx.x * co.chunk, c_hi = min(n, c_lo + co.chunk);
+    const int K0 = blockIdx.x * AGG;  // this block's first aggregate
+    // phase 0: ||D^-1/2 b|| and the aggregate sums of D^-1/2 b
     double nrm2 = 0.0, unused = 0.0;
-    for (int c = c0; c < n; c += stride) {
-        const double v = lo.dsc[c] * b[c];
-        nrm2 = fma(v, v, nrm2);
+    {
+        double a0[AGG] = {};
+        for (int c = c_lo + threadIdx.x; c < c_hi; c += blockDim.x) {
+            const double v = lo.dsc[c] * b[c];
+            nrm2 = fma(v, v, nrm2);
+            const int a = (c - c_lo) / co.seg;
+#pragma unroll
+            for (int k = 0; k < AGG; ++k)
+                if (k == a) a0[k] += v;
+        }
+        // aggregate sums in a fixed order: per warp, then warps in order
+        __shared__ double r0s[32][AGG];
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+        for (int k = 0; k < AGG; ++k) {
+            double v = a0[k];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+            if (lane == 0) r0s[warp][k] = v;
+        }
+        __syncthreads();
+        if (threadIdx.x < AGG) {
+            double t = 0.0;
+            for (int w = 0; w < nw; ++w) t += r0s[w][threadIdx.x];
+            __stcg(co.sums0 + K0 + threadIdx.x, t);
+        }
     }
     if (!grid_sum2(nrm2, unused, wk, nblk)) return;
     if (!(nrm2 > 0.0) || !isfinite(nrm2)) {  // nothing to correct
-        for (int c = c0; c < n; c += stride) xout[c] = 0.0;
+        for (int c = c_lo + threadIdx.x; c < c_hi; c += blockDim.x) xout[c] = 0.0;
         if (blockIdx.x == 0 && threadIdx.x == 0) {
             wk.stat[0] = 0;
             wk.relres[0] = 0.0;
@@ -185,24 +300,40 @@ __global__ void __launch_bounds__(THREADS) k_dsa_cg(Lo lo, CgWork wk, const doub
         return;
     }
     const double scale = sqrt(nrm2), inv = 1.0 / scale;
-    // r0 = D^-1/2 b / scale, w0 = A r0, s_{-1} = 0
+    // r0 = D^-1/2 b / scale, u0 = M^-1 r0, w0 = A u0, s_{-1} = p_{-1} = 0
+    for (int K = threadIdx.x; K < co.n_agg; K += blockDim.x) sR[K] = (float)(__ldcg(co.sums0 + K) * inv);
+    __syncthreads();
+    coarse_rows(co, sA, sR, sX);
+    __syncthreads();
+    float* pub = co.sums;  // parity 0
     double gamma = 0.0, delta = 0.0;
-    for (int c = c0; c < n; c += stride) {
-        const float rc = (float)(lo.dsc[c] * b[c] * inv);
-        float acc = rc;
-        for (int f = 0; f < F; ++f) {
-            const int o = lo.nb[(size_t)f * n + c];
-            if (o < 0) continue;
-            const float ro = (float)(lo.dsc[o] * b[o] * inv);
-            acc = __fmaf_rn(-lo.w[(size_t)f * n + c], ro, acc);
+    {
+        float acc[AGG][3] = {};
+        for (int c = c_lo + threadIdx.x; c < c_hi; c += blockDim.x) {
+            const float rc = (float)(lo.dsc[c] * b[c] * inv);
+            const float uc = rc + sX[co.agg_of(c)];
+            float wc = uc;
+            for (int f = 0; f < F; ++f) {
+                const int o = lo.nb[(size_t)f * n + c];
+                if (o < 0) continue;
+                const float uo = (float)(lo.dsc[o] * b[o] * inv) + sX[co.agg_of(o)];
+                wc = __fmaf_rn(-lo.w[(size_t)f * n + c], uo, wc);
+            }
+            __stcg(wk.r + c, rc);
+            __stcg(wk.aw + c, wc);
+            __stcg(wk.s + (size_t)n + c, 0.0f);
+            wk.u[c] = uc;
+            wk.x[c] = 0.0f;
+            wk.p[c] = 0.0f;
+            gamma = fma((double)rc, (double)uc, gamma);
+            delta = fma((double)wc, (double)uc, delta);
+            const int a = (c - c_lo) / co.seg;
+#pragma unroll
+            for (int k = 0; k < AGG; ++k)
+                if (k == a) { acc[k][0] += rc; acc[k][1] += wc; }
         }
-        __stcg(wk.r + c, rc);
-        __stcg(wk.aw + c, acc);
-        __stcg(wk.s + (size_t)n + c, 0.0f);
-        wk.x[c] = 0.0f;
-        wk.p[c] = 0.0f;
-        gamma = fma((double)rc, (double)rc, gamma);
-        delta = fma((double)acc, (double)rc, delta);
+        const float t = block_sum_aggs(acc, red);
+        if (threadIdx.x < 3 * AGG) __stcg(pub + (size_t)3 * K0 + threadIdx.x, t);
     }
     if (!grid_sum2(gamma, delta, wk, nblk)) return;
     const double gamma0 = gamma;
@@ -212,28 +343,48 @@ __global__ void __launch_bounds__(THREADS) k_dsa_cg(Lo lo, CgWork wk, const doub
     while (!stop && it < maxit) {
         const int P = it & 1;
         const float fa = (float)alpha, fma_ = -(float)alpha, fb = (float)beta;
+        // P^T r_{i+1} of every aggregate from the published sums, then the coarse solve
+        const float* got = co.sums + (size_t)3 * co.n_agg * P;
+        for (int K = threadIdx.x; K < co.n_agg; K += blockDim.x) {
+            const float sr = __ldcg(got + 3 * K), sw = __ldcg(got + 3 * K + 1), ss = __ldcg(got + 3 * K + 2);
+            sR[K] = __fmaf_rn(fma_, __fmaf_rn(fb, ss, sw), sr);
+        }
+        __syncthreads();
+        coarse_rows(co, sA, sR, sX);
+        __syncthreads();
         double gn = 0.0, dn = 0.0;
-        for (int c = c0; c < n; c += stride) {
+        float acc[AGG][3] = {};
+        for (int c = c_lo + threadIdx.x; c < c_hi; c += blockDim.x) {
             const float so = __ldcg(wk.s + (size_t)(P ^ 1) * n + c);
             const float wi = __ldcg(wk.aw + (size_t)P * n + c);
             const float ri = __ldcg(wk.r + (size_t)P * n + c);
             const float si = __fmaf_rn(fb, so, wi);
-            const float pc = __fmaf_rn(fb, wk.p[c], ri);
+            const float pc = __fmaf_rn(fb, wk.p[c], wk.u[c]);
             wk.p[c] = pc;
             wk.x[c] = __fmaf_rn(fa, pc, wk.x[c]);
             const float rn = __fmaf_rn(fma_, si, ri);
-            float acc = rn;
+            const float un = rn + sX[co.agg_of(c)];
+            float wn = un;
             for (int f = 0; f < F; ++f) {
                 const int o = lo.nb[(size_t)f * n + c];
                 if (o < 0) continue;
-                acc = __fmaf_rn(-lo.w[(size_t)f * n + c], next_residual(wk, P, o, fma_, fb, n), acc);
+                const float uo = next_residual(wk, P, o, fma_, fb, n) + sX[co.agg_of(o)];
+                wn = __fmaf_rn(-lo.w[(size_t)f * n + c], uo, wn);
             }
             __stcg(wk.s + (size_t)P * n + c, si);
             __stcg(wk.r + (size_t)(P ^ 1) * n + c, rn);
-            __stcg(wk.aw + (size_t)(P ^ 1) * n + c, acc);
-            gn = fma((double)rn, (double)rn, gn);
-            dn = fma((double)acc, (double)rn, dn);
+            __stcg(wk.aw + (size_t)(P ^ 1) * n + c, wn);
+            wk.u[c] = un;
+            gn = fma((double)rn, (double)un, gn);
+            dn = fma((double)wn, (double)un, dn);
+            const int a = (c - c_lo) / co.seg;
+#pragma unroll
+            for (int k = 0; k < AGG; ++k)
+                if (k == a) { acc[k][0] += rn; acc[k][1] += wn; acc[k][2] += si; }
         }
+        const float t = block_sum_aggs(acc, red);
+        if (threadIdx.x < 3 * AGG)
+            __stcg(co.sums + (size_t)3 * co.n_agg * (P ^ 1) + (size_t)3 * K0 + threadIdx.x, t);
         if (!grid_sum2(gn, dn, wk, nblk)) return;
         ++it;
         const double bnew = gn / gamma;
@@ -246,28 +397,35 @@ __global__ void __launch_bounds__(THREADS) k_dsa_cg(Lo lo, CgWork wk, const doub
             alpha = gn / den;
         }
     }
-    for (int c = c0; c < n; c += stride) xout[c] = (double)wk.x[c] * lo.dsc[c] * scale;
+    for (int c = c_lo + threadIdx.x; c < c_hi; c += blockDim.x) xout[c] = (double)wk.x[c] * lo.dsc[c] * scale;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         wk.stat[0] = it;
         wk.stat[2] += it;
-        wk.relres[0] = sqrt(gamma / gamma0);
+        wk.relres[0] = sqrt(fabs(gamma / gamma0));
     }
 }
 
-// Right-hand side V_c (T_c - T_src,c) of the low-order solve.
+// Right-hand side V_c (T_c - T_src,c) of the low-order solve, in its numbering:
+// position k holds cell order[k].
 __global__ void k_dsa_rhs(const double* __restrict__ T, const double* __restrict__ Tsrc,
-                          const double* __restrict__ volume, int n, double* __restrict__ b) {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c < n) b[c] = volume[c] * (T[c] - Tsrc[c]);
+                          const double* __restrict__ volume, const int* __restrict__ order, int n,
+                          double* __restrict__ b) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int c = order[k];
+    b[k] = volume[c] * (T[c] - Tsrc[c]);
 }
 
 // T += x, and the equilibrium energy density follows: ebar[b][c] = C_b / Omega_tot (T - T_ref).
-__global__ void k_dsa_apply(const double* __restrict__ x, const double* __restrict__ Cb, double solid_angle,
-                            double T_ref, int n, int n_band, size_t Np, double* __restrict__ T,
-                            double* __restrict__ ebar) {
+// x is in the solve's numbering (pos[c] = position of cell c); xc[c] receives it by cell.
+__global__ void k_dsa_apply(const double* __restrict__ x, const int* __restrict__ pos, const double* __restrict__ Cb,
+                            double solid_angle, double T_ref, int n, int n_band, size_t Np, double* __restrict__ T,
+                            double* __restrict__ ebar, double* __restrict__ xc) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= n) return;
-    const double t = T[c] + x[c];
+    const double dx = x[pos[c]];
+    xc[c] = dx;
+    const double t = T[c] + dx;
     T[c] = t;
     for (int b = 0; b < n_band; ++b) ebar[(size_t)b * Np + c] = Cb[b] / solid_angle * (t - T_ref);
 }

@@ -19,7 +19,9 @@
 // construction: each interior face is evaluated once and stored on both sides.
 #pragma once
 
+#include <algorithm>
 #include <cmath>
+#include <numeric>
 #include <vector>
 
 namespace bte {
@@ -91,6 +93,195 @@ inline void dsa_coefficients(int dim, int n, int F, const int* nbr, const double
             out.diag[c] += w;
             out.diag[o] += w;
         }
+}
+
+// ---------------------------------------------------------------------------
+// Two-level preconditioner of the low-order solve.
+//
+// The low-order operator's conjugate gradients need O(cells across the
+// domain) iterations with a diagonal preconditioner: too slow for the smooth
+// errors it exists to remove.  The preconditioner adds a coarse correction on
+// aggregates of neighbouring cells, M^-1 = I + P A_c^-1 P^T (on the
+// Jacobi-scaled operator, P piecewise constant on the aggregates,
+// A_c = P^T A P), which resolves every mode longer than an aggregate.  The
+// kernel gives each block one contiguous range of cells and splits it into
+// `per_block` contiguous aggregates, so the cells are first put in an order in
+// which contiguous ranges are compact: recursive bisection of the face
+// adjacency graph by breadth-first distance.
+
+// order[k] = the cell at position k.  Each range of more than `leaf` cells is
+// split at its median breadth-first distance from the farthest cell of a
+// first search (ties by index), then each half again.
+inline void locality_order(int n, int F, const int* nbr /* [n][F], < 0 none */, int leaf, std::vector<int>& order) {
+    order.resize(n);
+    std::iota(order.begin(), order.end(), 0);
+    std::vector<int> mark(n, -1), dist(n, -1), queue;
+    queue.reserve(n);
+    std::vector<std::pair<int, int>> stack{{0, n}};
+    int stamp = 0;
+    auto bfs = [&](int src, int id) {  // distances within the cells marked id; returns the last cell reached
+        queue.clear();
+        queue.push_back(src);
+        dist[src] = 0;
+        int last = src;
+        for (size_t h = 0; h < queue.size(); ++h) {
+            const int c = queue[h];
+            last = c;
+            for (int f = 0; f < F; ++f) {
+                const int o = nbr[(size_t)c * F + f];
+                if (o < 0 || o >= n || mark[o] != id || dist[o] >= 0) continue;
+                dist[o] = dist[c] + 1;
+                queue.push_back(o);
+            }
+        }
+        return last;
+    };
+    while (!stack.empty()) {
+        const auto [b, e] = stack.back();
+        stack.pop_back();
+        if (e - b <= std::max(leaf, 1)) continue;
+        const int id = stamp++;
+        for (int k = b; k < e; ++k) { mark[order[k]] = id; dist[order[k]] = -1; }
+        const int far = bfs(order[b], id);
+        for (int k = b; k < e; ++k) dist[order[k]] = -1;
+        bfs(far, id);
+        // cells the search did not reach (another component of the range) go last
+        std::stable_sort(order.begin() + b, order.begin() + e, [&](int x, int y) {
+            const long long dx = dist[x] < 0 ? (1ll << 40) : dist[x], dy = dist[y] < 0 ? (1ll << 40) : dist[y];
+            return dx != dy ? dx < dy : x < y;
+        });
+        const int mid = b + (e - b) / 2;
+        stack.push_back({mid, e});
+        stack.push_back({b, mid});
+    }
+}
+
+// Aggregates of the permuted cell range [0, n): block k owns [k chunk, (k+1) chunk)
+// and its aggregate a the cells with local index in [a seg, (a+1) seg).
+struct DsaCoarse {
+    int nblk = 0, per_block = 0, chunk = 0, seg = 0, n_agg = 0;
+    std::vector<float> ainv;   // [n_agg][n_agg] inverse of the coarse operator (identity rows for empty aggregates)
+    std::vector<int> need_ptr; // [nblk+1] aggregates a block's cells and their neighbours belong to
+    std::vector<int> need;
+    int agg_of(int c) const { const int k = c / chunk; return k * per_block + (c - k * chunk) / seg; }
+};
+
+// Coarse operator A_c = P^T A P of the scaled low-order operator (unit
+// diagonal, off-diagonal -w[f][c] to nb[f][c], in the permuted numbering) and
+// its inverse by a Cholesky factorisation.  Returns false if A_c is not
+// positive definite (no wall held at a fixed temperature).
+inline bool dsa_coarse(int n, int F, const int* nb /* [F][n] */, const double* w /* [F][n] */, int nblk,
+                       int per_block, DsaCoarse& out) {
+    out.nblk = nblk;
+    out.per_block = per_block;
+    out.chunk = (n + nblk - 1) / nblk;
+    out.seg = (out.chunk + per_block - 1) / per_block;
+    const int m = out.n_agg = nblk * per_block;
+    std::vector<double> Ac((size_t)m * m, 0.0);
+    std::vector<int> size(m, 0);
+    for (int c = 0; c < n; ++c) {
+        const int J = out.agg_of(c);
+        ++size[J];
+        Ac[(size_t)J * m + J] += 1.0;
+        for (int f = 0; f < F; ++f) {
+            const int o = nb[(size_t)f * n + c];
+            if (o < 0) continue;
+            Ac[(size_t)J * m + out.agg_of(o)] -= w[(size_t)f * n + c];
+        }
+    }
+    for (int J = 0; J < m; ++J)
+        if (size[J] == 0) Ac[(size_t)J * m + J] = 1.0;
+    // Cholesky A_c = L L^T (lower triangle in place), then the inverse column by column
+    std::vector<double> L = Ac;
+    for (int j = 0; j < m; ++j) {
+        double d = L[(size_t)j * m + j];
+        for (int k = 0; k < j; ++k) d -= L[(size_t)j * m + k] * L[(size_t)j * m + k];
+        if (!(d > 0.0)) return false;
+        d = std::sqrt(d);
+        L[(size_t)j * m + j] = d;
+        for (int i = j + 1; i < m; ++i) {
+            double v = L[(size_t)i * m + j];
+            for (int k = 0; k < j; ++k) v -= L[(size_t)i * m + k] * L[(size_t)j * m + k];
+            L[(size_t)i * m + j] = v / d;
+        }
+    }
+    out.ainv.assign((size_t)m * m, 0.0f);
+    std::vector<double> y(m);
+    for (int col = 0; col < m; ++col) {
+        for (int i = 0; i < m; ++i) {  // L y = e_col
+            double v = i == col ? 1.0 : 0.0;
+            for (int k = 0; k < i; ++k) v -= L[(size_t)i * m + k] * y[k];
+            y[i] = v / L[(size_t)i * m + i];
+        }
+        for (int i = m - 1; i >= 0; --i) {  // L^T x = y
+            double v = y[i];
+            for (int k = i + 1; k < m; ++k) v -= L[(size_t)k * m + i] * y[k];
+            y[i] = v / L[(size_t)i * m + i];
+        }
+        for (int i = 0; i < m; ++i) out.ainv[(size_t)i * m + col] = (float)y[i];
+    }
+    out.need_ptr.assign(nblk + 1, 0);
+    out.need.clear();
+    std::vector<int> seen(m, -1);
+    for (int k = 0; k < nblk; ++k) {
+        const int lo = k * out.chunk, hi = std::min(n, lo + out.chunk);
+        std::vector<int> list;
+        for (int c = lo; c < hi; ++c) {
+            const int J = out.agg_of(c);
+            if (seen[J] != k) { seen[J] = k; list.push_back(J); }
+            for (int f = 0; f < F; ++f) {
+                const int o = nb[(size_t)f * n + c];
+                if (o < 0) continue;
+                const int K = out.agg_of(o);
+                if (seen[K] != k) { seen[K] = k; list.push_back(K); }
+            }
+        }
+        std::sort(list.begin(), list.end());
+        out.need.insert(out.need.end(), list.begin(), list.end());
+        out.need_ptr[k + 1] = (int)out.need.size();
+    }
+    return true;
+}
+
+// Where each coupling of the low-order operator finds its neighbour when a
+// block keeps its own cells' state in shared memory: src[f][c] = the
+// neighbour's local index (0 .. chunk-1) when it is one of the block's cells,
+// chunk + h when it is the block's halo cell h (halo[halo_ptr[k] + h], a cell
+// of another block), -1 for no coupling.  Halo cells are sorted by index.
+struct DsaHalo {
+    int hmax = 0;                // longest halo of a block
+    std::vector<int> src;        // [F][n]
+    std::vector<int> halo_ptr;   // [nblk+1]
+    std::vector<int> halo;       // permuted cell numbers
+};
+
+inline void dsa_halo(int n, int F, const int* nb /* [F][n] */, int nblk, int chunk, DsaHalo& out) {
+    out.src.assign((size_t)F * n, -1);
+    out.halo_ptr.assign(nblk + 1, 0);
+    out.halo.clear();
+    out.hmax = 0;
+    std::vector<int> slot(n, -1);
+    for (int k = 0; k < nblk; ++k) {
+        const int lo = k * chunk, hi = std::min(n, lo + chunk);
+        std::vector<int> ext;
+        for (int c = lo; c < hi; ++c)
+            for (int f = 0; f < F; ++f) {
+                const int o = nb[(size_t)f * n + c];
+                if (o >= 0 && (o < lo || o >= hi)) ext.push_back(o);
+            }
+        std::sort(ext.begin(), ext.end());
+        ext.erase(std::unique(ext.begin(), ext.end()), ext.end());
+        for (size_t h = 0; h < ext.size(); ++h) slot[ext[h]] = (int)h;
+        for (int c = lo; c < hi; ++c)
+            for (int f = 0; f < F; ++f) {
+                const int o = nb[(size_t)f * n + c];
+                if (o < 0) continue;
+                out.src[(size_t)f * n + c] = (o >= lo && o < hi) ? o - lo : chunk + slot[o];
+            }
+        out.halo.insert(out.halo.end(), ext.begin(), ext.end());
+        out.halo_ptr[k + 1] = (int)out.halo.size();
+        out.hmax = std::max(out.hmax, (int)ext.size());
+    }
 }
 
 }  // namespace bte

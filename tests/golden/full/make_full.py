@@ -16,8 +16,14 @@ iterations interleaved with a CPU diffusion correction), and certifies it by
 one more uncorrected outer iteration; the fixture also keeps that
 certificate.
 
+cube200k (--iterations 2): the first outer iterations of the 3D configuration
+(196,608 tetrahedra x 5,120 systems; a full solve is days of CPU time): the
+fixture keeps T at every 4th cell, the sum of e over the cells of every
+(band, direction) system, the margins and the heat flux after them.
+
 Usage:  python tests/golden/full/make_full.py [square20k] [--threads 8]
         python tests/golden/full/make_full.py square100k --fixed-point
+        python tests/golden/full/make_full.py cube200k --iterations 2
 """
 from __future__ import annotations
 
@@ -49,9 +55,12 @@ def main() -> None:
     ap.add_argument("--threads", type=int, default=8)
     ap.add_argument("--max-iter", type=int, default=1000)
     ap.add_argument("--fixed-point", action="store_true")
+    ap.add_argument("--iterations", type=int, default=0)
     a = ap.parse_args()
     if a.fixed_point:
         return fixed_point(a)
+    if a.iterations:
+        return early(a)
     with tempfile.TemporaryDirectory() as tmp:
         p = synth.make_problem(a.name, tmp)
         h = file_hashes(p)
@@ -62,6 +71,21 @@ def main() -> None:
     print(a.name, "outer iterations", r.n_iter, "seconds", round(el, 1), "q", r.q)
     np.savez_compressed(os.path.join(HERE, f"{a.name}.npz"), T=r.T, q=r.q, q_band=r.q_band, margins=r.margins,
                         n_iter=r.n_iter, seconds=el, inner_iterations=r.inner["iterations"], hashes=json.dumps(h))
+
+
+def early(a) -> None:
+    with tempfile.TemporaryDirectory() as tmp:
+        p = synth.make_problem(a.name, tmp)
+        h = file_hashes(p)
+        o = Oracle(p.geo, p.bc_file, p.band_file, p.DM, p.num_theta, p.num_phi, p.T_ref, p.L_x, p.L_y, p.L_z)
+        t = time.time()
+        r = o.run(a.iterations, 0.0, threads=a.threads, want_energy=True)
+        el = time.time() - t
+    e_sums = r.e.sum(axis=2)  # [n_band][n_dir]
+    print(a.name, "outer iterations", r.n_iter, "seconds", round(el, 1), "margins", r.margins, "q", r.q)
+    np.savez_compressed(os.path.join(HERE, f"{a.name}_it{a.iterations}.npz"), T_every4=r.T[::4], T_sum=r.T.sum(),
+                        T_sq=np.sum((r.T - p.T_ref) ** 2), e_sums=e_sums, q=r.q, q_band=r.q_band,
+                        margins=r.margins, n_iter=r.n_iter, seconds=el, hashes=json.dumps(h))
 
 
 def fixed_point(a) -> None:

@@ -18,7 +18,7 @@ Sources, all from the reference or from the reference's own code run here:
     (oracle/Makefile `ref`, margin <= 1e-5 as in src/StaticBTESolver.cpp:798)
     -> ref.npz.
 
-Usage:  python tests/golden/make_golden.py [--reference /root/reference]
+Usage:  python tests/golden/make_golden.py [--reference DIR]   (default: $STATICBTESOLVER_REFERENCE)
 """
 from __future__ import annotations
 
@@ -71,7 +71,7 @@ def run_ref(case_dir, geo, bc, band, DM, nt, np_, Lx, Ly, Lz, max_iter):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=O.REFERENCE_ROOT)
     ap.add_argument("--only", default="", help="comma-separated case names")
     args = ap.parse_args()
     only = set(filter(None, args.only.split(",")))

@@ -35,6 +35,21 @@ extern "C" int dsa_c(int dim, int n, int F, const int* nbr, const double* area, 
     std::copy(co.diag.begin(), co.diag.end(), diag);
     return co.n_dirichlet;
 }
+extern "C" void order_c(int n, int F, const int* nbr, int leaf, int* out) {
+    std::vector<int> o;
+    bte::locality_order(n, F, nbr, leaf, o);
+    std::copy(o.begin(), o.end(), out);
+}
+extern "C" int coarse_c(int n, int F, const int* nb, const double* w, int nblk, int per, float* ainv, int* geo,
+                        int* need_ptr, int* need) {
+    bte::DsaCoarse co;
+    if (!bte::dsa_coarse(n, F, nb, w, nblk, per, co)) return -1;
+    std::copy(co.ainv.begin(), co.ainv.end(), ainv);
+    geo[0] = co.chunk; geo[1] = co.seg;
+    std::copy(co.need_ptr.begin(), co.need_ptr.end(), need_ptr);
+    std::copy(co.need.begin(), co.need.end(), need);
+    return co.n_agg;
+}
 '''
 
 
@@ -126,3 +141,64 @@ def test_adiabatic_walls_carry_no_term(lib, oracle_mod, get_case):
             assert (W[sel] > 0).all()
         else:
             assert (W[sel] == 0).all()
+
+
+def _scaled_permuted(lib, o, case, nblk, per):
+    """The low-order operator scaled to unit diagonal in the locality order, as the solve holds it."""
+    g, q, fixed, W, nbo, diag, nd = run(lib, o, bands_of(case.band), bc_rows(case.bc))
+    F, n = W.shape
+    cm = np.ascontiguousarray(np.where((nbo >= 0) & (W > 0), nbo, -1).T, np.int32)  # [n][F]
+    order = np.zeros(n, np.int32)
+    lib.order_c(n, F, cm.ctypes.data_as(C.c_void_p), max(8, n // (nblk * per) // 2), order.ctypes.data_as(C.c_void_p))
+    pos = np.argsort(order)
+    dsc = 1.0 / np.sqrt(diag)
+    nbp = np.full((F, n), -1, np.int32)
+    wp = np.zeros((F, n))
+    for f in range(F):
+        c = order
+        m = nbo[f, c] >= 0
+        nbp[f, m] = pos[nbo[f, c][m]]
+        wp[f, m] = W[f, c][m] * dsc[c][m] * dsc[nbo[f, c][m]]
+    return order, pos, nbp, wp
+
+
+@pytest.mark.parametrize("name", ["square16_b8", "cube4_b2"])
+def test_locality_order_and_coarse_operator(lib, oracle_mod, get_case, name):
+    import scipy.sparse as sp
+
+    case = get_case(name)
+    o = oracle_mod.Oracle(*case.args())
+    nblk, per = 8, 4
+    order, pos, nbp, wp = _scaled_permuted(lib, o, case, nblk, per)
+    F, n = wp.shape
+    assert np.array_equal(np.sort(order), np.arange(n))
+    m = nblk * per
+    ainv = np.zeros(m * m, np.float32)
+    geo = np.zeros(2, np.int32)
+    need_ptr = np.zeros(nblk + 1, np.int32)
+    need = np.zeros(m * nblk, np.int32)
+    f64p = lambda a: np.ascontiguousarray(a).ctypes.data_as(C.c_void_p)
+    got = lib.coarse_c(n, F, f64p(nbp), f64p(wp), nblk, per, ainv.ctypes.data_as(C.c_void_p),
+                       geo.ctypes.data_as(C.c_void_p), need_ptr.ctypes.data_as(C.c_void_p),
+                       need.ctypes.data_as(C.c_void_p))
+    assert got == m
+    chunk, seg = int(geo[0]), int(geo[1])
+    agg = (np.arange(n) // chunk) * per + (np.arange(n) - (np.arange(n) // chunk) * chunk) // seg
+    rows = np.broadcast_to(np.arange(n), (F, n))
+    msk = nbp >= 0
+    A = (sp.csr_matrix((-wp[msk], (rows[msk], nbp[msk])), shape=(n, n)) + sp.eye(n)).toarray()
+    P = np.zeros((n, m))
+    P[np.arange(n), agg] = 1.0
+    Ac = P.T @ A @ P
+    empty = P.sum(0) == 0
+    Ac[empty, empty] = 1.0
+    np.testing.assert_allclose(ainv.reshape(m, m) @ Ac, np.eye(m), atol=2e-4)
+    # every block's list holds the aggregates of its cells and of their neighbours
+    for k in range(nblk):
+        lst = set(need[need_ptr[k]:need_ptr[k + 1]].tolist())
+        cells = np.arange(k * chunk, min(n, (k + 1) * chunk))
+        want = set(agg[cells].tolist()) | set(agg[nbp[:, cells][nbp[:, cells] >= 0]].tolist())
+        assert lst == want
+    # compact aggregates: many couplings stay inside an aggregate
+    inside = (agg[rows[msk]] == agg[nbp[msk]]).mean()
+    assert inside > 0.4, inside  # a random numbering keeps ~1/32 inside

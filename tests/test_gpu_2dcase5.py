@@ -22,10 +22,12 @@ def _solve(sbte, c, **kw):
 
 
 PLAIN_2DCASE5 = pytest.mark.xfail(
-    reason="the reference's right-Jacobi BiCGSTAB is erratic on this mesh: its residual stays at 1e1-1e5 |b| "
-           "for 600-900 iterations before converging, so some systems miss even a 3,000-iteration limit on "
-           "GB300 and the outer iteration stalls near margin 1e10 (the reference's recorded run was lucky; "
-           "the oracle's CPU restatement converges with 17 of 1,280 solves unconverged)", strict=False)
+    reason="the reference's right-Jacobi BiCGSTAB needs 560-1,100 iterations on this mesh's nearly pure "
+           "advection systems (upwind graphs 560-810 levels deep) and the count of each system is decided by "
+           "rounding (one part in 1e15 of the right-hand side moves it by hundreds: "
+           "tests/test_bicgstab_sensitivity.py), so whether every system of a run stops within the reference's "
+           "1,000 iterations is luck; on GB300 some do not and their last iterates stall the outer iteration "
+           "near margin 1e10", strict=False)
 
 
 @pytest.mark.parametrize("form_name,tol", [("FORM_SWEEP", 1e-6), pytest.param("FORM_PLAIN", 1e-6, marks=PLAIN_2DCASE5),

@@ -61,13 +61,15 @@ def test_low_order_solve_matches_direct_solve(sbte, oracle_mod, tmp_path):
     b = vol * (rng.standard_normal(len(vol)) + 0.5)
     x_ref = spla.spsolve(A, b)
     dinv = 1.0 / np.sqrt(A.diagonal())
-    # FP32 vectors: the true residual follows the recurrence's down to ~1e-4
-    # (the correction only needs ~1e-3; the outer iteration is FP64)
+    # the solve stops on the preconditioned residual sqrt(r.M^-1 r), within a
+    # few times the plain one; FP32 vectors: the true residual follows the
+    # recurrence's down to ~1e-4 (the correction only needs ~1e-3; the outer
+    # iteration is FP64)
     for tol in (1e-3, 1e-4):
         x, it, rr = sbte.dsa_solve(nb, W, b, tol=tol, maxit=5000)
         assert 0 < it < 5000 and rr <= tol
         res = np.linalg.norm(dinv * (b - A @ x)) / np.linalg.norm(dinv * b)
-        assert res <= max(3 * tol, 1e-3), (tol, res)
+        assert res <= max(6 * tol, 1e-3), (tol, res)
         if tol == 1e-4:
             assert rel_l2(x, x_ref) < 1e-2
     # deterministic: a second call gives the same bits

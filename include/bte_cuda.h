@@ -123,6 +123,15 @@ typedef struct bte_report {
     int dsa_solves;            /* low-order corrections applied (dsa) */
     long long dsa_iterations;  /* conjugate-gradient iterations summed over them */
     double ms_dsa;             /* device time of the corrections (included in ms_reduce and ms_total) */
+    int sweep_staged;          /* sweep form: 1 the staged kernel was chosen (levels copied to shared memory
+                                  ahead by bulk copies, right-hand side formed beforehand), 0 the
+                                  level-synchronous one; the autotuner times both */
+    double ms_host_setup;      /* host wall time of this call's set-up after new inputs (uploads, geometry) */
+    double ms_host_plan;       /* ... of building the sweep plan (level order, layout) after new geometry */
+    double ms_host_order;      /*     of which the level order (host threads over directions) */
+    double ms_host_dsa;        /* ... of building the low-order operator of dsa after new inputs (its host
+                                  part runs on a host thread next to the sweep plan's, so the two overlap) */
+    double ms_wall;            /* host wall time of the whole call (set-up, solve, read-backs) */
 } bte_report;
 
 /* Fill opts with the reference's defaults (max_iter 10000 as BTEcmd's -I default,
@@ -249,9 +258,13 @@ bte_status bte_get_kernel_stats(bte_ctx* ctx, bte_kernel_stat* stats, int cap, i
 /* The sweep autotuner's table from the first sweep of the current plan (empty
  * when the choice came from the per-process cache): candidate k ran with
  * group[k] bands and threads[k] threads per block and ring[k] positions per
- * band, in ms[k] milliseconds.  Entries are written up to cap (arrays may be
- * NULL when cap is 0); *n = candidates timed. */
-bte_status bte_get_sweep_tuning(bte_ctx* ctx, int* group, int* threads, int* ring, float* ms, int cap, int* n);
+ * band, with the level-synchronous (staged[k] = 0) or the staged kernel
+ * (staged[k] = 1), in ms[k] milliseconds.  Entries are written up to cap
+ * (arrays may be NULL when cap is 0); *n = candidates timed.  The environment
+ * variable BTE_SWEEP_KERNEL=level|staged restricts the candidates to one
+ * kernel (the temperatures are the same to the bit either way). */
+bte_status bte_get_sweep_tuning(bte_ctx* ctx, int* group, int* threads, int* ring, int* staged, float* ms, int cap,
+                                int* n);
 
 /* The reference's inner-solve operator boundary (src/bicgstab.hpp:65,96,138):
  * BICGSTAB(n, maxit, tol); init(rowptr, colind, val, nnz, b); solve(x) --

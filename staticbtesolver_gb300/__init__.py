@@ -64,7 +64,10 @@ class Report(C.Structure):
                 ("kernel_launches", C.c_longlong), ("sweep_group", C.c_int), ("sweep_threads", C.c_int),
                 ("accel_steps", C.c_int), ("accel_reverts", C.c_int), ("sweep_ring", C.c_int),
                 ("sweep_margin", C.c_int), ("dsa_solves", C.c_int), ("dsa_iterations", C.c_longlong),
-                ("ms_dsa", C.c_double)]
+                ("ms_dsa", C.c_double), ("sweep_staged", C.c_int),
+                ("ms_host_setup", C.c_double), ("ms_host_plan", C.c_double), ("ms_host_order", C.c_double),
+                ("ms_host_dsa", C.c_double),
+                ("ms_wall", C.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -121,7 +124,7 @@ def _load():
     L.bte_mlp_param_count.restype = C.c_int
     L.bte_get_kernel_stats.argtypes = [vp, C.c_void_p, C.c_int, C.POINTER(C.c_int)]
     L.bte_get_kernel_stats.restype = C.c_int
-    L.bte_get_sweep_tuning.argtypes = [vp, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
+    L.bte_get_sweep_tuning.argtypes = [vp, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
                                        C.POINTER(C.c_int)]
     L.bte_get_sweep_tuning.restype = C.c_int
     L.bte_bicgstab_csr.argtypes = [C.c_int, _ip, _ip, _dp, C.c_int, _dp, _dp, C.c_int, C.c_double,
@@ -350,16 +353,17 @@ class Context:
 
     def sweep_tuning(self):
         """The sweep autotuner's candidates on this context's plan, as dicts
-        (bands and threads per block, ring positions per band, milliseconds);
-        empty when the shape came from the per-process cache."""
+        (bands and threads per block, ring positions per band, kernel "level"
+        or "staged", milliseconds); empty when the shape came from the
+        per-process cache."""
         n = C.c_int(0)
-        self._check(_cuda.bte_get_sweep_tuning(self._h, None, None, None, None, 0, C.byref(n)))
+        self._check(_cuda.bte_get_sweep_tuning(self._h, None, None, None, None, None, 0, C.byref(n)))
         m = n.value
-        cols = [np.zeros(max(m, 1), np.int32) for _ in range(3)] + [np.zeros(max(m, 1), np.float32)]
+        cols = [np.zeros(max(m, 1), np.int32) for _ in range(4)] + [np.zeros(max(m, 1), np.float32)]
         self._check(_cuda.bte_get_sweep_tuning(self._h, *[c.ctypes.data_as(C.c_void_p) for c in cols], m,
                                                C.byref(n)))
-        return [dict(group=int(cols[0][k]), threads=int(cols[1][k]), ring=int(cols[2][k]), ms=float(cols[3][k]))
-                for k in range(m)]
+        return [dict(group=int(cols[0][k]), threads=int(cols[1][k]), ring=int(cols[2][k]),
+                     kernel="staged" if cols[3][k] else "level", ms=float(cols[4][k])) for k in range(m)]
 
     def margins(self):
         k = C.c_int(0)

@@ -10,11 +10,13 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <tuple>
 #include <string>
@@ -76,11 +78,21 @@ struct SweepShape {
     int G = 2, threads = 128, W = 2048;
     size_t smem = 0;
     bool margin = false;  // acyclic plans: the sweep sums the margin partials (else k_reduce does)
+    bool staged = false;  // k_sweep_staged (right-hand side from k_sweep_src, levels staged by bulk copies)
+    int cap = 0;          // staged: positions per stage
+};
+
+// Stage bounds of the staged sweep for one stage width: per direction, its
+// levels split into slices of at most cap positions.
+struct StageList {
+    DevBuf stages, off;
 };
 
 struct bte_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t setup_stream = nullptr;  // the low-order operator's set-up, next to the sweep plan's
+    std::mutex err_mutex;                 // err is written from the set-up thread too
     std::string err;
     // inputs (host copies)
     int dim = 0, n = 0, F = 0;
@@ -132,6 +144,13 @@ struct bte_ctx {
     long long plan_levels = 0;
     DevBuf p_cell, p_dg, p_vo, p_nb, p_fc, p_lvl, p_lvl_off, p_part, p_bad, p_voi, p_kinv, d_spart, p_bidx, p_binvd;
     DevBuf d_bcell, d_bidx, d_bsum;
+    // staged sweep: plan records, level-ordered right-hand side of a batch,
+    // error flag of its bounded waits, stage lists by width; row length n2
+    DevBuf p_rec, d_ssrc, d_sweep_err;
+    std::vector<int> plan_lvl, plan_lvl_off;  // host copies of the level starts
+    std::map<int, std::unique_ptr<StageList>> stage_lists;
+    int n2 = 0;
+    double ms_last_order = 0.0;  // host wall time of the last plan's level order
     DevBuf d_snap_e, d_snap_T, d_snap_ebar;  // accelerator: state before the last jump
     DevBuf d_aa_x, d_aa_g, d_aa_f, d_aa_part, d_aa_gram, d_aa_alpha, d_aa_flag;  // Anderson mixing
     double aa_prev_margin = 0.0;  // cells with boundary faces, cell -> row, boundary rhs per (system, row)
@@ -158,6 +177,7 @@ struct bte_ctx {
     bool dsa_ready = false;
     int dsa_walls = 0;   // wall faces held at a fixed temperature
     int dsa_blocks = 0;  // cooperative grid of k_dsa_cg
+    DevBuf d_lo_agg, d_lo_nagg;  // aggregate of each cell / of each face's neighbour (solve numbering)
     DevBuf d_lo_nb, d_lo_w, d_lo_dsc, d_Tsrc, d_dsa_b, d_dsa_x, d_dsa_xc, d_dsa_order, d_dsa_pos;
     DevBuf d_co_ainv, d_co_need_ptr, d_co_need, d_co_sums, d_co_sums0;
     DevBuf cg_r, cg_aw, cg_s, cg_x, cg_p, cg_u, cg_part, cg_bar, cg_stat, cg_relres;
@@ -193,7 +213,10 @@ struct bte_ctx {
     } while (0)
 
 static bte_status fail(bte_ctx* ctx, bte_status st, const std::string& msg) {
-    if (ctx) ctx->err = msg;
+    if (ctx) {
+        std::lock_guard<std::mutex> lock(ctx->err_mutex);
+        ctx->err = msg;
+    }
     return st;
 }
 
@@ -310,6 +333,7 @@ bte_status bte_destroy(bte_ctx* ctx) {
     if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);
     if (ctx->h_pinned_i) cudaFreeHost(ctx->h_pinned_i);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    if (ctx->setup_stream) cudaStreamDestroy(ctx->setup_stream);
     delete ctx;
     return BTE_OK;
 }
@@ -421,6 +445,25 @@ static int mirror_of(int type, int dim, int d, int num_phi) {
 }
 
 // Upload inputs, build boundary tables, per-direction geometry and state buffers.
+// BTE_HOST_TIMING=1: each host set-up step's wall time goes to stderr
+// (a diagnostic of the end-to-end cost of new inputs).
+struct HostTimer {
+    const char* what;
+    std::chrono::steady_clock::time_point t = std::chrono::steady_clock::now();
+    static bool on() {
+        static const bool v = [] { const char* e = std::getenv("BTE_HOST_TIMING"); return e && *e && *e != '0'; }();
+        return v;
+    }
+    explicit HostTimer(const char* w) : what(w) {}
+    void lap(const char* step) {
+        if (!on()) return;
+        const auto now = std::chrono::steady_clock::now();
+        std::fprintf(stderr, "[bte host] %s: %s %.3f ms\n", what, step,
+                     std::chrono::duration<double, std::milli>(now - t).count());
+        t = now;
+    }
+};
+
 static bte_status setup(bte_ctx* ctx, int batch_systems) {
     const int n = ctx->n, F = ctx->F, ND = ctx->n_dir, NB = ctx->n_band, dim = ctx->dim;
     ctx->Np = (size_t)((n + bte::CH - 1) / bte::CH) * bte::CH;
@@ -666,15 +709,22 @@ constexpr int kDsaThreads = bte::dsa::THREADS;
 // symmetrically scaled form, in a locality order of the cells with the
 // two-level preconditioner's coarse operator, and size the conjugate-gradient
 // work for n cells.
-static bte_status dsa_prepare(bte_ctx* ctx, int n, int F, const int* nb, const double* W) {
-    cudaStream_t st = ctx->stream;
-    int coop = 0, sms = 0, occ = 0;
-    BTE_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, ctx->device));
-    if (!coop) return fail(ctx, BTE_ERR_CUDA, "dsa: the device does not support cooperative launches");
-    BTE_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
-    // at most one block per SM: enough threads for the cells, few blocks at each barrier
-    const int nblk = std::max(1, std::min(sms, (n + kDsaThreads - 1) / kDsaThreads));
-    ctx->dsa_blocks = nblk;
+// Host part of the low-order solve's set-up: Jacobi scaling, locality
+// order, the permuted operator and the coarse operator.  No CUDA calls, so it
+// can run on a host thread while the sweep plan is built.
+struct DsaHostPlan {
+    int n = 0, F = 0, nblk = 0;
+    std::vector<int> order, pos, nbv, agg, nagg;
+    std::vector<double> dscp;
+    std::vector<float> w;
+    bte::DsaCoarse co;
+};
+
+static void dsa_host_plan(int n, int F, const int* nb, const double* W, int nblk, DsaHostPlan& hp) {
+    HostTimer tm("dsa_host_plan");
+    hp.n = n;
+    hp.F = F;
+    hp.nblk = nblk;
     std::vector<double> diag(n, 0.0), dsc(n, 0.0);
     for (int f = 0; f < F; ++f)
         for (int c = 0; c < n; ++c) diag[c] += W[(size_t)f * n + c];
@@ -684,31 +734,93 @@ static bte_status dsa_prepare(bte_ctx* ctx, int n, int F, const int* nb, const d
     for (int f = 0; f < F; ++f)
         for (int c = 0; c < n; ++c) cm[(size_t)c * F + f] = W[(size_t)f * n + c] > 0.0 ? nb[(size_t)f * n + c] : -1;
     const int agg_cells = std::max(1, n / (nblk * bte::dsa::AGG));
-    bte::locality_order(n, F, cm.data(), std::max(8, agg_cells / 2), ctx->dsa_order);
-    const std::vector<int>& order = ctx->dsa_order;
-    std::vector<int> pos(n);
+    tm.lap("scaling");
+    bte::locality_order(n, F, cm.data(), std::max(8, agg_cells / 2), hp.order);
+    tm.lap("locality order");
+    const std::vector<int>& order = hp.order;
+    std::vector<int>& pos = hp.pos;
+    pos.assign(n, 0);
     for (int k = 0; k < n; ++k) pos[order[k]] = k;
-    std::vector<double> wd((size_t)F * n, 0.0), dscp(n);
-    std::vector<float> w((size_t)F * n, 0.0f);
-    std::vector<int> nbv((size_t)F * n, -1);
+    std::vector<double> wd((size_t)F * n, 0.0);
+    hp.dscp.assign(n, 0.0);
+    hp.w.assign((size_t)F * n, 0.0f);
+    hp.nbv.assign((size_t)F * n, -1);
     for (int k = 0; k < n; ++k) {
         const int c = order[k];
-        dscp[k] = dsc[c];
+        hp.dscp[k] = dsc[c];
         for (int f = 0; f < F; ++f) {
             const size_t q = (size_t)f * n + c;
             const int o = nb[q];
             if (o >= 0 && W[q] > 0.0) {
                 const size_t qk = (size_t)f * n + k;
                 wd[qk] = W[q] * dsc[c] * dsc[o];
-                w[qk] = (float)wd[qk];
-                nbv[qk] = pos[o];
+                hp.w[qk] = (float)wd[qk];
+                hp.nbv[qk] = pos[o];
             }
         }
     }
-    bte::DsaCoarse co;
-    if (!bte::dsa_coarse(n, F, nbv.data(), wd.data(), nblk, bte::dsa::AGG, co))
-        return fail(ctx, BTE_ERR_INVALID_ARGUMENT,
-                    "dsa: the low-order operator is singular (no wall held at a fixed temperature)");
+    tm.lap("permuted operator");
+    bte::dsa_coarse(n, F, hp.nbv.data(), wd.data(), nblk, bte::dsa::AGG, hp.co);
+    hp.agg.assign(n, 0);
+    hp.nagg.assign((size_t)F * n, -1);
+    for (int k = 0; k < n; ++k) hp.agg[k] = hp.co.agg_of(k);
+    for (size_t q = 0; q < (size_t)F * n; ++q)
+        if (hp.nbv[q] >= 0) hp.nagg[q] = hp.co.agg_of(hp.nbv[q]);
+    tm.lap("coarse operator");
+}
+
+// Blocks of the cooperative low-order kernel for n cells: at most one per SM.
+static bte_status dsa_blocks(bte_ctx* ctx, int n, int* nblk) {
+    int coop = 0, sms = 0;
+    BTE_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, ctx->device));
+    if (!coop) return fail(ctx, BTE_ERR_CUDA, "dsa: the device does not support cooperative launches");
+    BTE_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
+    // enough threads for the cells, few blocks at each barrier
+    *nblk = std::max(1, std::min(sms, (n + kDsaThreads - 1) / kDsaThreads));
+    return BTE_OK;
+}
+
+// Device part: the coarse inverse, the uploads and the work vectors.
+static bte_status dsa_upload(bte_ctx* ctx, DsaHostPlan& hp, cudaStream_t st) {
+    HostTimer tm("dsa_upload");
+    const int n = hp.n, F = hp.F, nblk = hp.nblk;
+    int sms = 0, occ = 0;
+    BTE_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
+    ctx->dsa_blocks = nblk;
+    ctx->dsa_order = hp.order;
+    const bte::DsaCoarse& co = hp.co;
+    const std::vector<int>& order = hp.order;
+    const std::vector<int>& pos = hp.pos;
+    const std::vector<int>& nbv = hp.nbv;
+    const std::vector<float>& w = hp.w;
+    const std::vector<double>& dscp = hp.dscp;
+    // the coarse operator's inverse by Gauss-Jordan steps on the device (FP64),
+    // stored in FP32 for the preconditioner
+    {
+        const int m = co.n_agg;
+        DevBuf ga, gb, gbad;
+        BTE_CUDA(upload(ga, co.ac, st));
+        BTE_CUDA(gb.alloc(sizeof(double) * (size_t)m * m));
+        BTE_CUDA(gbad.alloc(sizeof(int)));
+        BTE_CUDA(cudaMemsetAsync(gbad.p, 0, sizeof(int), st));
+        double* a = ga.as<double>();
+        double* b = gb.as<double>();
+        for (int k = 0; k < m; ++k) {
+            bte::dsa::k_gj_step<<<dim3((m + 255) / 256, m), 256, 0, st>>>(a, b, m, k, gbad.as<int>());
+            std::swap(a, b);
+        }
+        BTE_CUDA(ctx->d_co_ainv.alloc(sizeof(float) * (size_t)m * m));
+        bte::dsa::k_to_float<<<(unsigned)(((size_t)m * m + 255) / 256), 256, 0, st>>>(
+            a, ctx->d_co_ainv.as<float>(), (size_t)m * m);
+        BTE_LAUNCHED();
+        int bad = 0;
+        BTE_CUDA(cudaMemcpyAsync(&bad, gbad.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+        BTE_CUDA(cudaStreamSynchronize(st));
+        if (bad)
+            return fail(ctx, BTE_ERR_INVALID_ARGUMENT,
+                        "dsa: the low-order operator is singular (no wall held at a fixed temperature)");
+        tm.lap("coarse inverse (device)");
+    }
     ctx->dsa_chunk = co.chunk;
     ctx->dsa_seg = co.seg;
     ctx->dsa_n_agg = co.n_agg;
@@ -728,8 +840,9 @@ static bte_status dsa_prepare(bte_ctx* ctx, int n, int F, const int* nb, const d
     BTE_CUDA(upload(ctx->d_lo_dsc, dscp, st));
     BTE_CUDA(upload(ctx->d_dsa_order, order, st));
     BTE_CUDA(upload(ctx->d_dsa_pos, pos, st));
-    BTE_CUDA(upload(ctx->d_co_ainv, co.ainv, st));
     BTE_CUDA(upload(ctx->d_co_need_ptr, co.need_ptr, st));
+    BTE_CUDA(upload(ctx->d_lo_agg, hp.agg, st));
+    BTE_CUDA(upload(ctx->d_lo_nagg, hp.nagg, st));
     BTE_CUDA(upload(ctx->d_co_need, co.need, st));
     BTE_CUDA(ctx->d_co_sums.alloc(sizeof(float) * 6 * (size_t)co.n_agg));
     BTE_CUDA(ctx->d_co_sums0.alloc(sizeof(double) * (size_t)co.n_agg));
@@ -742,7 +855,7 @@ static bte_status dsa_prepare(bte_ctx* ctx, int n, int F, const int* nb, const d
     BTE_CUDA(ctx->cg_x.alloc(sizeof(float) * nn));
     BTE_CUDA(ctx->cg_p.alloc(sizeof(float) * nn));
     BTE_CUDA(ctx->cg_u.alloc(sizeof(float) * nn));
-    BTE_CUDA(ctx->cg_part.alloc(sizeof(double) * (2 * (size_t)nblk + 2)));
+    BTE_CUDA(ctx->cg_part.alloc(sizeof(double) * 4 * (size_t)nblk));
     BTE_CUDA(ctx->cg_bar.alloc(sizeof(unsigned) * 2));
     BTE_CUDA(ctx->cg_stat.alloc(sizeof(int) * 4));
     BTE_CUDA(ctx->cg_relres.alloc(sizeof(double)));
@@ -750,7 +863,21 @@ static bte_status dsa_prepare(bte_ctx* ctx, int n, int F, const int* nb, const d
     BTE_CUDA(ctx->d_dsa_x.alloc(sizeof(double) * nn));
     BTE_CUDA(ctx->d_dsa_xc.alloc(sizeof(double) * nn));
     BTE_CUDA(cudaMemsetAsync(ctx->cg_stat.p, 0, sizeof(int) * 4, st));
+    tm.lap("uploads");
     return BTE_OK;
+}
+
+// Upload a low-order operator (nb, W as bte_dsa_solve takes them) in its
+// symmetrically scaled form, in a locality order of the cells with the
+// two-level preconditioner's coarse operator, and size the conjugate-gradient
+// work for n cells.
+static bte_status dsa_prepare(bte_ctx* ctx, int n, int F, const int* nb, const double* W) {
+    int nblk = 0;
+    bte_status s = dsa_blocks(ctx, n, &nblk);
+    if (s != BTE_OK) return s;
+    DsaHostPlan hp;
+    dsa_host_plan(n, F, nb, W, nblk, hp);
+    return dsa_upload(ctx, hp, ctx->stream);
 }
 
 // One low-order solve of d_dsa_b into d_dsa_x, both in the solve's numbering
@@ -758,7 +885,8 @@ static bte_status dsa_prepare(bte_ctx* ctx, int n, int F, const int* nb, const d
 static bte_status dsa_launch(bte_ctx* ctx, int n, int F, double tol, int maxit) {
     cudaStream_t st = ctx->stream;
     BTE_CUDA(cudaMemsetAsync(ctx->cg_bar.p, 0, sizeof(unsigned) * 2, st));
-    bte::dsa::Lo lo{n, F, ctx->d_lo_nb.as<int>(), ctx->d_lo_w.as<float>(), ctx->d_lo_dsc.as<double>()};
+    bte::dsa::Lo lo{n, F, ctx->d_lo_nb.as<int>(), ctx->d_lo_w.as<float>(), ctx->d_lo_dsc.as<double>(),
+                    ctx->d_lo_agg.as<int>(), ctx->d_lo_nagg.as<int>()};
     bte::dsa::Coarse co{ctx->dsa_chunk, ctx->dsa_seg, ctx->dsa_n_agg, ctx->dsa_stage ? 1 : 0,
                         ctx->d_co_ainv.as<float>(),
                         ctx->d_co_need_ptr.as<int>(), ctx->d_co_need.as<int>(), ctx->d_co_sums.as<float>(),
@@ -775,8 +903,15 @@ static bte_status dsa_launch(bte_ctx* ctx, int n, int F, double tol, int maxit) 
     return BTE_OK;
 }
 
-// The low-order operator of the mesh, bands and walls of ctx.
-static bte_status setup_dsa(bte_ctx* ctx) {
+// The low-order operator of the mesh, bands and walls of ctx: the host part
+// (coefficients, then dsa_host_plan; it reads only ctx's host-side inputs, so
+// it can run on a host thread next to the sweep plan's construction) ...
+struct DsaSetupHost {
+    int n_dirichlet = 0;
+    DsaHostPlan hp;
+};
+
+static void setup_dsa_host(const bte_ctx* ctx, int nblk, DsaSetupHost& out) {
     const int n = ctx->n, F = ctx->F;
     // walls held at a fixed temperature: isothermal rows, and boundary faces
     // that no row names (their wall energy stays 0 in the reference)
@@ -789,17 +924,25 @@ static bte_status setup_dsa(bte_ctx* ctx) {
             if (ctx->bc_index[i] == code) { row = i; break; }
         fixed[cf] = row < 0 || ctx->bc_type[row] == 1;
     }
+    HostTimer tm("setup_dsa_host");
     bte::DsaCoefficients co;
     bte::dsa_coefficients(ctx->dim, n, F, ctx->nbr.data(), ctx->area.data(), ctx->normal.data(), ctx->volume.data(),
                           ctx->n_dir, ctx->s.data(), ctx->S.data(), ctx->solid_angle, ctx->n_band, ctx->vg.data(),
                           ctx->tau.data(), ctx->Lr.data(), fixed, kDsaBeta, co);
-    ctx->dsa_walls = co.n_dirichlet;
-    if (co.n_dirichlet > 0) {
-        bte_status s = dsa_prepare(ctx, n, F, co.nb.data(), co.W.data());
+    tm.lap("coefficients");
+    out.n_dirichlet = co.n_dirichlet;
+    if (co.n_dirichlet > 0) dsa_host_plan(n, F, co.nb.data(), co.W.data(), nblk, out.hp);
+}
+
+// ... and the device part.
+static bte_status setup_dsa_device(bte_ctx* ctx, DsaSetupHost& h, cudaStream_t st) {
+    ctx->dsa_walls = h.n_dirichlet;
+    if (h.n_dirichlet > 0) {
+        bte_status s = dsa_upload(ctx, h.hp, st);
         if (s != BTE_OK) return s;
         BTE_CUDA(ctx->d_Tsrc.alloc(sizeof(double) * ctx->Np));
+        BTE_CUDA(cudaStreamSynchronize(st));
     }
-    ctx->dsa_ready = true;
     return BTE_OK;
 }
 
@@ -808,6 +951,7 @@ static int sweep_slots(const bte_ctx* ctx) { return std::max(2, std::min(ctx->pl
 
 // Build the sweep plan for every direction from the device's inflow coefficients.
 static bte_status build_sweep_plan(bte_ctx* ctx) {
+    HostTimer tm("build_sweep_plan");
     const int n = ctx->n, F = ctx->F, ND = ctx->n_dir;
     const size_t Np = ctx->Np;
     cudaStream_t st = ctx->stream;
@@ -820,37 +964,51 @@ static bte_status build_sweep_plan(bte_ctx* ctx) {
     BTE_CUDA(cudaMemcpyAsync(mask.data(), d_mask.p, mask.size(), cudaMemcpyDeviceToHost, st));
     BTE_CUDA(cudaStreamSynchronize(st));
     std::vector<std::vector<int>> perm(ND), lvl(ND), lag(ND);
+    tm.lap("inflow mask (device + copy)");
+    const auto t_order = std::chrono::steady_clock::now();
     const int nth = std::max(1, std::min<int>(ND, (int)std::thread::hardware_concurrency()));
     std::vector<std::thread> pool;
+    std::vector<int> h_perm((size_t)ND * n);
+    std::vector<char> lag_any(ND, 0);
     for (int t = 0; t < nth; ++t)
         pool.emplace_back([&, t]() {
-            for (int d = t; d < ND; d += nth)
+            for (int d = t; d < ND; d += nth) {
                 bte::level_order(n, F, &mask[(size_t)d * n], ctx->nbr.data(), perm[d], lvl[d], lag[d]);
+                std::copy(perm[d].begin(), perm[d].end(), h_perm.begin() + (size_t)d * n);
+                lag_any[d] = std::any_of(lag[d].begin(), lag[d].end(), [](int v) { return v != 0; });
+            }
         });
     for (auto& th : pool) th.join();
+    ctx->ms_last_order = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_order).count();
+    tm.lap("level order");
     // the sweep's face slots: the largest inflow count of a cell
     int fm = 0;
     for (uint8_t m : mask) fm = std::max(fm, bte::inflow_count(m));
     ctx->plan_fm = fm;
-    std::vector<int> h_perm((size_t)ND * n), h_pos((size_t)ND * n), h_lag((size_t)ND * F * n), h_lvl, h_off(ND + 1, 0);
+    std::vector<int> h_lvl, h_off(ND + 1, 0);
     int lagged_dirs = 0;
     long long levels = 0;
     for (int d = 0; d < ND; ++d) {
-        std::copy(perm[d].begin(), perm[d].end(), h_perm.begin() + (size_t)d * n);
-        for (int j = 0; j < n; ++j) h_pos[(size_t)d * n + perm[d][j]] = j;
-        std::copy(lag[d].begin(), lag[d].end(), h_lag.begin() + (size_t)d * F * n);
         h_off[d] = (int)h_lvl.size();
         h_lvl.insert(h_lvl.end(), lvl[d].begin(), lvl[d].end());
         levels += (long long)lvl[d].size() - 1;
-        bool any = false;
-        for (int v : lag[d]) any |= v != 0;
-        lagged_dirs += any;
+        lagged_dirs += lag_any[d];
     }
     h_off[ND] = (int)h_lvl.size();
+    tm.lap("order arrays");
     DevBuf d_perm, d_pos, d_lag;
     BTE_CUDA(upload(d_perm, h_perm, st));
-    BTE_CUDA(upload(d_pos, h_pos, st));
-    BTE_CUDA(upload(d_lag, h_lag, st));
+    tm.lap("order upload");
+    // cell -> position from the order on the device; the lagged-edge flags
+    // only when some direction has a cycle (none on planar meshes)
+    BTE_CUDA(d_pos.alloc(sizeof(int) * (size_t)ND * n));
+    bte::k_inverse_perm<<<dim3((n + 255) / 256, ND), 256, 0, st>>>(d_perm.as<int>(), n, d_pos.as<int>());
+    BTE_LAUNCHED();
+    if (lagged_dirs > 0) {
+        std::vector<int> h_lag((size_t)ND * F * n);
+        for (int d = 0; d < ND; ++d) std::copy(lag[d].begin(), lag[d].end(), h_lag.begin() + (size_t)d * F * n);
+        BTE_CUDA(upload(d_lag, h_lag, st));
+    }
     BTE_CUDA(upload(ctx->p_lvl, h_lvl, st));
     BTE_CUDA(upload(ctx->p_lvl_off, h_off, st));
     BTE_CUDA(ctx->p_cell.alloc(sizeof(int) * ND * n));
@@ -868,21 +1026,59 @@ static bte_status build_sweep_plan(bte_ctx* ctx) {
         BTE_LAUNCHED();
     }
     bte::k_sweep_layout<<<dim3((n + 255) / 256, ND), 256, 0, st>>>(
-        d_perm.as<int>(), d_pos.as<int>(), d_lag.as<int>(), ctx->d_dg.as<double>(), ctx->d_vo.as<double>(), ctx->d_fc.as<double>(),
+        d_perm.as<int>(), d_pos.as<int>(), lagged_dirs > 0 ? d_lag.as<int>() : nullptr, ctx->d_dg.as<double>(), ctx->d_vo.as<double>(), ctx->d_fc.as<double>(),
         ctx->d_nbr.as<int>(), ctx->d_bidx.as<int>(), F, n, Np, ND, ctx->p_cell.as<int>(), ctx->p_bidx.as<int>(),
         ctx->p_dg.as<double>(), ctx->p_vo.as<double>(), ctx->p_nb.as<int>(), ctx->p_fc.as<double>());
     BTE_LAUNCHED();
-    BTE_CUDA(ctx->p_voi.alloc(sizeof(double) * ctx->n_band * ND * n));
-    BTE_CUDA(ctx->p_kinv.alloc(sizeof(double) * ctx->n_band * ND * n));
+    ctx->n2 = (n + 1) & ~1;
+    tm.lap("layout");
+    BTE_CUDA(ctx->p_voi.alloc(sizeof(double) * ctx->n_band * ND * (size_t)ctx->n2));
+    BTE_CUDA(ctx->p_kinv.alloc(sizeof(double) * ctx->n_band * ND * (size_t)ctx->n2));
     {
         bte::SweepPlan sp{ctx->p_cell.as<int>(), ctx->p_bidx.as<int>(), ctx->p_dg.as<double>(), ctx->p_vo.as<double>(), ctx->p_nb.as<int>(),
-                          ctx->p_fc.as<double>(), ctx->p_lvl.as<int>(), ctx->p_lvl_off.as<int>(), n, F};
+                          ctx->p_fc.as<double>(), ctx->p_lvl.as<int>(), ctx->p_lvl_off.as<int>(), n, F, ctx->n2};
         bte::k_sweep_invd<<<dim3((n + 255) / 256, ND), 256, 0, st>>>(sp, ctx->d_kb.as<double>(), ctx->n_band, ND,
                                                                      ctx->p_voi.as<double>(),
                                                                      ctx->p_kinv.as<double>());
         BTE_LAUNCHED();
     }
+    tm.lap("per-system diagonal");
+    // staged sweep: one record per (direction, position), the batch's
+    // level-ordered right-hand side, the error flag of its bounded waits
+    {
+        const int fmx = sweep_slots(ctx);
+        const int rb = fmx == 2 ? bte::SweepRecLayout<2>::bytes
+                                : fmx == 3 ? bte::SweepRecLayout<3>::bytes : bte::SweepRecLayout<4>::bytes;
+        BTE_CUDA(ctx->p_rec.alloc((size_t)rb * ND * n));
+        const dim3 g((n + 255) / 256, ND);
+        if (fmx == 2)
+            bte::k_sweep_records<2><<<g, 256, 0, st>>>(ctx->p_cell.as<int>(), ctx->p_nb.as<int>(),
+                                                       ctx->p_fc.as<double>(), n, F, ND,
+                                                       ctx->p_rec.as<unsigned char>());
+        else if (fmx == 3)
+            bte::k_sweep_records<3><<<g, 256, 0, st>>>(ctx->p_cell.as<int>(), ctx->p_nb.as<int>(),
+                                                       ctx->p_fc.as<double>(), n, F, ND,
+                                                       ctx->p_rec.as<unsigned char>());
+        else
+            bte::k_sweep_records<4><<<g, 256, 0, st>>>(ctx->p_cell.as<int>(), ctx->p_nb.as<int>(),
+                                                       ctx->p_fc.as<double>(), n, F, ND,
+                                                       ctx->p_rec.as<unsigned char>());
+        BTE_LAUNCHED();
+        BTE_CUDA(ctx->d_ssrc.alloc(sizeof(double) * (size_t)ctx->nbb * ND * ctx->n2));
+        BTE_CUDA(ctx->d_sweep_err.alloc(sizeof(int)));
+        BTE_CUDA(cudaMemsetAsync(ctx->d_sweep_err.p, 0, sizeof(int), st));
+        int smem_max = 0;
+        BTE_CUDA(cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device));
+        BTE_CUDA(cudaFuncSetAttribute(bte::k_sweep_staged<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max));
+        BTE_CUDA(cudaFuncSetAttribute(bte::k_sweep_staged<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max));
+        BTE_CUDA(cudaFuncSetAttribute(bte::k_sweep_staged<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max));
+        ctx->plan_lvl = h_lvl;
+        ctx->plan_lvl_off = h_off;
+        ctx->stage_lists.clear();
+    }
+    tm.lap("records");
     BTE_CUDA(cudaStreamSynchronize(st));  // d_perm / d_lag go out of scope
+    tm.lap("sync");
     ctx->sweep_tuned = false;
     ctx->sweep_tune_cand.clear();
     ctx->sweep_tune_ms.clear();
@@ -1099,7 +1295,7 @@ static bte_status solve_batch_mixed(bte_ctx* ctx, int b0, int nbb, const bte_opt
 
 // Launch shapes chosen by the sweep's autotuner, per (device, cells, faces,
 // directions, bands per batch, levels, margin restriction).
-using SweepTuneKey = std::tuple<int, int, int, int, int, long long, int>;
+using SweepTuneKey = std::tuple<int, int, int, int, int, long long, int, int, int>;
 
 // BTE_SWEEP_MARGIN=1 (in the sweep) or 0 (in k_reduce) fixes where the margin
 // of an acyclic plan is summed instead of timing both (the temperatures are
@@ -1108,6 +1304,22 @@ static int sweep_margin_restriction() {
     const char* v = std::getenv("BTE_SWEEP_MARGIN");
     if (!v || !*v) return -1;
     return v[0] == '0' ? 0 : v[0] == '1' ? 1 : -1;
+}
+// BTE_SWEEP_KERNEL=level (k_sweep) or staged (k_sweep_staged) restricts the
+// autotuner to one sweep kernel (x is the same to the bit either way).
+static int sweep_kernel_restriction() {
+    const char* v = std::getenv("BTE_SWEEP_KERNEL");
+    if (!v || !*v) return -1;
+    return v[0] == 'l' ? 0 : v[0] == 's' ? 1 : -1;
+}
+// BTE_SWEEP_SHAPE=G,T restricts the autotuner to G bands and T threads per
+// block (a test of a particular shape, e.g. stages narrower than a level);
+// returns G * 10000 + T, or -1.
+static int sweep_shape_restriction() {
+    const char* v = std::getenv("BTE_SWEEP_SHAPE");
+    int g = 0, t = 0;
+    if (!v || std::sscanf(v, "%d,%d", &g, &t) != 2 || g <= 0 || t <= 0) return -1;
+    return g * 10000 + t;
 }
 static std::mutex g_sweep_tune_mutex;
 static std::map<SweepTuneKey, SweepShape> g_sweep_tune;
@@ -1121,20 +1333,77 @@ static int sweep_ring(int G) {
 
 // Candidates of the autotuner for batches of nbb bands: (bands per block,
 // threads); k_sweep takes at most 128 threads.
-static std::vector<SweepShape> sweep_candidates(int nbb) {
+// Shared memory of a staged candidate (face slots fm).
+static size_t staged_smem(int fm, int cap, int G, int W) {
+    return fm == 2 ? bte::staged_smem_bytes<2>(cap, G, W)
+                   : fm == 3 ? bte::staged_smem_bytes<3>(cap, G, W) : bte::staged_smem_bytes<4>(cap, G, W);
+}
+
+// Candidates of the autotuner for batches of nbb bands: k_sweep (bands per
+// block, threads; at most 128 threads) and k_sweep_staged (at most 256
+// threads; two rounds of the block's positions per stage, a ring of 2048 / G
+// positions per band).
+static std::vector<SweepShape> sweep_candidates(const bte_ctx* ctx, int nbb, int only_kernel, int only_margin,
+                                                int only_shape) {
     static const int cand[][2] = {{1, 64}, {1, 128}, {2, 64}, {2, 128}, {4, 64}, {4, 128}, {8, 128}, {16, 128}};
+    static const int staged[][2] = {{1, 128}, {1, 256}, {2, 128}, {2, 256}, {4, 64},
+                                    {4, 128}, {4, 256}, {8, 256}};
     std::vector<SweepShape> out;
     for (const auto& c : cand) {
+        if (only_kernel == 1) break;
+        if (only_shape >= 0 && only_shape != c[0] * 10000 + c[1]) continue;
         SweepShape sh;
         sh.G = std::max(1, std::min(c[0], nbb));
         sh.threads = c[1];
         sh.W = sweep_ring(sh.G);
         sh.smem = sizeof(double) * (size_t)sh.G * sh.W;
         bool dup = false;
-        for (const SweepShape& o : out) dup |= o.G == sh.G && o.threads == sh.threads;
+        for (const SweepShape& o : out) dup |= !o.staged && o.G == sh.G && o.threads == sh.threads;
+        if (!dup) out.push_back(sh);
+    }
+    int smem_max = 0;
+    cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device);
+    for (const auto& c : staged) {
+        // the staged kernel leaves the margin to k_reduce
+        if (only_kernel == 0 || only_margin == 1) break;
+        if (only_shape >= 0 && only_shape != c[0] * 10000 + c[1]) continue;
+        SweepShape sh;
+        sh.staged = true;
+        sh.G = std::max(1, std::min(c[0], nbb));
+        sh.threads = c[1];
+        int gp = 1;
+        while (gp < sh.G) gp <<= 1;
+        sh.cap = 2 * (sh.threads / gp);
+        sh.W = std::max(256, 2048 / gp);
+        sh.smem = staged_smem(sweep_slots(ctx), sh.cap, sh.G, sh.W);
+        if (sh.smem > (size_t)smem_max) continue;
+        bool dup = false;
+        for (const SweepShape& o : out) dup |= o.staged && o.G == sh.G && o.threads == sh.threads;
         if (!dup) out.push_back(sh);
     }
     return out;
+}
+
+// Stage bounds for stages of at most cap positions (built once per width).
+static bte_status stage_list(bte_ctx* ctx, int cap, const StageList** out) {
+    auto it = ctx->stage_lists.find(cap);
+    if (it == ctx->stage_lists.end()) {
+        std::vector<int> stages, off(ctx->n_dir + 1, 0);
+        for (int d = 0; d < ctx->n_dir; ++d) {
+            off[d] = (int)stages.size();
+            const int l0 = ctx->plan_lvl_off[d], l1 = ctx->plan_lvl_off[d + 1];  // level starts, then n
+            for (int l = l0; l + 1 < l1; ++l)
+                for (int j = ctx->plan_lvl[l]; j < ctx->plan_lvl[l + 1]; j += cap) stages.push_back(j);
+            stages.push_back(ctx->n);
+        }
+        off[ctx->n_dir] = (int)stages.size();
+        auto sl = std::make_unique<StageList>();
+        BTE_CUDA(upload(sl->stages, stages, ctx->stream));
+        BTE_CUDA(upload(sl->off, off, ctx->stream));
+        it = ctx->stage_lists.emplace(cap, std::move(sl)).first;
+    }
+    *out = it->second.get();
+    return BTE_OK;
 }
 
 // One sweep of bands b0 .. b0+nbb-1 in every direction with shape sh, for the
@@ -1146,6 +1415,20 @@ static void launch_sweep(const bte_ctx* ctx, const SweepShape& sh, int nbb, int 
     const double* voi = ctx->p_voi.as<double>();
     const double* kinv = ctx->p_kinv.as<double>();
     const int fm = sweep_slots(ctx);
+    if (sh.staged) {  // MARGIN is false here: the staged kernel leaves the margin to k_reduce
+        const StageList* sl = ctx->stage_lists.find(sh.cap)->second.get();
+        const bte::StagedPlan pl{ctx->p_rec.as<unsigned char>(), sl->stages.as<int>(), sl->off.as<int>(),
+                                 ctx->p_cell.as<int>(), ctx->n, ctx->n2, sh.cap};
+#define BTE_STAGED_FM(FM)                                                                                          \
+    bte::k_sweep_staged<FM><<<grid, sh.threads, sh.smem, st>>>(pl, kinv, ctx->d_ssrc.as<double>(), src.x_old,      \
+                                                               ctx->e_curr, first_sweep, sh.G, sh.W, nbb, b0,      \
+                                                               ctx->n_dir, ctx->Np, ctx->d_sweep_err.as<int>())
+        if (fm == 2) BTE_STAGED_FM(2);
+        else if (fm == 3) BTE_STAGED_FM(3);
+        else BTE_STAGED_FM(4);
+#undef BTE_STAGED_FM
+        return;
+    }
 #define BTE_SWEEP_FM(FM)                                                                                         \
     bte::k_sweep<MARGIN, FM><<<grid, sh.threads, sh.smem, st>>>(sp, voi, kinv, src, ctx->e_curr, first_sweep, sh.G, \
                                                                 sh.W, nbb, b0, ctx->n_band, ctx->n_dir, ctx->Np, mpart)
@@ -1153,6 +1436,13 @@ static void launch_sweep(const bte_ctx* ctx, const SweepShape& sh, int nbb, int 
     else if (fm == 3) BTE_SWEEP_FM(3);
     else BTE_SWEEP_FM(4);
 #undef BTE_SWEEP_FM
+}
+
+// The staged sweep's right-hand side of the batch in level order (k_sweep_src).
+static void launch_sweep_src(const bte_ctx* ctx, int nbb, int b0, cudaStream_t st, const bte::SweepSrc& src) {
+    const dim3 g((ctx->n + 255) / 256, nbb * ctx->n_dir);
+    bte::k_sweep_src<<<g, 256, 0, st>>>(ctx->p_cell.as<int>(), ctx->p_bidx.as<int>(), ctx->p_voi.as<double>(), src,
+                                        ctx->n, ctx->n2, ctx->n_dir, nbb, b0, ctx->Np, ctx->d_ssrc.as<double>());
 }
 
 // Solve all systems of one batch by upwind sweeps (exact in one sweep when no
@@ -1179,13 +1469,17 @@ static bte_status solve_batch_sweep(bte_ctx* ctx, int b0, int nbb, const bte_opt
     }
     const bte::SweepSrc ssrc{ctx->d_ebar.as<double>(), ctx->d_bsum.as<double>(), ctx->e_prev, ctx->nbcell};
     bte::SweepPlan sp{ctx->p_cell.as<int>(), ctx->p_bidx.as<int>(), ctx->p_dg.as<double>(), ctx->p_vo.as<double>(), ctx->p_nb.as<int>(),
-                      ctx->p_fc.as<double>(), ctx->p_lvl.as<int>(), ctx->p_lvl_off.as<int>(), ctx->n, ctx->F};
+                      ctx->p_fc.as<double>(), ctx->p_lvl.as<int>(), ctx->p_lvl_off.as<int>(), ctx->n, ctx->F,
+                      ctx->n2};
     // launch-shape autotuning on the first sweep of this plan (each candidate
     // computes the same x from the same inputs); the choice is kept per
     // process for the same device and plan shape, so a new context on the
     // same mesh does not time the candidates again
     const int only_margin = sweep_margin_restriction();
-    const SweepTuneKey tkey{ctx->device, ctx->n, ctx->F, ctx->n_dir, nbb, ctx->plan_levels, only_margin};
+    const int only_kernel = sweep_kernel_restriction();
+    const int only_shape = sweep_shape_restriction();
+    const SweepTuneKey tkey{ctx->device, ctx->n, ctx->F, ctx->n_dir, nbb, ctx->plan_levels, only_margin, only_kernel,
+                            only_shape};
     if (!ctx->sweep_tuned) {
         std::lock_guard<std::mutex> lock(g_sweep_tune_mutex);
         auto hit = g_sweep_tune.find(tkey);
@@ -1195,7 +1489,10 @@ static bte_status solve_batch_sweep(bte_ctx* ctx, int b0, int nbb, const bte_opt
         }
     }
     if (!ctx->sweep_tuned) {
-        const std::vector<SweepShape> cand = sweep_candidates(nbb);
+        const std::vector<SweepShape> cand = sweep_candidates(ctx, nbb, only_kernel, only_margin, only_shape);
+        if (cand.empty())
+            return fail(ctx, BTE_ERR_INVALID_ARGUMENT,
+                        "sweep: no launch shape left by BTE_SWEEP_KERNEL / BTE_SWEEP_SHAPE / BTE_SWEEP_MARGIN");
         ctx->sweep_tune_cand = cand;
         ctx->sweep_tune_ms.assign(cand.size(), 0.f);
         cudaEvent_t e0, e1;
@@ -1203,7 +1500,13 @@ static bte_status solve_batch_sweep(bte_ctx* ctx, int b0, int nbb, const bte_opt
         BTE_CUDA(cudaEventCreate(&e1));
         float best = 1e30f;
         for (size_t k = 0; k < cand.size(); ++k) {
+            if (cand[k].staged) {
+                const StageList* sl = nullptr;
+                bte_status s2 = stage_list(ctx, cand[k].cap, &sl);
+                if (s2 != BTE_OK) return s2;
+            }
             BTE_CUDA(cudaEventRecord(e0, st));
+            if (cand[k].staged) launch_sweep_src(ctx, nbb, b0, st, ssrc);  // its right-hand side counts too
             launch_sweep<false>(ctx, cand[k], nbb, b0, st, sp, ssrc, 1, nullptr);
             BTE_LAUNCHED();
             BTE_CUDA(cudaEventRecord(e1, st));
@@ -1221,7 +1524,7 @@ static bte_status solve_batch_sweep(bte_ctx* ctx, int b0, int nbb, const bte_opt
         // margin only when that saves 3 % of the sweeps and reduction, so a
         // near tie (2D meshes) does not flip between runs.
         bool fuse = false;
-        if (ctx->plan_lagged_dirs == 0) {
+        if (ctx->plan_lagged_dirs == 0 && !ctx->sweep_shape.staged) {
             if (only_margin >= 0) fuse = only_margin == 1;
             else {
                 auto time_best = [&](auto&& launch) -> float {
@@ -1267,13 +1570,20 @@ static bte_status solve_batch_sweep(bte_ctx* ctx, int b0, int nbb, const bte_opt
         g_sweep_tune[tkey] = ctx->sweep_shape;
     }
     const SweepShape shape = ctx->sweep_shape;
-    ctx->sweep_margin = shape.margin && ctx->plan_lagged_dirs == 0;
+    if (shape.staged) {  // a shape from the per-process cache: this plan's stage list may not exist yet
+        const StageList* sl = nullptr;
+        bte_status s2 = stage_list(ctx, shape.cap, &sl);
+        if (s2 != BTE_OK) return s2;
+    }
+    ctx->sweep_margin = shape.margin && !shape.staged && ctx->plan_lagged_dirs == 0;
     // algorithmic HBM bytes of a sweep per system and cell: V Omega / D and
     // k / D read, x written (and, with the fused margin, the previous iterate
     // read), plus the level-ordered geometry per direction; ebar and the
     // boundary values come from L2
     const bool margin = ctx->sweep_margin;
     const double sweep_bytes = S * N * (margin ? 4 : 3) * w + geo;
+    if (shape.staged)  // the staged sweep's right-hand side: V Omega / D read, src written (ebar from L2)
+        BTE_LAUNCH(KK_RHS, -1, S * N * 2 * w, 0, launch_sweep_src(ctx, nbb, b0, st, ssrc));
     int sweeps = 0;
     for (;;) {
         if (margin) {
@@ -1399,21 +1709,66 @@ extern "C" bte_status bte_solve(bte_ctx* ctx, const bte_options* opts, bte_repor
         std::memset(&ctx->stats[k], 0, sizeof(bte_kernel_stat));
         std::snprintf(ctx->stats[k].name, sizeof(ctx->stats[k].name), "%s", kKindNames[k]);
     }
+    const auto wall0 = std::chrono::steady_clock::now();
+    auto since = [](std::chrono::steady_clock::time_point t) {
+        return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t).count();
+    };
     if (ctx->dirty) {
+        const auto t = std::chrono::steady_clock::now();
         bte_status s = setup(ctx, o.batch_systems);
         if (s != BTE_OK) return s;
+        rep.ms_host_setup = since(t);
     }
-    if (o.form == BTE_FORM_SWEEP && !ctx->plan_ready) {
+    // new geometry with dsa: the low-order operator's host work runs on a
+    // host thread while the sweep plan is built
+    const bool need_plan = o.form == BTE_FORM_SWEEP && !ctx->plan_ready;
+    const bool need_dsa = o.dsa && !ctx->dsa_ready;
+    DsaSetupHost dsa_host;
+    std::thread dsa_thread;
+    struct Joiner {
+        std::thread& t;
+        ~Joiner() {
+            if (t.joinable()) t.join();
+        }
+    } joiner{dsa_thread};
+    const auto t_dsa = std::chrono::steady_clock::now();
+    bte_status dsa_status = BTE_OK;
+    if (need_dsa) {
+        int nblk = 0;
+        bte_status s = dsa_blocks(ctx, ctx->n, &nblk);
+        if (s != BTE_OK) return s;
+        if (need_plan) {
+            // host part and device part (on its own stream) on a host thread
+            if (!ctx->setup_stream) BTE_CUDA(cudaStreamCreateWithFlags(&ctx->setup_stream, cudaStreamNonBlocking));
+            dsa_thread = std::thread([ctx, nblk, &dsa_host, &dsa_status] {
+                if (cudaSetDevice(ctx->device) != cudaSuccess) {
+                    dsa_status = fail(ctx, BTE_ERR_CUDA, "dsa: cudaSetDevice on the set-up thread failed");
+                    return;
+                }
+                setup_dsa_host(ctx, nblk, dsa_host);
+                dsa_status = setup_dsa_device(ctx, dsa_host, ctx->setup_stream);
+            });
+        } else {
+            setup_dsa_host(ctx, nblk, dsa_host);
+            dsa_status = setup_dsa_device(ctx, dsa_host, ctx->stream);
+        }
+    }
+    if (need_plan) {
+        const auto t = std::chrono::steady_clock::now();
         bte_status s = build_sweep_plan(ctx);
         if (s != BTE_OK) return s;
+        rep.ms_host_plan = since(t);
+        rep.ms_host_order = ctx->ms_last_order;
     }
     if (o.form == BTE_FORM_MIXED && !ctx->mixed_ready) {
         bte_status s = setup_mixed(ctx);
         if (s != BTE_OK) return s;
     }
-    if (o.dsa && !ctx->dsa_ready) {
-        bte_status s = setup_dsa(ctx);
-        if (s != BTE_OK) return s;
+    if (need_dsa) {
+        if (dsa_thread.joinable()) dsa_thread.join();
+        if (dsa_status != BTE_OK) return dsa_status;
+        ctx->dsa_ready = true;
+        rep.ms_host_dsa = since(t_dsa);  // (overlaps the plan's time when both were built)
     }
     // without a wall held at a fixed temperature the low-order operator is singular: dsa is ignored
     const bool dsa_on = o.dsa && ctx->dsa_walls > 0;
@@ -1778,8 +2133,17 @@ extern "C" bte_status bte_solve(bte_ctx* ctx, const bte_options* opts, bte_repor
     BTE_LAUNCHED();
     int dsa_stat[4] = {0, 0, 0, 0};
     if (dsa_on) BTE_CUDA(cudaMemcpyAsync(dsa_stat, ctx->cg_stat.p, sizeof(dsa_stat), cudaMemcpyDeviceToHost, st));
+    int sweep_err = 0;
+    if (o.form == BTE_FORM_SWEEP && ctx->d_sweep_err.p)
+        BTE_CUDA(cudaMemcpyAsync(&sweep_err, ctx->d_sweep_err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
     BTE_CUDA(cudaStreamSynchronize(st));
     if (ctx->profile) prof_resolve(ctx, nullptr, 0);
+    if (sweep_err) {
+        BTE_CUDA(cudaMemsetAsync(ctx->d_sweep_err.p, 0, sizeof(int), st));
+        BTE_CUDA(cudaStreamSynchronize(st));
+        if (report) *report = rep;
+        return fail(ctx, BTE_ERR_CUDA, "sweep: a stage's copies did not complete in time (the fields are not valid)");
+    }
     if (dsa_on) {
         rep.dsa_iterations = dsa_stat[2];
         if (dsa_stat[1]) {
@@ -1792,6 +2156,8 @@ extern "C" bte_status bte_solve(bte_ctx* ctx, const bte_options* opts, bte_repor
     rep.sweep_threads = o.form == BTE_FORM_SWEEP ? ctx->sweep_shape.threads : 0;
     rep.sweep_ring = o.form == BTE_FORM_SWEEP ? ctx->sweep_shape.W : 0;
     rep.sweep_margin = o.form == BTE_FORM_SWEEP && ctx->sweep_margin ? 1 : 0;
+    rep.sweep_staged = o.form == BTE_FORM_SWEEP && ctx->sweep_shape.staged ? 1 : 0;
+    rep.ms_wall = since(wall0);
     ctx->solved = true;
     if (report) *report = rep;
     if (result == BTE_ERR_NOT_CONVERGED && ctx->err.empty()) ctx->err = "max_iter reached";
@@ -1862,15 +2228,17 @@ bte_status bte_get_kernel_stats(bte_ctx* ctx, bte_kernel_stat* stats, int cap, i
     return BTE_OK;
 }
 
-bte_status bte_get_sweep_tuning(bte_ctx* ctx, int* group, int* threads, int* ring, float* ms, int cap, int* n) {
+bte_status bte_get_sweep_tuning(bte_ctx* ctx, int* group, int* threads, int* ring, int* staged, float* ms, int cap,
+                                int* n) {
     if (!ctx || cap < 0) return BTE_ERR_INVALID_ARGUMENT;
     const int m = (int)ctx->sweep_tune_cand.size();
-    if (cap > 0 && (!group || !threads || !ring || !ms)) return BTE_ERR_INVALID_ARGUMENT;
+    if (cap > 0 && (!group || !threads || !ring || !staged || !ms)) return BTE_ERR_INVALID_ARGUMENT;
     for (int k = 0; k < m && k < cap; ++k) {
         const SweepShape& c = ctx->sweep_tune_cand[k];
         group[k] = c.G;
         threads[k] = c.threads;
         ring[k] = c.W;
+        staged[k] = c.staged ? 1 : 0;
         ms[k] = ctx->sweep_tune_ms[k];
     }
     if (n) *n = m;

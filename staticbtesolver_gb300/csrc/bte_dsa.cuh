@@ -43,6 +43,8 @@ struct Lo {
     const int* nb;     // [F][n]
     const float* w;    // [F][n]
     const double* dsc; // [n]
+    const int* agg;    // [n] aggregate of each cell (Coarse::agg_of)
+    const int* nagg;   // [F][n] aggregate of the neighbour nb[f][c] (-1 none)
 };
 
 // Aggregates per block of the coarse correction (dsa_setup.h dsa_coarse).
@@ -72,8 +74,8 @@ struct CgWork {
     float* x;          // [n]
     float* p;          // [n]
     float* u;          // [n] preconditioned residual
-    double* part;      // [nblk][2] per-block partial dot products, then [2] the grid's sums
-    unsigned* bar;     // [2] barrier arrival count and generation (zero before the launch)
+    double* part;      // [2][nblk][2] per-block partial dot products, by round parity
+    unsigned* bar;     // [2] barrier arrivals in this launch (zero before the launch), spare
     int* stat;         // [0] iterations of the last solve, [1] error flag (barrier timeout),
                        // [2] iterations summed over solves
     double* relres;    // [1] final sqrt(r.M r / r0.M r0)
@@ -106,49 +108,46 @@ __device__ __forceinline__ void block_sum2(double& a, double& b) {
 }
 
 // Grid-wide sum of two doubles with one barrier (cooperative launch: every
-// block is resident).  Each block sums its threads' values (fixed order) and
-// publishes the pair; the block that arrives last adds the blocks' pairs in
-// block order (lane l takes blocks l, l+32, ..., then a fixed butterfly), so
-// the sums never depend on which block was last or on timing, writes them
-// once and releases the others, which read just the two sums.  The wait is
-// bounded: after kBarrierPolls polls a block records an error and the call
-// reports failure, so a kernel never spins forever.
-__device__ __forceinline__ bool grid_sum2(double& a, double& b, const CgWork& wk, unsigned nblk) {
-    __shared__ int s_last, s_ok;
+// block is resident).  Each block sums its threads' values (fixed order),
+// publishes the pair in the partials of this round's parity and counts itself
+// in on a counter that only grows during the launch; once the counter reaches
+// round x nblk every block adds the nblk pairs itself, in block order (lane l
+// takes blocks l, l+32, ..., then a fixed butterfly), so every block gets the
+// same sums, independent of timing, without a second hop through a reducing
+// block.  A block can publish round r+1 while another still reads round r
+// (other parity), never round r+2 (that needs every block past round r+1).
+// The wait is bounded: after kBarrierPolls polls a block records an error and
+// the call reports failure, so a kernel never spins forever.
+__device__ __forceinline__ bool grid_sum2(double& a, double& b, const CgWork& wk, unsigned nblk, unsigned& round) {
+    __shared__ int s_ok;
     __shared__ double s_a, s_b;
     block_sum2(a, b);
-    double* sums = wk.part + 2 * (size_t)nblk;
+    ++round;
+    double* part = wk.part + (size_t)(round & 1u) * 2 * nblk;
     if (threadIdx.x == 0) {
-        wk.part[2 * blockIdx.x] = a;
-        wk.part[2 * blockIdx.x + 1] = b;
-        const unsigned gen = ld_acquire(wk.bar + 1);
+        __stcg(part + 2 * blockIdx.x, a);
+        __stcg(part + 2 * blockIdx.x + 1, b);
         __threadfence();
-        const bool last = atomicAdd(wk.bar, 1u) == nblk - 1;
-        s_last = last;
+        atomicAdd(wk.bar, 1u);
+        const unsigned target = round * nblk;
         s_ok = 1;
-        if (!last) {
-            long long k = 0;
-            while (ld_acquire(wk.bar + 1) == gen) {
-                if (++k > kBarrierPolls || *(volatile int*)(wk.stat + 1)) {
-                    atomicExch(wk.stat + 1, 1);
-                    s_ok = 0;
-                    break;
-                }
-                __nanosleep(20);
+        long long k = 0;
+        while (ld_acquire(wk.bar) < target) {
+            if (++k > kBarrierPolls || *(volatile int*)(wk.stat + 1)) {
+                atomicExch(wk.stat + 1, 1);
+                s_ok = 0;
+                break;
             }
-            __threadfence();
-            s_a = __ldcg(sums);
-            s_b = __ldcg(sums + 1);
+            __nanosleep(20);
         }
     }
     __syncthreads();
-    if (s_last && threadIdx.x < 32) {
-        __threadfence();
+    if (threadIdx.x < 32) {
         double x = 0.0, y = 0.0;
 #pragma unroll 4
         for (unsigned i = threadIdx.x; i < nblk; i += 32) {
-            x += __ldcg(wk.part + 2 * i);
-            y += __ldcg(wk.part + 2 * i + 1);
+            x += __ldcg(part + 2 * i);
+            y += __ldcg(part + 2 * i + 1);
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
@@ -156,22 +155,14 @@ __device__ __forceinline__ bool grid_sum2(double& a, double& b, const CgWork& wk
             y += __shfl_xor_sync(0xffffffffu, y, o);
         }
         if (threadIdx.x == 0) {
-            __stcg(sums, x);
-            __stcg(sums + 1, y);
             s_a = x;
             s_b = y;
-            __threadfence();
-            atomicExch(wk.bar, 0u);
-            __threadfence();
-            atomicAdd(wk.bar + 1, 1u);
         }
     }
     __syncthreads();
     a = s_a;
     b = s_b;
-    const bool ok = s_ok != 0;
-    __syncthreads();
-    return ok;
+    return s_ok != 0;
 }
 
 // r_{i+1} of cell c from the previous iteration's parity copies: the one
@@ -290,7 +281,8 @@ __global__ void __launch_bounds__(THREADS) k_dsa_pcg(Lo lo, Coarse co, CgWork wk
             __stcg(co.sums0 + K0 + threadIdx.x, t);
         }
     }
-    if (!grid_sum2(nrm2, unused, wk, nblk)) return;
+    unsigned round = 0;  // barriers passed in this launch
+    if (!grid_sum2(nrm2, unused, wk, nblk, round)) return;
     if (!(nrm2 > 0.0) || !isfinite(nrm2)) {  // nothing to correct
         for (int c = c_lo + threadIdx.x; c < c_hi; c += blockDim.x) xout[c] = 0.0;
         if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -311,12 +303,12 @@ __global__ void __launch_bounds__(THREADS) k_dsa_pcg(Lo lo, Coarse co, CgWork wk
         float acc[AGG][3] = {};
         for (int c = c_lo + threadIdx.x; c < c_hi; c += blockDim.x) {
             const float rc = (float)(lo.dsc[c] * b[c] * inv);
-            const float uc = rc + sX[co.agg_of(c)];
+            const float uc = rc + sX[lo.agg[c]];
             float wc = uc;
             for (int f = 0; f < F; ++f) {
                 const int o = lo.nb[(size_t)f * n + c];
                 if (o < 0) continue;
-                const float uo = (float)(lo.dsc[o] * b[o] * inv) + sX[co.agg_of(o)];
+                const float uo = (float)(lo.dsc[o] * b[o] * inv) + sX[lo.nagg[(size_t)f * n + c]];
                 wc = __fmaf_rn(-lo.w[(size_t)f * n + c], uo, wc);
             }
             __stcg(wk.r + c, rc);
@@ -335,7 +327,7 @@ __global__ void __launch_bounds__(THREADS) k_dsa_pcg(Lo lo, Coarse co, CgWork wk
         const float t = block_sum_aggs(acc, red);
         if (threadIdx.x < 3 * AGG) __stcg(pub + (size_t)3 * K0 + threadIdx.x, t);
     }
-    if (!grid_sum2(gamma, delta, wk, nblk)) return;
+    if (!grid_sum2(gamma, delta, wk, nblk, round)) return;
     const double gamma0 = gamma;
     double alpha = delta > 0.0 ? gamma / delta : 0.0, beta = 0.0;
     int it = 0;
@@ -363,12 +355,13 @@ __global__ void __launch_bounds__(THREADS) k_dsa_pcg(Lo lo, Coarse co, CgWork wk
             wk.p[c] = pc;
             wk.x[c] = __fmaf_rn(fa, pc, wk.x[c]);
             const float rn = __fmaf_rn(fma_, si, ri);
-            const float un = rn + sX[co.agg_of(c)];
+            const int ac = lo.agg[c];
+            const float un = rn + sX[ac];
             float wn = un;
             for (int f = 0; f < F; ++f) {
                 const int o = lo.nb[(size_t)f * n + c];
                 if (o < 0) continue;
-                const float uo = next_residual(wk, P, o, fma_, fb, n) + sX[co.agg_of(o)];
+                const float uo = next_residual(wk, P, o, fma_, fb, n) + sX[lo.nagg[(size_t)f * n + c]];
                 wn = __fmaf_rn(-lo.w[(size_t)f * n + c], uo, wn);
             }
             __stcg(wk.s + (size_t)P * n + c, si);
@@ -377,7 +370,7 @@ __global__ void __launch_bounds__(THREADS) k_dsa_pcg(Lo lo, Coarse co, CgWork wk
             wk.u[c] = un;
             gn = fma((double)rn, (double)un, gn);
             dn = fma((double)wn, (double)un, dn);
-            const int a = (c - c_lo) / co.seg;
+            const int a = ac - K0;
 #pragma unroll
             for (int k = 0; k < AGG; ++k)
                 if (k == a) { acc[k][0] += rn; acc[k][1] += wn; acc[k][2] += si; }
@@ -385,7 +378,7 @@ __global__ void __launch_bounds__(THREADS) k_dsa_pcg(Lo lo, Coarse co, CgWork wk
         const float t = block_sum_aggs(acc, red);
         if (threadIdx.x < 3 * AGG)
             __stcg(co.sums + (size_t)3 * co.n_agg * (P ^ 1) + (size_t)3 * K0 + threadIdx.x, t);
-        if (!grid_sum2(gn, dn, wk, nblk)) return;
+        if (!grid_sum2(gn, dn, wk, nblk, round)) return;
         ++it;
         const double bnew = gn / gamma;
         const double den = dn - bnew * gn / alpha;
@@ -403,6 +396,36 @@ __global__ void __launch_bounds__(THREADS) k_dsa_pcg(Lo lo, Coarse co, CgWork wk
         wk.stat[2] += it;
         wk.relres[0] = sqrt(fabs(gamma / gamma0));
     }
+}
+
+// One step of the in-place Gauss-Jordan inversion of a symmetric positive
+// definite m x m matrix (no pivoting: its pivots stay positive): B = the
+// matrix after eliminating column k of A.  After m steps (A and B swapped
+// between steps) the matrix is the inverse.  A pivot that is not positive
+// sets *bad (the matrix is not positive definite).
+__global__ void k_gj_step(const double* __restrict__ A, double* __restrict__ B, int m, int k, int* bad) {
+    __shared__ double s_rp;
+    const int i = blockIdx.y;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (threadIdx.x == 0) {
+        const double p = A[(size_t)k * m + k];
+        if (!(p > 0.0) && i == 0 && blockIdx.x == 0) atomicExch(bad, 1);
+        s_rp = 1.0 / p;
+    }
+    __syncthreads();
+    if (j >= m) return;
+    const double rp = s_rp;
+    const double aik = A[(size_t)i * m + k], akj = A[(size_t)k * m + j];
+    double v;
+    if (i == k) v = j == k ? rp : akj * rp;
+    else if (j == k) v = -aik * rp;
+    else v = fma(-aik, akj * rp, A[(size_t)i * m + j]);
+    B[(size_t)i * m + j] = v;
+}
+
+__global__ void k_to_float(const double* __restrict__ a, float* __restrict__ out, size_t n) {
+    const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < n) out[q] = (float)a[q];
 }
 
 // Right-hand side V_c (T_c - T_src,c) of the low-order solve, in its numbering:

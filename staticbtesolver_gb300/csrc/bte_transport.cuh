@@ -312,6 +312,7 @@ struct SweepPlan {
     const int* lvl;
     const int* lvl_off;
     int n, F;
+    int n2;  // row length of the per-system arrays (voi, kinv): n rounded up to even
 };
 
 // The diagonal folded into the sweep's coefficients, per system in level
@@ -329,7 +330,7 @@ __global__ void k_sweep_invd(SweepPlan sp, const double* __restrict__ kb, int n_
     const double vo = sp.vo[pj], dg = sp.dg[pj];
     for (int b = 0; b < n_band; ++b) {
         const double invD = 1.0 / fma(kb[b], dg, vo);
-        const size_t q = ((size_t)b * n_dir + d) * sp.n + j;
+        const size_t q = ((size_t)b * n_dir + d) * sp.n2 + j;
         voi[q] = vo * invD;
         kinv[q] = kb[b] * invD;
     }
@@ -448,8 +449,8 @@ __global__ void __launch_bounds__(128, 5) k_sweep(SweepPlan sp, const double* __
     rows.bidx = sp.bidx + (size_t)d * n;
     rows.nb = sp.nb + (size_t)d * sp.F * n;
     rows.fc = sp.fc + (size_t)d * sp.F * n;
-    rows.voi = voi + sys * n;
-    rows.kinv = kinv + sys * n;
+    rows.voi = voi + sys * sp.n2;
+    rows.kinv = kinv + sys * sp.n2;
     rows.eb = src.ebar + (size_t)b * Np;
     rows.bs = src.bsum + ((size_t)d * nbb + (b - b0)) * src.nbcell;
     rows.xold = src.x_old + sys * Np;
@@ -525,6 +526,306 @@ __global__ void __launch_bounds__(128, 5) k_sweep(SweepPlan sp, const double* __
     }
 }
 
+// ---------------------------------------------------------------------------
+// Staged sweep: the substitution of k_sweep with every operand of a level
+// already in shared memory when the level starts.
+//
+// k_sweep's items wait on two dependent loads each level (the cell index, then
+// the cell's ebar and boundary value): load latency along the level chain,
+// not HBM or the FP64 pipe, sets its time.  Here the right-hand side is formed
+// beforehand in level order by k_sweep_src (src = ebar voi + bs/D per system
+// and position, the same fma as k_sweep's), so everything a level reads is a
+// contiguous slice of a position-indexed array: the level's plan records
+// (cell, upstream positions, face coefficients), and per band k/D and src.
+// One thread copies those slices for stage s + 3 into one of three
+// shared-memory buffers with 1-D bulk copies (cp.async.bulk, completion on an
+// mbarrier) while the block solves stage s.  A stage is a level, or a slice of
+// at most `cap` positions of a wider one (positions of one level never depend
+// on each other, so splitting a level keeps the substitution exact).  The
+// arithmetic is k_sweep's term for term, so x is the same to the bit.
+
+// Record of one position in a direction's level order: ints (cell, upstream
+// positions of the FM face slots, padding to 16 bytes), then the FM face
+// coefficients (FP64, padding to 16 bytes).
+template <int FM>
+struct SweepRecLayout {
+    static constexpr int ints = 4 * ((FM + 4) / 4);    // 1 + FM rounded up to 4
+    static constexpr int dbls = 2 * ((FM + 1) / 2);    // FM rounded up to 2
+    static constexpr int bytes = 4 * ints + 8 * dbls;  // 32 (FM 2), 48 (FM 3), 64 (FM 4)
+};
+
+// rec[d][j] from the level-ordered plan arrays (k_sweep_layout's output).
+template <int FM>
+__global__ void k_sweep_records(const int* __restrict__ cell, const int* __restrict__ nb,
+                                const double* __restrict__ fc, int n, int F, int n_dir,
+                                unsigned char* __restrict__ rec) {
+    using L = SweepRecLayout<FM>;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int d = blockIdx.y;
+    if (j >= n) return;
+    unsigned char* r = rec + ((size_t)d * n + j) * L::bytes;
+    int* ri = reinterpret_cast<int*>(r);
+    double* rd = reinterpret_cast<double*>(r + 4 * L::ints);
+    ri[0] = cell[(size_t)d * n + j];
+    for (int f = 0; f < FM; ++f) {
+        const bool in = f < F;
+        ri[1 + f] = in ? nb[((size_t)d * F + f) * n + j] : -1;
+        rd[f] = in ? fc[((size_t)d * F + f) * n + j] : 0.0;
+    }
+    for (int k = 1 + FM; k < L::ints; ++k) ri[k] = -1;
+    for (int k = FM; k < L::dbls; ++k) rd[k] = 0.0;
+}
+
+// src[bl][d][j] = ebar[b][cell] voi[b][d][j] + bs[d][bl][row]/D (row = the
+// cell's boundary row, 0 without one) for the batch's bands bl = b - b0: the
+// right-hand side k_sweep forms inside its level loop, in the same fma.
+// Rows of voi and src are n2 (n rounded up to even) long.
+__global__ void k_sweep_src(const int* __restrict__ cell, const int* __restrict__ bidx,
+                            const double* __restrict__ voi, SweepSrc src, int n, int n2, int n_dir, int nbb, int b0,
+                            size_t Np, double* __restrict__ out) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int s = blockIdx.y;  // bl * n_dir + d
+    if (j >= n) return;
+    const int bl = s / n_dir, d = s - bl * n_dir;
+    const int b = b0 + bl;
+    const size_t pj = (size_t)d * n + j;
+    const int c = cell[pj];
+    const int bi = bidx[pj];
+    const double bs = bi >= 0 ? src.bsum[((size_t)d * nbb + bl) * src.nbcell + bi] : 0.0;
+    const double eb = src.ebar[(size_t)b * Np + c];
+    out[(size_t)s * n2 + j] = fma(eb, voi[((size_t)b * n_dir + d) * n2 + j], bs);
+}
+
+// Shared-memory barrier and bulk-copy primitives (PTX ISA: mbarrier,
+// cp.async.bulk; one CTA, no cluster: the CTA's own shared memory is its
+// shared::cluster window).
+__device__ __forceinline__ unsigned smem_addr(const void* p) {
+    return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_init_fence() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+// One bounded wait for the phase of the given parity: the thread is suspended
+// for at most ~1 us (the suspend-time hint) before the call returns false.
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity), "r"(1000u)
+        : "memory");
+    return ok != 0;
+}
+// Global -> shared, `bytes` a multiple of 16, both addresses 16-byte aligned.
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_addr(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_addr(bar))
+                 : "memory");
+}
+// Orders this thread's earlier generic-proxy accesses to shared memory before
+// later async-proxy ones (a bulk copy into a buffer the block has just read).
+__device__ __forceinline__ void fence_proxy_async_smem() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// Bounded waits on a stage's mbarrier before the block gives up (the copies
+// of a stage complete within microseconds; ~1 s at most, then an error).
+constexpr long long kStagePolls = 1ll << 20;
+
+// Plan of the staged sweep: records, stage bounds and the level order's cells.
+struct StagedPlan {
+    const unsigned char* rec;  // [n_dir][n] records (SweepRecLayout<FM>)
+    const int* stages;         // per direction: start positions of its stages, then n
+    const int* stage_off;      // [n_dir + 1] first entry of direction d in stages
+    const int* cell;           // [n_dir][n] level order (lagged and old upstream values)
+    int n, n2, cap;            // cells, row length of k/D and src, positions per stage (even)
+};
+
+// Bytes of one stage buffer: cap records, then per band of the block k/D and
+// src slices of cap + 2 doubles (a slice starts at an even position).
+template <int FM>
+__host__ __device__ constexpr size_t staged_buffer_bytes(int cap, int G) {
+    return (size_t)cap * SweepRecLayout<FM>::bytes + sizeof(double) * 2 * (size_t)G * (cap + 2);
+}
+// Dynamic shared memory of k_sweep_staged: a 64-byte header (three mbarriers,
+// the bounds of the stage each buffer holds), the ring of G x W solved
+// values, three stage buffers.
+template <int FM>
+__host__ __device__ constexpr size_t staged_smem_bytes(int cap, int G, int W) {
+    return 64 + sizeof(double) * (size_t)G * W + 3 * staged_buffer_bytes<FM>(cap, G);
+}
+
+// One block sweeps direction blockIdx.y for the batch's bands blockIdx.x * G
+// .. + G - 1 (thread t serves band t mod gp, positions t / gp, t / gp +
+// blockDim / gp, ... of each stage, as in k_sweep).  x = e_curr, x_old =
+// e_prev ([band][n_dir][Np]); kinv [band][n_dir][n2] (all bands), srcv
+// [batch band][n_dir][n2] (k_sweep_src).  The ring keeps the last W solved
+// positions per band: a position p is still there during the stage [j0, j1)
+// whenever p >= j1 - W.  A stage's copies that have not landed after
+// kStagePolls polls set *err; the block then waits (bounded) for its copies
+// in flight and returns (x is then not valid; the host reports the error).
+template <int FM>
+__global__ void __launch_bounds__(256) k_sweep_staged(StagedPlan sp, const double* __restrict__ kinv,
+                                                      const double* __restrict__ srcv,
+                                                      const double* __restrict__ x_old, double* x, int first_sweep,
+                                                      int G, int W, int nbb, int b0, int n_dir, size_t Np, int* err) {
+    using L = SweepRecLayout<FM>;
+    extern __shared__ __align__(16) unsigned char smem[];
+    unsigned long long* bar = reinterpret_cast<unsigned long long*>(smem);  // [3]
+    int* hdr = reinterpret_cast<int*>(smem + 32);                           // [3][2] stage bounds per buffer
+    double* ring = reinterpret_cast<double*>(smem + 64);                    // [G][W]
+    unsigned char* bufs = smem + 64 + sizeof(double) * (size_t)G * W;
+    const int cap = sp.cap;
+    const size_t rec_bytes = (size_t)cap * L::bytes;
+    const int vlen = cap + 2;
+    const size_t buf_bytes = staged_buffer_bytes<FM>(cap, G);
+    const int d = blockIdx.y;
+    const int g0 = blockIdx.x * G;
+    const int gn = min(G, nbb - g0);
+    if (gn <= 0) return;
+    int gp = 1;
+    while (gp < gn) gp <<= 1;
+    const int sh = __ffs(gp) - 1;
+    const int bl = threadIdx.x & (gp - 1);
+    const bool serves = bl < gn;
+    const int bb = g0 + (serves ? bl : 0);  // band within the batch
+    const int n = sp.n, n2 = sp.n2;
+    double* xb = x + ((size_t)(b0 + bb) * n_dir + d) * Np;
+    const double* xo = x_old + ((size_t)(b0 + bb) * n_dir + d) * Np;
+    double* rg = ring + (size_t)bl * W;
+    const int* cell_d = sp.cell + (size_t)d * n;
+    const unsigned char* rec_d = sp.rec + (size_t)d * n * L::bytes;
+    const int* stg = sp.stages + sp.stage_off[d];
+    const int ns = sp.stage_off[d + 1] - sp.stage_off[d] - 1;  // stages; stg[0 .. ns]
+    const int per_round = blockDim.x >> sh;
+    const int tpos = threadIdx.x >> sh;
+    // thread 0 copies stage s (bounds j0, j1) into buffer s % 3 and records
+    // the bounds in the buffer's header, where the block reads them
+    auto issue = [&](int s, int j0, int j1) {
+        const int q = s % 3;
+        unsigned char* B = bufs + (size_t)q * buf_bytes;
+        hdr[2 * q] = j0;
+        hdr[2 * q + 1] = j1;
+        const int ja = j0 & ~1, jb = (j1 + 1) & ~1;
+        const unsigned rb = (unsigned)(j1 - j0) * (unsigned)L::bytes;
+        const unsigned vb = (unsigned)(jb - ja) * 8u;
+        mbar_arrive_expect_tx(&bar[q], rb + 2u * (unsigned)gn * vb);
+        bulk_load(B, rec_d + (size_t)j0 * L::bytes, rb, &bar[q]);
+        double* kv = reinterpret_cast<double*>(B + rec_bytes);
+        for (int g = 0; g < gn; ++g) {
+            const size_t sys_all = (size_t)(b0 + g0 + g) * n_dir + d;
+            const size_t sys_batch = (size_t)(g0 + g) * n_dir + d;
+            bulk_load(kv + (size_t)g * vlen, kinv + sys_all * n2 + ja, vb, &bar[q]);
+            bulk_load(kv + (size_t)(G + g) * vlen, srcv + sys_batch * n2 + ja, vb, &bar[q]);
+        }
+    };
+    if (threadIdx.x == 0) {
+        for (int q = 0; q < 3; ++q) mbar_init(&bar[q], 1);
+        mbar_init_fence();
+    }
+    __syncthreads();
+    int issued = 0;  // thread 0: stages whose copies were issued
+    int next_start = 0;  // thread 0: start of the next stage to issue
+    if (threadIdx.x == 0) {
+        int j = stg[0];
+        for (; issued < 3 && issued < ns; ++issued) {
+            const int e = stg[issued + 1];
+            issue(issued, j, e);
+            j = e;
+        }
+        next_start = j;
+    }
+    __syncthreads();  // the headers of the first stages
+    bool failed = false;
+    int s = 0;
+    for (; s < ns; ++s) {
+        const int q = s % 3;
+        const unsigned par = (unsigned)(s / 3) & 1u;
+        // thread 0: the end of stage s + 3, loaded now and used after this stage
+        const int next_end = threadIdx.x == 0 ? stg[min(s + 4, ns)] : 0;
+        long long k = 0;
+        while (!mbar_try_wait(&bar[q], par)) {
+            if (++k > kStagePolls) {
+                failed = true;
+                break;
+            }
+        }
+        if (!failed && serves) {
+            const unsigned char* B = bufs + (size_t)q * buf_bytes;
+            const double* kv = reinterpret_cast<const double*>(B + rec_bytes) + (size_t)bl * vlen;
+            const double* sv = reinterpret_cast<const double*>(B + rec_bytes) + (size_t)(G + bl) * vlen;
+            const int j0 = hdr[2 * q], j1 = hdr[2 * q + 1];
+            const int ja = j0 & ~1;
+            const int keep = j1 - W;  // oldest position still readable from the ring
+            for (int j = j0 + tpos; j < j1; j += per_round) {
+                const unsigned char* r = B + (size_t)(j - j0) * L::bytes;
+                int iv[L::ints];
+                double dv[L::dbls];
+#pragma unroll
+                for (int m = 0; m < L::ints / 4; ++m) {
+                    const int4 t = reinterpret_cast<const int4*>(r)[m];
+                    iv[4 * m] = t.x;
+                    iv[4 * m + 1] = t.y;
+                    iv[4 * m + 2] = t.z;
+                    iv[4 * m + 3] = t.w;
+                }
+#pragma unroll
+                for (int m = 0; m < L::dbls / 2; ++m) {
+                    const double2 t = reinterpret_cast<const double2*>(r + 4 * L::ints)[m];
+                    dv[2 * m] = t.x;
+                    dv[2 * m + 1] = t.y;
+                }
+                double off = 0.0;
+#pragma unroll
+                for (int f = 0; f < FM; ++f) {
+                    const int u = iv[1 + f];
+                    if (u == -1) continue;
+                    double xu;
+                    if (u >= 0) xu = u >= keep ? rg[u & (W - 1)] : xb[cell_d[u]];
+                    else {  // lagged (u = -2 - position): previous sweep's value (or the previous outer iterate)
+                        const int cu = cell_d[-u - 2];
+                        xu = first_sweep ? xo[cu] : xb[cu];
+                    }
+                    off = fma(dv[f], xu, off);
+                }
+                const double v = fma(-kv[j - ja], off, sv[j - ja]);
+                xb[iv[0]] = v;
+                rg[j & (W - 1)] = v;
+            }
+        }
+        if (__syncthreads_or(failed)) {
+            failed = true;
+            break;
+        }
+        if (threadIdx.x == 0 && s + 3 < ns) {
+            fence_proxy_async_smem();  // the block's reads of buffer q come before the copy into it
+            issue(s + 3, next_start, next_end);
+            next_start = next_end;
+            ++issued;
+        }
+    }
+    if (failed && threadIdx.x == 0) {
+        atomicExch(err, 1);
+        // copies still in flight land in this block's shared memory: wait
+        // for them (bounded) before the block exits
+        for (int r = s; r < issued; ++r) {
+            long long k = 0;
+            while (!mbar_try_wait(&bar[r % 3], (unsigned)(r / 3) & 1u) && ++k <= kStagePolls) {
+            }
+        }
+    }
+}
+
 // Residual test of the sweep solution: partials of ||R - A x||^2 and ||R||^2
 // per (row, chunk), positions j in sweep order.
 __global__ void __launch_bounds__(THREADS) k_sweep_residual(FaceFluxOp op, RhsSrc src, const int* __restrict__ perm,
@@ -577,9 +878,16 @@ __global__ void k_inflow_mask(const double* __restrict__ fc, int F, int n, size_
     mask[(size_t)d * n + c] = m;
 }
 
+// pos[d][perm[d][j]] = j: the position of each cell in direction d's order.
+__global__ void k_inverse_perm(const int* __restrict__ perm, int n, int* __restrict__ pos) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int d = blockIdx.y;
+    if (j < n) pos[(size_t)d * n + perm[(size_t)d * n + j]] = j;
+}
+
 // Gather the per-direction geometry into level order.
 __global__ void k_sweep_layout(const int* __restrict__ perm, const int* __restrict__ pos,  // pos [n_dir][n]: cell -> position
-                               const int* __restrict__ lagged,  // [n_dir][F][n] 0/1
+                               const int* __restrict__ lagged,  // [n_dir][F][n] 0/1, or null: none
                                const double* __restrict__ dg, const double* __restrict__ vo,
                                const double* __restrict__ fc, const int* __restrict__ nbr,  // nbr [n][F]
                                const int* __restrict__ bidx,                                // [n] boundary-cell row or -1
@@ -605,7 +913,7 @@ __global__ void k_sweep_layout(const int* __restrict__ perm, const int* __restri
         const size_t q = ((size_t)d * F + k) * n + j;
         const int pu = pos[(size_t)d * n + nbr[(size_t)c * F + f]];
         sfc[q] = v;
-        snb[q] = lagged[((size_t)d * F + f) * n + c] ? -2 - pu : pu;
+        snb[q] = lagged && lagged[((size_t)d * F + f) * n + c] ? -2 - pu : pu;
         ++k;
     }
     for (; k < F; ++k) {

@@ -22,6 +22,7 @@
 #include <algorithm>
 #include <cmath>
 #include <numeric>
+#include <thread>
 #include <vector>
 
 namespace bte {
@@ -65,6 +66,40 @@ inline void dsa_coefficients(int dim, int n, int F, const int* nbr, const double
         gabs *= 0.5;
         return area[(size_t)c * F + f] / solid_angle * (gabs * a1 + beta * a2 * q / delta);
     };
+    // each stored face's coefficient (the expensive part: a sum over the
+    // directions) in parallel, then the scatter in cell order
+    std::vector<double> wv((size_t)n * F, 0.0);
+    auto stored = [&](int c, int f, double* delta) -> bool {
+        const size_t cf = (size_t)c * F + f;
+        const int o = nbr[cf];
+        const double A = area[cf];
+        if (!(A > 0.0)) return false;
+        if (o < 0 || o >= n) {
+            if (!(o < 0 && dirichlet[cf])) return false;
+            *delta = hfac * volume[c] / A;
+            return true;
+        }
+        if (o <= c) return false;  // evaluated once, from the lower-numbered cell
+        *delta = hfac * (volume[c] + volume[o]) / A;
+        return true;
+    };
+    {
+        const int nth = std::max(1, std::min(16, (int)std::thread::hardware_concurrency()));
+        const int T = std::max(1, std::min(nth, n / 8192));
+        auto run = [&](int t) {
+            for (int c = t; c < n; c += T)
+                for (int f = 0; f < F; ++f) {
+                    double delta = 0.0;
+                    if (stored(c, f, &delta)) wv[(size_t)c * F + f] = coefficient(c, f, delta);
+                }
+        };
+        if (T == 1) run(0);
+        else {
+            std::vector<std::thread> pool;
+            for (int t = 0; t < T; ++t) pool.emplace_back(run, t);
+            for (auto& th : pool) th.join();
+        }
+    }
     for (int c = 0; c < n; ++c)
         for (int f = 0; f < F; ++f) {
             const size_t cf = (size_t)c * F + f;
@@ -73,7 +108,7 @@ inline void dsa_coefficients(int dim, int n, int F, const int* nbr, const double
             if (!(A > 0.0)) continue;
             if (o < 0 || o >= n) {
                 if (o < 0 && dirichlet[cf]) {
-                    const double w = coefficient(c, f, hfac * volume[c] / A);
+                    const double w = wv[cf];
                     out.W[(size_t)f * n + c] = w;
                     out.diag[c] += w;
                     ++out.n_dirichlet;
@@ -85,7 +120,7 @@ inline void dsa_coefficients(int dim, int n, int F, const int* nbr, const double
             for (int g = 0; g < F; ++g)
                 if (nbr[(size_t)o * F + g] == c) { back = g; break; }
             if (back < 0) continue;  // a one-sided link (no face of o names c): left out
-            const double w = coefficient(c, f, hfac * (volume[c] + volume[o]) / A);
+            const double w = wv[cf];
             out.W[(size_t)f * n + c] = w;
             out.nb[(size_t)f * n + c] = o;
             out.W[(size_t)back * n + o] = w;
@@ -110,49 +145,92 @@ inline void dsa_coefficients(int dim, int n, int F, const int* nbr, const double
 // adjacency graph by breadth-first distance.
 
 // order[k] = the cell at position k.  Each range of more than `leaf` cells is
-// split at its median breadth-first distance from the farthest cell of a
-// first search (ties by index), then each half again.
+// ordered by breadth-first distance from the farthest cell (found by a first
+// search from the range's first cell), ties by cell index, and split at the
+// median, then each half again; cells the search did not reach (another
+// component of the range) go last.  (Searching from a half's end cell without
+// the first search saves that search but made the aggregates less compact:
+// ~20 % more conjugate-gradient iterations on a 100k-cell square.)  The ranges of one depth are disjoint, so
+// they are ordered in parallel (host threads); the result does not depend on
+// the thread count.
 inline void locality_order(int n, int F, const int* nbr /* [n][F], < 0 none */, int leaf, std::vector<int>& order) {
     order.resize(n);
     std::iota(order.begin(), order.end(), 0);
-    std::vector<int> mark(n, -1), dist(n, -1), queue;
-    queue.reserve(n);
-    std::vector<std::pair<int, int>> stack{{0, n}};
-    int stamp = 0;
-    auto bfs = [&](int src, int id) {  // distances within the cells marked id; returns the last cell reached
-        queue.clear();
-        queue.push_back(src);
-        dist[src] = 0;
-        int last = src;
-        for (size_t h = 0; h < queue.size(); ++h) {
-            const int c = queue[h];
-            last = c;
-            for (int f = 0; f < F; ++f) {
-                const int o = nbr[(size_t)c * F + f];
-                if (o < 0 || o >= n || mark[o] != id || dist[o] >= 0) continue;
-                dist[o] = dist[c] + 1;
-                queue.push_back(o);
-            }
-        }
-        return last;
+    // mark[c] = id of the range being ordered that holds c (unique per depth and range)
+    std::vector<long long> mark(n, -1);
+    std::vector<int> dist(n, -1), scratch(n);
+    struct Work {
+        std::vector<int> queue, count;
     };
-    while (!stack.empty()) {
-        const auto [b, e] = stack.back();
-        stack.pop_back();
-        if (e - b <= std::max(leaf, 1)) continue;
-        const int id = stamp++;
+    struct Range {
+        int b, e;
+    };
+    auto split = [&](const Range& r, long long id, Work& w) {
+        const int b = r.b, e = r.e;
+        auto bfs = [&](int src) {  // distances within the range; returns the last cell reached
+            w.queue.clear();
+            w.queue.push_back(src);
+            dist[src] = 0;
+            int last = src;
+            for (size_t h = 0; h < w.queue.size(); ++h) {
+                const int c = w.queue[h];
+                last = c;
+                for (int f = 0; f < F; ++f) {
+                    const int o = nbr[(size_t)c * F + f];
+                    if (o < 0 || o >= n || mark[o] != id || dist[o] >= 0) continue;
+                    dist[o] = dist[c] + 1;
+                    w.queue.push_back(o);
+                }
+            }
+            return last;
+        };
         for (int k = b; k < e; ++k) { mark[order[k]] = id; dist[order[k]] = -1; }
-        const int far = bfs(order[b], id);
+        const int far = bfs(order[b]);
         for (int k = b; k < e; ++k) dist[order[k]] = -1;
-        bfs(far, id);
-        // cells the search did not reach (another component of the range) go last
-        std::stable_sort(order.begin() + b, order.begin() + e, [&](int x, int y) {
-            const long long dx = dist[x] < 0 ? (1ll << 40) : dist[x], dy = dist[y] < 0 ? (1ll << 40) : dist[y];
-            return dx != dy ? dx < dy : x < y;
-        });
-        const int mid = b + (e - b) / 2;
-        stack.push_back({mid, e});
-        stack.push_back({b, mid});
+        bfs(far);
+        // (distance, index) order: an index sort, then a stable counting sort by distance
+        std::sort(order.begin() + b, order.begin() + e);
+        int dmax = 0;
+        for (int k = b; k < e; ++k) dmax = std::max(dmax, dist[order[k]]);
+        w.count.assign((size_t)dmax + 3, 0);
+        for (int k = b; k < e; ++k) ++w.count[(dist[order[k]] < 0 ? dmax + 1 : dist[order[k]]) + 1];
+        for (int v = 1; v < dmax + 3; ++v) w.count[v] += w.count[v - 1];
+        for (int k = b; k < e; ++k) {
+            const int c = order[k];
+            scratch[b + w.count[dist[c] < 0 ? dmax + 1 : dist[c]]++] = c;
+        }
+        std::copy(scratch.begin() + b, scratch.begin() + e, order.begin() + b);
+    };
+    const int nth = std::max(1, std::min(16, (int)std::thread::hardware_concurrency()));
+    std::vector<Work> work(nth);
+    std::vector<Range> ranges{{0, n}}, next;
+    for (long long depth = 0; !ranges.empty(); ++depth) {
+        std::vector<Range> todo;
+        long long cells = 0;
+        for (const Range& r : ranges)
+            if (r.e - r.b > std::max(leaf, 1)) {
+                todo.push_back(r);
+                cells += r.e - r.b;
+            }
+        // threads only where there is enough work to pay for starting them
+        const int T = (int)std::min<long long>({(long long)nth, (long long)todo.size(), cells / 16384 + 1});
+        auto run = [&](int t) {
+            for (size_t i = t; i < todo.size(); i += T) split(todo[i], depth * (long long)n + todo[i].b, work[t]);
+        };
+        if (T <= 1) {
+            if (!todo.empty()) run(0);
+        } else {
+            std::vector<std::thread> pool;
+            for (int t = 0; t < T; ++t) pool.emplace_back(run, t);
+            for (auto& th : pool) th.join();
+        }
+        next.clear();
+        for (const Range& r : todo) {
+            const int mid = r.b + (r.e - r.b) / 2;
+            next.push_back({r.b, mid});
+            next.push_back({mid, r.e});
+        }
+        ranges.swap(next);
     }
 }
 
@@ -160,24 +238,25 @@ inline void locality_order(int n, int F, const int* nbr /* [n][F], < 0 none */, 
 // and its aggregate a the cells with local index in [a seg, (a+1) seg).
 struct DsaCoarse {
     int nblk = 0, per_block = 0, chunk = 0, seg = 0, n_agg = 0;
-    std::vector<float> ainv;   // [n_agg][n_agg] inverse of the coarse operator (identity rows for empty aggregates)
+    std::vector<double> ac;    // [n_agg][n_agg] coarse operator (identity rows for empty aggregates); its
+                               // inverse is formed on the device (k_gj_step)
     std::vector<int> need_ptr; // [nblk+1] aggregates a block's cells and their neighbours belong to
     std::vector<int> need;
     int agg_of(int c) const { const int k = c / chunk; return k * per_block + (c - k * chunk) / seg; }
 };
 
 // Coarse operator A_c = P^T A P of the scaled low-order operator (unit
-// diagonal, off-diagonal -w[f][c] to nb[f][c], in the permuted numbering) and
-// its inverse by a Cholesky factorisation.  Returns false if A_c is not
-// positive definite (no wall held at a fixed temperature).
-inline bool dsa_coarse(int n, int F, const int* nb /* [F][n] */, const double* w /* [F][n] */, int nblk,
+// diagonal, off-diagonal -w[f][c] to nb[f][c], in the permuted numbering).
+// Symmetric positive definite when a wall holds a fixed temperature.
+inline void dsa_coarse(int n, int F, const int* nb /* [F][n] */, const double* w /* [F][n] */, int nblk,
                        int per_block, DsaCoarse& out) {
     out.nblk = nblk;
     out.per_block = per_block;
     out.chunk = (n + nblk - 1) / nblk;
     out.seg = (out.chunk + per_block - 1) / per_block;
     const int m = out.n_agg = nblk * per_block;
-    std::vector<double> Ac((size_t)m * m, 0.0);
+    std::vector<double>& Ac = out.ac;
+    Ac.assign((size_t)m * m, 0.0);
     std::vector<int> size(m, 0);
     for (int c = 0; c < n; ++c) {
         const int J = out.agg_of(c);
@@ -191,35 +270,6 @@ inline bool dsa_coarse(int n, int F, const int* nb /* [F][n] */, const double* w
     }
     for (int J = 0; J < m; ++J)
         if (size[J] == 0) Ac[(size_t)J * m + J] = 1.0;
-    // Cholesky A_c = L L^T (lower triangle in place), then the inverse column by column
-    std::vector<double> L = Ac;
-    for (int j = 0; j < m; ++j) {
-        double d = L[(size_t)j * m + j];
-        for (int k = 0; k < j; ++k) d -= L[(size_t)j * m + k] * L[(size_t)j * m + k];
-        if (!(d > 0.0)) return false;
-        d = std::sqrt(d);
-        L[(size_t)j * m + j] = d;
-        for (int i = j + 1; i < m; ++i) {
-            double v = L[(size_t)i * m + j];
-            for (int k = 0; k < j; ++k) v -= L[(size_t)i * m + k] * L[(size_t)j * m + k];
-            L[(size_t)i * m + j] = v / d;
-        }
-    }
-    out.ainv.assign((size_t)m * m, 0.0f);
-    std::vector<double> y(m);
-    for (int col = 0; col < m; ++col) {
-        for (int i = 0; i < m; ++i) {  // L y = e_col
-            double v = i == col ? 1.0 : 0.0;
-            for (int k = 0; k < i; ++k) v -= L[(size_t)i * m + k] * y[k];
-            y[i] = v / L[(size_t)i * m + i];
-        }
-        for (int i = m - 1; i >= 0; --i) {  // L^T x = y
-            double v = y[i];
-            for (int k = i + 1; k < m; ++k) v -= L[(size_t)k * m + i] * y[k];
-            y[i] = v / L[(size_t)i * m + i];
-        }
-        for (int i = 0; i < m; ++i) out.ainv[(size_t)i * m + col] = (float)y[i];
-    }
     out.need_ptr.assign(nblk + 1, 0);
     out.need.clear();
     std::vector<int> seen(m, -1);
@@ -240,7 +290,6 @@ inline bool dsa_coarse(int n, int F, const int* nb /* [F][n] */, const double* w
         out.need.insert(out.need.end(), list.begin(), list.end());
         out.need_ptr[k + 1] = (int)out.need.size();
     }
-    return true;
 }
 
 // Where each coupling of the low-order operator finds its neighbour when a

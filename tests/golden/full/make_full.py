@@ -83,7 +83,11 @@ def early(a) -> None:
         el = time.time() - t
     e_sums = r.e.sum(axis=2)  # [n_band][n_dir]
     print(a.name, "outer iterations", r.n_iter, "seconds", round(el, 1), "margins", r.margins, "q", r.q)
+    # the band values themselves: NumPy's exp/expm1 differ in the last bit
+    # across CPU architectures, so another host regenerates them from these
+    bands = synth.debye_bands(len(r.q_band[0]))
     np.savez_compressed(os.path.join(HERE, f"{a.name}_it{a.iterations}.npz"), T_every4=r.T[::4], T_sum=r.T.sum(),
+                        band_vg=bands["vg"], band_tau=bands["tau"], band_C=bands["C"], band_Lr=bands["Lr"],
                         T_sq=np.sum((r.T - p.T_ref) ** 2), e_sums=e_sums, q=r.q, q_band=r.q_band,
                         margins=r.margins, n_iter=r.n_iter, seconds=el, hashes=json.dumps(h))
 

@@ -40,11 +40,11 @@ extern "C" void order_c(int n, int F, const int* nbr, int leaf, int* out) {
     bte::locality_order(n, F, nbr, leaf, o);
     std::copy(o.begin(), o.end(), out);
 }
-extern "C" int coarse_c(int n, int F, const int* nb, const double* w, int nblk, int per, float* ainv, int* geo,
+extern "C" int coarse_c(int n, int F, const int* nb, const double* w, int nblk, int per, double* ac, int* geo,
                         int* need_ptr, int* need) {
     bte::DsaCoarse co;
-    if (!bte::dsa_coarse(n, F, nb, w, nblk, per, co)) return -1;
-    std::copy(co.ainv.begin(), co.ainv.end(), ainv);
+    bte::dsa_coarse(n, F, nb, w, nblk, per, co);
+    std::copy(co.ac.begin(), co.ac.end(), ac);
     geo[0] = co.chunk; geo[1] = co.seg;
     std::copy(co.need_ptr.begin(), co.need_ptr.end(), need_ptr);
     std::copy(co.need.begin(), co.need.end(), need);
@@ -173,12 +173,12 @@ def test_locality_order_and_coarse_operator(lib, oracle_mod, get_case, name):
     F, n = wp.shape
     assert np.array_equal(np.sort(order), np.arange(n))
     m = nblk * per
-    ainv = np.zeros(m * m, np.float32)
+    ac = np.zeros(m * m)
     geo = np.zeros(2, np.int32)
     need_ptr = np.zeros(nblk + 1, np.int32)
     need = np.zeros(m * nblk, np.int32)
     f64p = lambda a: np.ascontiguousarray(a).ctypes.data_as(C.c_void_p)
-    got = lib.coarse_c(n, F, f64p(nbp), f64p(wp), nblk, per, ainv.ctypes.data_as(C.c_void_p),
+    got = lib.coarse_c(n, F, f64p(nbp), f64p(wp), nblk, per, ac.ctypes.data_as(C.c_void_p),
                        geo.ctypes.data_as(C.c_void_p), need_ptr.ctypes.data_as(C.c_void_p),
                        need.ctypes.data_as(C.c_void_p))
     assert got == m
@@ -192,7 +192,18 @@ def test_locality_order_and_coarse_operator(lib, oracle_mod, get_case, name):
     Ac = P.T @ A @ P
     empty = P.sum(0) == 0
     Ac[empty, empty] = 1.0
-    np.testing.assert_allclose(ainv.reshape(m, m) @ Ac, np.eye(m), atol=2e-4)
+    np.testing.assert_allclose(ac.reshape(m, m), Ac, rtol=0, atol=1e-12)
+    # the device inverts it by Gauss-Jordan steps without pivoting (k_gj_step):
+    # the same steps in NumPy reach the inverse of this positive definite matrix
+    G = ac.reshape(m, m).copy()
+    for k in range(m):
+        rp = 1.0 / G[k, k]
+        col, row = G[:, k].copy(), G[k, :].copy()
+        G = G - np.outer(col, row * rp)
+        G[k, :] = row * rp
+        G[:, k] = -col * rp
+        G[k, k] = rp
+    np.testing.assert_allclose(G @ Ac, np.eye(m), atol=1e-9)
     # every block's list holds the aggregates of its cells and of their neighbours
     for k in range(nblk):
         lst = set(need[need_ptr[k]:need_ptr[k + 1]].tolist())

@@ -801,13 +801,28 @@ static bte_status dsa_upload(bte_ctx* ctx, DsaHostPlan& hp, cudaStream_t st) {
         DevBuf ga, gb, gbad;
         BTE_CUDA(upload(ga, co.ac, st));
         BTE_CUDA(gb.alloc(sizeof(double) * (size_t)m * m));
-        BTE_CUDA(gbad.alloc(sizeof(int)));
-        BTE_CUDA(cudaMemsetAsync(gbad.p, 0, sizeof(int), st));
+        BTE_CUDA(gbad.alloc(sizeof(int) * 2));  // [0] error flag, [1] (as unsigned) grid barrier counter
+        BTE_CUDA(cudaMemsetAsync(gbad.p, 0, sizeof(int) * 2, st));
         double* a = ga.as<double>();
         double* b = gb.as<double>();
-        for (int k = 0; k < m; ++k) {
-            bte::dsa::k_gj_step<<<dim3((m + 255) / 256, m), 256, 0, st>>>(a, b, m, k, gbad.as<int>());
-            std::swap(a, b);
+        // one cooperative launch (one block per SM) when every block fits, else one launch per step
+        int coop_ok = 0, occ_gj = 0, sms_gj = 0;
+        BTE_CUDA(cudaDeviceGetAttribute(&coop_ok, cudaDevAttrCooperativeLaunch, ctx->device));
+        BTE_CUDA(cudaDeviceGetAttribute(&sms_gj, cudaDevAttrMultiProcessorCount, ctx->device));
+        BTE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_gj, bte::dsa::k_gj_all, 1024, 0));
+        if (coop_ok && occ_gj >= 1) {
+            const int nb = std::min(sms_gj, m);
+            int* badp = gbad.as<int>();
+            unsigned* barp = reinterpret_cast<unsigned*>(badp + 1);
+            int mm = m;
+            void* args[] = {&a, &b, &mm, &barp, &badp};
+            BTE_CUDA(cudaLaunchCooperativeKernel((const void*)bte::dsa::k_gj_all, dim3(nb), dim3(1024), args, 0, st));
+            if (m % 2) std::swap(a, b);  // the inverse is in A after an even number of steps
+        } else {
+            for (int k = 0; k < m; ++k) {
+                bte::dsa::k_gj_step<<<dim3((m + 255) / 256, m), 256, 0, st>>>(a, b, m, k, gbad.as<int>());
+                std::swap(a, b);
+            }
         }
         BTE_CUDA(ctx->d_co_ainv.alloc(sizeof(float) * (size_t)m * m));
         bte::dsa::k_to_float<<<(unsigned)(((size_t)m * m + 255) / 256), 256, 0, st>>>(
@@ -816,6 +831,7 @@ static bte_status dsa_upload(bte_ctx* ctx, DsaHostPlan& hp, cudaStream_t st) {
         int bad = 0;
         BTE_CUDA(cudaMemcpyAsync(&bad, gbad.p, sizeof(int), cudaMemcpyDeviceToHost, st));
         BTE_CUDA(cudaStreamSynchronize(st));
+        if (bad == 2) return fail(ctx, BTE_ERR_CUDA, "dsa: a grid barrier of the coarse inversion timed out");
         if (bad)
             return fail(ctx, BTE_ERR_INVALID_ARGUMENT,
                         "dsa: the low-order operator is singular (no wall held at a fixed temperature)");
@@ -970,21 +986,24 @@ static bte_status build_sweep_plan(bte_ctx* ctx) {
     std::vector<std::thread> pool;
     std::vector<int> h_perm((size_t)ND * n);
     std::vector<char> lag_any(ND, 0);
+    std::vector<int> fm_dir(ND, 0);  // largest inflow count of a cell, per direction
     for (int t = 0; t < nth; ++t)
         pool.emplace_back([&, t]() {
             for (int d = t; d < ND; d += nth) {
                 bte::level_order(n, F, &mask[(size_t)d * n], ctx->nbr.data(), perm[d], lvl[d], lag[d]);
                 std::copy(perm[d].begin(), perm[d].end(), h_perm.begin() + (size_t)d * n);
                 lag_any[d] = std::any_of(lag[d].begin(), lag[d].end(), [](int v) { return v != 0; });
+                int fm = 0;
+                const uint8_t* md = &mask[(size_t)d * n];
+                for (int c = 0; c < n; ++c) fm = std::max(fm, bte::inflow_count(md[c]));
+                fm_dir[d] = fm;
             }
         });
     for (auto& th : pool) th.join();
     ctx->ms_last_order = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_order).count();
     tm.lap("level order");
     // the sweep's face slots: the largest inflow count of a cell
-    int fm = 0;
-    for (uint8_t m : mask) fm = std::max(fm, bte::inflow_count(m));
-    ctx->plan_fm = fm;
+    ctx->plan_fm = *std::max_element(fm_dir.begin(), fm_dir.end());
     std::vector<int> h_lvl, h_off(ND + 1, 0);
     int lagged_dirs = 0;
     long long levels = 0;

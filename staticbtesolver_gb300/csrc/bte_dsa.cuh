@@ -423,6 +423,62 @@ __global__ void k_gj_step(const double* __restrict__ A, double* __restrict__ B, 
     B[(size_t)i * m + j] = v;
 }
 
+// All m steps of the same inversion in one cooperative launch (every block
+// resident): step k reads src and writes dst (rows by block, columns by
+// thread), then a grid barrier -- a counter that only grows during the
+// launch, zero before it -- and the buffers swap; after the last step the
+// inverse is in A when m is even, else in B.  Values another block wrote are
+// read through L2 (__ldcg).  A wait that runs out (kBarrierPolls polls) sets
+// *bad = 2 and the block returns; a pivot that is not positive sets *bad = 1.
+__global__ void __launch_bounds__(1024) k_gj_all(double* A, double* B, int m, unsigned* bar, int* bad) {
+    __shared__ double s_rp;
+    __shared__ int s_abort;
+    const unsigned nblk = gridDim.x;
+    double* src = A;
+    double* dst = B;
+    for (int k = 0; k < m; ++k) {
+        if (threadIdx.x == 0) {
+            const double p = __ldcg(src + (size_t)k * m + k);
+            if (!(p > 0.0) && blockIdx.x == 0) atomicExch(bad, 1);
+            s_rp = 1.0 / p;
+        }
+        __syncthreads();
+        const double rp = s_rp;
+        for (int i = blockIdx.x; i < m; i += nblk) {
+            const double aik = __ldcg(src + (size_t)i * m + k);
+            for (int j = threadIdx.x; j < m; j += blockDim.x) {
+                const double akj = __ldcg(src + (size_t)k * m + j);
+                double v;
+                if (i == k) v = j == k ? rp : akj * rp;
+                else if (j == k) v = -aik * rp;
+                else v = fma(-aik, akj * rp, __ldcg(src + (size_t)i * m + j));
+                __stcg(dst + (size_t)i * m + j, v);
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            s_abort = 0;
+            __threadfence();
+            atomicAdd(bar, 1u);
+            const unsigned target = (unsigned)(k + 1) * nblk;
+            long long polls = 0;
+            while (ld_acquire(bar) < target) {
+                if (++polls > kBarrierPolls || *(volatile int*)bad == 2) {
+                    atomicExch(bad, 2);
+                    s_abort = 1;
+                    break;
+                }
+                __nanosleep(20);
+            }
+        }
+        __syncthreads();
+        if (s_abort) return;
+        double* t = src;
+        src = dst;
+        dst = t;
+    }
+}
+
 __global__ void k_to_float(const double* __restrict__ a, float* __restrict__ out, size_t n) {
     const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (q < n) out[q] = (float)a[q];

@@ -132,6 +132,9 @@ typedef struct bte_report {
     double ms_host_dsa;        /* ... of building the low-order operator of dsa after new inputs (its host
                                   part runs on a host thread next to the sweep plan's, so the two overlap) */
     double ms_wall;            /* host wall time of the whole call (set-up, solve, read-backs) */
+    int sweep_host_dirs;       /* sweep form: directions of the current plan whose level order was built on the
+                                  host (a cycle in the upwind graph, or a wave wider than the device's frontier
+                                  buffers); the others on the device */
 } bte_report;
 
 /* Fill opts with the reference's defaults (max_iter 10000 as BTEcmd's -I default,
@@ -265,6 +268,14 @@ bte_status bte_get_kernel_stats(bte_ctx* ctx, bte_kernel_stat* stats, int cap, i
  * kernel (the temperatures are the same to the bit either way). */
 bte_status bte_get_sweep_tuning(bte_ctx* ctx, int* group, int* threads, int* ring, int* staged, float* ms, int cap,
                                 int* n);
+
+/* Diagnostics: the current sweep plan's level order of direction d (no
+ * counterpart in the reference): perm[k] = the cell at position k (n_cell
+ * entries); lvl = the level starts, then n_cell (*nlev + 1 entries, written up
+ * to cap_lvl).  Built on the device (one block per direction, Kahn's waves,
+ * each wave in cell-index order); BTE_LEVEL_ORDER=host builds it on the host
+ * instead (the same order).  BTE_ERR_STATE before a sweep-form solve. */
+bte_status bte_get_level_order(bte_ctx* ctx, int d, int* perm, int* lvl, int cap_lvl, int* nlev);
 
 /* The reference's inner-solve operator boundary (src/bicgstab.hpp:65,96,138):
  * BICGSTAB(n, maxit, tol); init(rowptr, colind, val, nnz, b); solve(x) --

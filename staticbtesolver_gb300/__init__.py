@@ -67,7 +67,7 @@ class Report(C.Structure):
                 ("ms_dsa", C.c_double), ("sweep_staged", C.c_int),
                 ("ms_host_setup", C.c_double), ("ms_host_plan", C.c_double), ("ms_host_order", C.c_double),
                 ("ms_host_dsa", C.c_double),
-                ("ms_wall", C.c_double)]
+                ("ms_wall", C.c_double), ("sweep_host_dirs", C.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -127,6 +127,8 @@ def _load():
     L.bte_get_sweep_tuning.argtypes = [vp, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
                                        C.POINTER(C.c_int)]
     L.bte_get_sweep_tuning.restype = C.c_int
+    L.bte_get_level_order.argtypes = [vp, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.POINTER(C.c_int)]
+    L.bte_get_level_order.restype = C.c_int
     L.bte_bicgstab_csr.argtypes = [C.c_int, _ip, _ip, _dp, C.c_int, _dp, _dp, C.c_int, C.c_double,
                                    C.POINTER(C.c_int), C.POINTER(C.c_int)]
     L.bte_dsa_solve.argtypes = [C.c_int, C.c_int, _ip, _dp, _dp, _dp, C.c_double, C.c_int, C.POINTER(C.c_int),
@@ -364,6 +366,16 @@ class Context:
                                                C.byref(n)))
         return [dict(group=int(cols[0][k]), threads=int(cols[1][k]), ring=int(cols[2][k]),
                      kernel="staged" if cols[3][k] else "level", ms=float(cols[4][k])) for k in range(m)]
+
+    def level_order(self, d):
+        """The sweep plan's level order of direction d: (cells in order, level starts then n)."""
+        n = self._dims[0]
+        perm = np.zeros(n, np.int32)
+        lvl = np.zeros(n + 1, np.int32)
+        k = C.c_int(0)
+        self._check(_cuda.bte_get_level_order(self._h, int(d), perm.ctypes.data_as(C.c_void_p),
+                                              lvl.ctypes.data_as(C.c_void_p), n + 1, C.byref(k)))
+        return perm, lvl[:k.value + 1].copy()
 
     def margins(self):
         k = C.c_int(0)

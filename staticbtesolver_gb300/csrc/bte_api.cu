@@ -147,6 +147,9 @@ struct bte_ctx {
     // staged sweep: plan records, level-ordered right-hand side of a batch,
     // error flag of its bounded waits, stage lists by width; row length n2
     DevBuf p_rec, d_ssrc, d_sweep_err;
+    // level-order work: inflow masks, order, positions, level starts, in-degrees, counts
+    DevBuf lo_mask, lo_perm, lo_pos, lo_lvl, lo_indeg, lo_small;
+    int plan_host_dirs = 0;  // directions the last plan ordered on the host
     std::vector<int> plan_lvl, plan_lvl_off;  // host copies of the level starts
     std::map<int, std::unique_ptr<StageList>> stage_lists;
     int n2 = 0;
@@ -966,44 +969,96 @@ static bte_status setup_dsa_device(bte_ctx* ctx, DsaSetupHost& h, cudaStream_t s
 static int sweep_slots(const bte_ctx* ctx) { return std::max(2, std::min(ctx->plan_fm, 4)); }
 
 // Build the sweep plan for every direction from the device's inflow coefficients.
+// BTE_LEVEL_ORDER=host builds every direction's level order on the host
+// (sweep_order.h) instead of on the device (k_level_order); the order is the
+// same either way.
+static bool level_order_on_host() {
+    const char* v = std::getenv("BTE_LEVEL_ORDER");
+    return v && v[0] == 'h';
+}
+
 static bte_status build_sweep_plan(bte_ctx* ctx) {
     HostTimer tm("build_sweep_plan");
     const int n = ctx->n, F = ctx->F, ND = ctx->n_dir;
     const size_t Np = ctx->Np;
     cudaStream_t st = ctx->stream;
-    DevBuf d_mask;
-    BTE_CUDA(d_mask.alloc((size_t)ND * n));
+    BTE_CUDA(ctx->lo_mask.alloc((size_t)ND * n));
     bte::k_inflow_mask<<<dim3((n + 255) / 256, ND), 256, 0, st>>>(ctx->d_fc.as<double>(), F, n, Np, ND,
-                                                                  d_mask.as<uint8_t>());
+                                                                  ctx->lo_mask.as<uint8_t>());
     BTE_LAUNCHED();
-    std::vector<uint8_t> mask((size_t)ND * n);
-    BTE_CUDA(cudaMemcpyAsync(mask.data(), d_mask.p, mask.size(), cudaMemcpyDeviceToHost, st));
-    BTE_CUDA(cudaStreamSynchronize(st));
-    std::vector<std::vector<int>> perm(ND), lvl(ND), lag(ND);
-    tm.lap("inflow mask (device + copy)");
     const auto t_order = std::chrono::steady_clock::now();
-    const int nth = std::max(1, std::min<int>(ND, (int)std::thread::hardware_concurrency()));
-    std::vector<std::thread> pool;
-    std::vector<int> h_perm((size_t)ND * n);
+    // level order: on the device, one block per direction (each wave sorted
+    // in shared memory); a direction with a cycle or a wave wider than the
+    // block's frontier buffers is ordered on the host
+    BTE_CUDA(ctx->lo_perm.alloc(sizeof(int) * (size_t)ND * n));
+    BTE_CUDA(ctx->lo_lvl.alloc(sizeof(int) * (size_t)ND * (n + 1)));
+    BTE_CUDA(ctx->lo_small.alloc(sizeof(int) * (2 * (size_t)ND + 1)));
+    std::vector<int> small(2 * (size_t)ND + 1, 1);  // nlev[ND], status[ND], fmax
+    int* d_small = ctx->lo_small.as<int>();
+    const bool host_all = level_order_on_host();
+    if (!host_all) {
+        BTE_CUDA(ctx->lo_indeg.alloc(sizeof(int) * (size_t)ND * n));
+        int smem_max = 0;
+        BTE_CUDA(cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device));
+        int cap = 1;  // frontier capacity: a power of two, two frontiers in at most 128 KB
+        while (cap < n && (size_t)cap * 2 * 2 * sizeof(int) <= std::min<size_t>(128 * 1024, smem_max - 1024)) cap *= 2;
+        const size_t smem = (size_t)2 * cap * sizeof(int);
+        BTE_CUDA(cudaFuncSetAttribute(bte::k_level_order, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        BTE_CUDA(cudaMemsetAsync(d_small + 2 * ND, 0, sizeof(int), st));
+        bte::k_level_order<<<ND, 1024, smem, st>>>(ctx->lo_mask.as<uint8_t>(), ctx->d_nbr.as<int>(), n, F, cap,
+                                                   ctx->lo_indeg.as<int>(), ctx->lo_perm.as<int>(),
+                                                   ctx->lo_lvl.as<int>(), d_small, d_small + ND, d_small + 2 * ND);
+        BTE_LAUNCHED();
+        BTE_CUDA(cudaMemcpyAsync(small.data(), d_small, sizeof(int) * small.size(), cudaMemcpyDeviceToHost, st));
+        BTE_CUDA(cudaStreamSynchronize(st));
+    }
+    std::vector<int> host_dirs;
+    for (int d = 0; d < ND; ++d)
+        if (host_all || small[ND + d] != 0) host_dirs.push_back(d);
+    std::vector<std::vector<int>> lvl(ND), lag(ND);
     std::vector<char> lag_any(ND, 0);
-    std::vector<int> fm_dir(ND, 0);  // largest inflow count of a cell, per direction
-    for (int t = 0; t < nth; ++t)
-        pool.emplace_back([&, t]() {
-            for (int d = t; d < ND; d += nth) {
-                bte::level_order(n, F, &mask[(size_t)d * n], ctx->nbr.data(), perm[d], lvl[d], lag[d]);
-                std::copy(perm[d].begin(), perm[d].end(), h_perm.begin() + (size_t)d * n);
-                lag_any[d] = std::any_of(lag[d].begin(), lag[d].end(), [](int v) { return v != 0; });
-                int fm = 0;
-                const uint8_t* md = &mask[(size_t)d * n];
-                for (int c = 0; c < n; ++c) fm = std::max(fm, bte::inflow_count(md[c]));
-                fm_dir[d] = fm;
-            }
-        });
-    for (auto& th : pool) th.join();
+    int fm_all = host_all ? 0 : small[2 * ND];
+    if (!host_dirs.empty()) {
+        std::vector<uint8_t> mask((size_t)ND * n);
+        BTE_CUDA(cudaMemcpyAsync(mask.data(), ctx->lo_mask.p, mask.size(), cudaMemcpyDeviceToHost, st));
+        BTE_CUDA(cudaStreamSynchronize(st));
+        std::vector<std::vector<int>> perm(ND);
+        std::vector<int> fm_dir(ND, 0);
+        const int nth = std::max(1, std::min<int>((int)host_dirs.size(), (int)std::thread::hardware_concurrency()));
+        std::vector<std::thread> pool;
+        for (int t = 0; t < nth; ++t)
+            pool.emplace_back([&, t]() {
+                for (size_t k = t; k < host_dirs.size(); k += nth) {
+                    const int d = host_dirs[k];
+                    bte::level_order(n, F, &mask[(size_t)d * n], ctx->nbr.data(), perm[d], lvl[d], lag[d]);
+                    lag_any[d] = std::any_of(lag[d].begin(), lag[d].end(), [](int v) { return v != 0; });
+                    int fm = 0;
+                    const uint8_t* md = &mask[(size_t)d * n];
+                    for (int c = 0; c < n; ++c) fm = std::max(fm, bte::inflow_count(md[c]));
+                    fm_dir[d] = fm;
+                }
+            });
+        for (auto& th : pool) th.join();
+        for (int d : host_dirs) {
+            fm_all = std::max(fm_all, fm_dir[d]);
+            BTE_CUDA(cudaMemcpyAsync(ctx->lo_perm.as<int>() + (size_t)d * n, perm[d].data(), sizeof(int) * n,
+                                     cudaMemcpyHostToDevice, st));
+        }
+        BTE_CUDA(cudaStreamSynchronize(st));  // perm[] goes out of scope
+    }
+    // level starts of the device-ordered directions
+    for (int d = 0; d < ND; ++d) {
+        if (!lvl[d].empty()) continue;
+        lvl[d].resize((size_t)small[d] + 1);
+        BTE_CUDA(cudaMemcpyAsync(lvl[d].data(), ctx->lo_lvl.as<int>() + (size_t)d * (n + 1),
+                                 sizeof(int) * lvl[d].size(), cudaMemcpyDeviceToHost, st));
+    }
+    BTE_CUDA(cudaStreamSynchronize(st));
     ctx->ms_last_order = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_order).count();
+    ctx->plan_host_dirs = (int)host_dirs.size();
     tm.lap("level order");
     // the sweep's face slots: the largest inflow count of a cell
-    ctx->plan_fm = *std::max_element(fm_dir.begin(), fm_dir.end());
+    ctx->plan_fm = fm_all;
     std::vector<int> h_lvl, h_off(ND + 1, 0);
     int lagged_dirs = 0;
     long long levels = 0;
@@ -1015,17 +1070,16 @@ static bte_status build_sweep_plan(bte_ctx* ctx) {
     }
     h_off[ND] = (int)h_lvl.size();
     tm.lap("order arrays");
-    DevBuf d_perm, d_pos, d_lag;
-    BTE_CUDA(upload(d_perm, h_perm, st));
-    tm.lap("order upload");
     // cell -> position from the order on the device; the lagged-edge flags
     // only when some direction has a cycle (none on planar meshes)
-    BTE_CUDA(d_pos.alloc(sizeof(int) * (size_t)ND * n));
-    bte::k_inverse_perm<<<dim3((n + 255) / 256, ND), 256, 0, st>>>(d_perm.as<int>(), n, d_pos.as<int>());
+    DevBuf d_lag;
+    BTE_CUDA(ctx->lo_pos.alloc(sizeof(int) * (size_t)ND * n));
+    bte::k_inverse_perm<<<dim3((n + 255) / 256, ND), 256, 0, st>>>(ctx->lo_perm.as<int>(), n, ctx->lo_pos.as<int>());
     BTE_LAUNCHED();
     if (lagged_dirs > 0) {
-        std::vector<int> h_lag((size_t)ND * F * n);
-        for (int d = 0; d < ND; ++d) std::copy(lag[d].begin(), lag[d].end(), h_lag.begin() + (size_t)d * F * n);
+        std::vector<int> h_lag((size_t)ND * F * n, 0);
+        for (int d = 0; d < ND; ++d)
+            if (!lag[d].empty()) std::copy(lag[d].begin(), lag[d].end(), h_lag.begin() + (size_t)d * F * n);
         BTE_CUDA(upload(d_lag, h_lag, st));
     }
     BTE_CUDA(upload(ctx->p_lvl, h_lvl, st));
@@ -1045,7 +1099,7 @@ static bte_status build_sweep_plan(bte_ctx* ctx) {
         BTE_LAUNCHED();
     }
     bte::k_sweep_layout<<<dim3((n + 255) / 256, ND), 256, 0, st>>>(
-        d_perm.as<int>(), d_pos.as<int>(), lagged_dirs > 0 ? d_lag.as<int>() : nullptr, ctx->d_dg.as<double>(), ctx->d_vo.as<double>(), ctx->d_fc.as<double>(),
+        ctx->lo_perm.as<int>(), ctx->lo_pos.as<int>(), lagged_dirs > 0 ? d_lag.as<int>() : nullptr, ctx->d_dg.as<double>(), ctx->d_vo.as<double>(), ctx->d_fc.as<double>(),
         ctx->d_nbr.as<int>(), ctx->d_bidx.as<int>(), F, n, Np, ND, ctx->p_cell.as<int>(), ctx->p_bidx.as<int>(),
         ctx->p_dg.as<double>(), ctx->p_vo.as<double>(), ctx->p_nb.as<int>(), ctx->p_fc.as<double>());
     BTE_LAUNCHED();
@@ -2177,6 +2231,7 @@ extern "C" bte_status bte_solve(bte_ctx* ctx, const bte_options* opts, bte_repor
     rep.sweep_margin = o.form == BTE_FORM_SWEEP && ctx->sweep_margin ? 1 : 0;
     rep.sweep_staged = o.form == BTE_FORM_SWEEP && ctx->sweep_shape.staged ? 1 : 0;
     rep.ms_wall = since(wall0);
+    rep.sweep_host_dirs = o.form == BTE_FORM_SWEEP ? ctx->plan_host_dirs : 0;
     ctx->solved = true;
     if (report) *report = rep;
     if (result == BTE_ERR_NOT_CONVERGED && ctx->err.empty()) ctx->err = "max_iter reached";
@@ -2244,6 +2299,19 @@ bte_status bte_get_kernel_stats(bte_ctx* ctx, bte_kernel_stat* stats, int cap, i
     if (!ctx) return BTE_ERR_INVALID_ARGUMENT;
     for (int k = 0; k < kNumKinds && k < cap && stats; ++k) stats[k] = ctx->stats[k];
     if (n) *n = kNumKinds;
+    return BTE_OK;
+}
+
+bte_status bte_get_level_order(bte_ctx* ctx, int d, int* perm, int* lvl, int cap_lvl, int* nlev) {
+    if (!ctx || !perm || cap_lvl < 0 || (cap_lvl > 0 && !lvl)) return BTE_ERR_INVALID_ARGUMENT;
+    if (!ctx->plan_ready) return fail(ctx, BTE_ERR_STATE, "bte_get_level_order: no sweep plan (solve in the sweep form first)");
+    if (d < 0 || d >= ctx->n_dir) return fail(ctx, BTE_ERR_INVALID_ARGUMENT, "bte_get_level_order: direction out of range");
+    BTE_CUDA(cudaSetDevice(ctx->device));
+    BTE_CUDA(cudaMemcpy(perm, ctx->p_cell.as<int>() + (size_t)d * ctx->n, sizeof(int) * ctx->n,
+                        cudaMemcpyDeviceToHost));
+    const int l0 = ctx->plan_lvl_off[d], l1 = ctx->plan_lvl_off[d + 1];
+    for (int k = 0; k < l1 - l0 && k < cap_lvl; ++k) lvl[k] = ctx->plan_lvl[l0 + k];
+    if (nlev) *nlev = l1 - l0 - 1;
     return BTE_OK;
 }
 

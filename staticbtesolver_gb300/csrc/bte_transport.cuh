@@ -1,5 +1,7 @@
 // bte_transport.cuh -- assembly, boundary conditions, reductions and heat flux.
 #pragma once
+#include <climits>
+
 #include "bte_kernels.cuh"
 
 namespace bte {
@@ -876,6 +878,112 @@ __global__ void k_inflow_mask(const double* __restrict__ fc, int F, int n, size_
     for (int f = 0; f < F; ++f)
         if (fc[((size_t)d * F + f) * Np + c] != 0.0) m |= (uint8_t)(1u << f);
     mask[(size_t)d * n + c] = m;
+}
+
+// Level order of every direction's upwind graph on the device, one block per
+// direction: Kahn's algorithm in waves (a wave is the cells whose inflow
+// neighbours all lie in earlier waves), each wave sorted by cell index -- the
+// order bte::level_order (sweep_order.h) builds on the host, for acyclic
+// graphs.  mask[d][c] bit f: face f of c is an inflow face; an edge u -> c
+// exists once per such face g of c with nbr[c][g] == u.  Both frontiers live
+// in dynamic shared memory, cap cells each (cap a power of two); a direction
+// whose graph has a cycle (status 1: cells left when no cell is free) or a
+// wave wider than cap (status 2) is left to the host.  Outputs: perm[d][pos],
+// lvl[d][0 .. nlev] (level starts, then n), the largest inflow count over
+// all directions in *fmax; indeg [n_dir][n] is work memory.
+__global__ void __launch_bounds__(1024) k_level_order(const uint8_t* __restrict__ mask, const int* __restrict__ nbr,
+                                                      int n, int F, int cap, int* __restrict__ indeg,
+                                                      int* __restrict__ perm, int* __restrict__ lvl,
+                                                      int* __restrict__ nlev, int* __restrict__ status,
+                                                      int* __restrict__ fmax) {
+    extern __shared__ int fr[];  // [2][cap]
+    __shared__ int cnt[2];
+    __shared__ int s_over;
+    const int d = blockIdx.x;
+    const uint8_t* md = mask + (size_t)d * n;
+    int* ind = indeg + (size_t)d * n;
+    int* pd = perm + (size_t)d * n;
+    int* ld = lvl + (size_t)d * (n + 1);
+    if (threadIdx.x == 0) {
+        cnt[0] = 0;
+        cnt[1] = 0;
+        s_over = 0;
+    }
+    __syncthreads();
+    int fm = 0;
+    for (int c = threadIdx.x; c < n; c += blockDim.x) {
+        const int k = __popc((unsigned)md[c]);
+        fm = max(fm, k);
+        ind[c] = k;
+        if (k == 0) {
+            const int slot = atomicAdd(&cnt[0], 1);
+            if (slot < cap) fr[slot] = c;
+            else s_over = 1;
+        }
+    }
+    if (fm > 0) atomicMax(fmax, fm);
+    __syncthreads();
+    int cur = 0, pos = 0, level = 0;
+    for (;;) {
+        const int m = cnt[cur];
+        if (m == 0 || s_over) break;
+        int* a = fr + (size_t)cur * cap;
+        // bitonic sort of the wave, padded to a power of two (<= cap) with INT_MAX
+        int P = 1;
+        while (P < m) P <<= 1;
+        for (int i = m + threadIdx.x; i < P; i += blockDim.x) a[i] = INT_MAX;
+        __syncthreads();
+        for (int k = 2; k <= P; k <<= 1)
+            for (int j = k >> 1; j > 0; j >>= 1) {
+                for (int i = threadIdx.x; i < P; i += blockDim.x) {
+                    const int l = i ^ j;
+                    if (l > i) {
+                        const int x = a[i], y = a[l];
+                        if ((x > y) == ((i & k) == 0)) {
+                            a[i] = y;
+                            a[l] = x;
+                        }
+                    }
+                }
+                __syncthreads();
+            }
+        for (int i = threadIdx.x; i < m; i += blockDim.x) pd[pos + i] = a[i];
+        if (threadIdx.x == 0) {
+            ld[level] = pos;
+            cnt[cur ^ 1] = 0;
+        }
+        __syncthreads();
+        int* b = fr + (size_t)(cur ^ 1) * cap;
+        for (int i = threadIdx.x; i < m; i += blockDim.x) {
+            const int u = a[i];
+            for (int f = 0; f < F; ++f) {
+                const int c = nbr[(size_t)u * F + f];
+                if (c < 0 || c >= n) continue;
+                bool dup = false;  // c reached through an earlier face of u
+                for (int f2 = 0; f2 < f; ++f2) dup |= nbr[(size_t)u * F + f2] == c;
+                if (dup) continue;
+                const unsigned mc = md[c];
+                for (int g = 0; g < F; ++g) {
+                    if (!((mc >> g) & 1u) || nbr[(size_t)c * F + g] != u) continue;
+                    if (atomicSub(&ind[c], 1) == 1) {
+                        const int slot = atomicAdd(&cnt[cur ^ 1], 1);
+                        if (slot < cap) b[slot] = c;
+                        else s_over = 1;
+                    }
+                }
+            }
+        }
+        pos += m;
+        ++level;
+        cur ^= 1;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const int stat = s_over ? 2 : (pos < n ? 1 : 0);
+        status[d] = stat;
+        nlev[d] = level;
+        if (stat == 0) ld[level] = n;
+    }
 }
 
 // pos[d][perm[d][j]] = j: the position of each cell in direction d's order.

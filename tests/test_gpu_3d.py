@@ -97,3 +97,28 @@ def test_cube200k_first_iterations_match_oracle(sbte, tmp_path):
     print("cube200k after 2 iterations: rel-L2(T - T_ref)", rel_l2(T[::4] - p.T_ref, fx["T_every4"] - p.T_ref),
           "max e-sum difference / max |e-sum|",
           float(np.max(np.abs(e_sums - fx["e_sums"])) / np.abs(fx["e_sums"]).max()))
+
+
+@pytest.mark.parametrize("form_name,tol", [("FORM_SWEEP", 1e-6), ("FORM_PLAIN", 1e-6), ("FORM_MIXED", 1e-5)])
+def test_cube15_converged_matches_oracle(sbte, tmp_path, form_name, tol):
+    """A converged 3D solve against the oracle's (tests/golden/full/cube15_b8.npz:
+    20,250 tetrahedra, 8 bands x 128 directions, 84 outer iterations to margin
+    1e-5, 13 minutes on 8 host threads): the same outer iteration count, T and
+    the heat fluxes within the FP64 bar (1e-6) or the mixed form's (1e-5)."""
+    from staticbtesolver_gb300 import synth
+
+    root = os.path.dirname(os.path.abspath(__file__))
+    fx = np.load(os.path.join(root, "golden", "full", "cube15_b8.npz"))
+    p = synth.make_problem("cube15_b8", str(tmp_path))
+    synth.write_band_file(p.band_file, {k: fx["band_" + k] for k in ("vg", "tau", "C", "Lr")})
+    have = {k: hashlib.sha256(open(getattr(p, k), "rb").read()).hexdigest() for k in ("geo", "band_file", "bc_file")}
+    assert have == json.loads(str(fx["hashes"]))
+    res = _solve(sbte, _args(p), max_iter=1000, tol=1e-5, form=getattr(sbte, form_name))
+    assert res.status == 0
+    if form_name == "FORM_MIXED":  # FP32 inner solves: the margin near the stop moves by their error
+        assert abs(res.report["n_iter"] - int(fx["n_iter"])) <= 2
+    else:
+        assert res.report["n_iter"] == int(fx["n_iter"])
+    assert rel_l2(res.T - p.T_ref, fx["T"] - p.T_ref) < tol
+    big = np.abs(fx["q"]) > 1e-3 * np.abs(fx["q"]).max()
+    np.testing.assert_allclose(res.q[big], fx["q"][big], rtol=tol)

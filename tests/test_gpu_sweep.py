@@ -182,3 +182,48 @@ def test_sweep_kernels_agree(sbte, get_case, monkeypatch, tmp_path, name, shape)
     assert r0["n_iter"] == r1["n_iter"] and r0["inner_iterations"] == r1["inner_iterations"]
     assert np.array_equal(T0, T1)
     assert np.array_equal(m0, m1)
+
+
+@pytest.mark.parametrize("name", ["square16_b8", "2DM2DG", "3DM2DG", "cube5_b8", "square16_b8/cycles", "slab1d/odd",
+                                  "2Dcase5"])
+def test_device_level_order_matches_host(sbte, get_case, monkeypatch, tmp_path, name):
+    """The sweep plan's level order built on the device (k_level_order: one
+    block per direction, Kahn's waves, each wave sorted by cell index in
+    shared memory) is the host's (sweep_order.h, BTE_LEVEL_ORDER=host) entry
+    for entry.  Directions whose upwind graph has a cycle are ordered on the
+    host in both runs (they need the host's cycle breaking)."""
+    from staticbtesolver_gb300 import synth
+
+    base = name.split("/")[0]
+    if base.startswith("cube"):
+        p = synth.make_problem(base, str(tmp_path))
+        args = (p.geo, p.bc_file, p.band_file, p.DM, p.num_theta, p.num_phi, p.T_ref, p.L_x, p.L_y, p.L_z)
+        c = None
+    else:
+        c = get_case(base)
+        args = _odd_slab(c) if name.endswith("/odd") else c.args()
+    orders, host_dirs = {}, {}
+    for where in ("device", "host"):
+        if where == "host":
+            monkeypatch.setenv("BTE_LEVEL_ORDER", "host")
+        else:
+            monkeypatch.delenv("BTE_LEVEL_ORDER", raising=False)
+        if name.endswith("/cycles"):
+            ctx = sbte.Context(0).set_arrays(_rewired(sbte, c, n_swaps=10))
+        else:
+            ctx = sbte.Context(0).load(sbte.Problem(*args))
+        st, rep = ctx.solve(max_iter=2, tol=0.0, form=sbte.FORM_SWEEP)
+        nd = ctx._dims[1]
+        orders[where] = [ctx.level_order(d) for d in range(nd)]
+        host_dirs[where] = rep.sweep_host_dirs
+        ctx.close()
+    assert host_dirs["host"] == nd
+    if name.endswith("/cycles"):
+        assert host_dirs["device"] > 0  # (here every direction's graph has a cycle)
+    else:
+        assert host_dirs["device"] == 0
+    for d in range(nd):
+        (pd, ld), (ph, lh) = orders["device"][d], orders["host"][d]
+        assert np.array_equal(pd, ph), d
+        assert np.array_equal(ld, lh), d
+        assert np.array_equal(np.sort(pd), np.arange(len(pd)))

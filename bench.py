@@ -520,7 +520,7 @@ def run_ours(args, rank, world, local):
                        "mixed_fp32_fp64_form": mixed,
                        "sweep_shape": {"bands_per_block": last["sweep_group"], "threads": last["sweep_threads"],
                                        "ring": last["sweep_ring"],
-                                       "kernel": "k_sweep_staged" if last["sweep_staged"] else "k_sweep",
+                                       "kernel": ("k_sweep", "k_sweep_staged")[last["sweep_kernel"]],
                                        "margin_summed_in": "sweep" if last["sweep_margin"] else "k_reduce"},
                        "speedup_vs_plain_fp64": (plain["s_extrapolated"] / t_step)
                        if plain and "s_extrapolated" in plain else None},

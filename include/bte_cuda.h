@@ -123,9 +123,9 @@ typedef struct bte_report {
     int dsa_solves;            /* low-order corrections applied (dsa) */
     long long dsa_iterations;  /* conjugate-gradient iterations summed over them */
     double ms_dsa;             /* device time of the corrections (included in ms_reduce and ms_total) */
-    int sweep_staged;          /* sweep form: 1 the staged kernel was chosen (levels copied to shared memory
-                                  ahead by bulk copies, right-hand side formed beforehand), 0 the
-                                  level-synchronous one; the autotuner times both */
+    int sweep_kernel;          /* sweep form: the kernel the autotuner chose -- 0 level-synchronous (k_sweep),
+                                  1 staged (levels copied to shared memory ahead by bulk copies, right-hand
+                                  side from a level-ordered pre-pass) */
     double ms_host_setup;      /* host wall time of this call's set-up after new inputs (uploads, geometry) */
     double ms_host_plan;       /* ... of building the sweep plan (level order, layout) after new geometry */
     double ms_host_order;      /*     of which the level order (host threads over directions) */
@@ -261,12 +261,13 @@ bte_status bte_get_kernel_stats(bte_ctx* ctx, bte_kernel_stat* stats, int cap, i
 /* The sweep autotuner's table from the first sweep of the current plan (empty
  * when the choice came from the per-process cache): candidate k ran with
  * group[k] bands and threads[k] threads per block and ring[k] positions per
- * band, with the level-synchronous (staged[k] = 0) or the staged kernel
- * (staged[k] = 1), in ms[k] milliseconds.  Entries are written up to cap
- * (arrays may be NULL when cap is 0); *n = candidates timed.  The environment
- * variable BTE_SWEEP_KERNEL=level|staged restricts the candidates to one
- * kernel (the temperatures are the same to the bit either way). */
-bte_status bte_get_sweep_tuning(bte_ctx* ctx, int* group, int* threads, int* ring, int* staged, float* ms, int cap,
+ * band, with kernel[k] (0 level-synchronous, 1 staged, as
+ * bte_report.sweep_kernel), in ms[k] milliseconds.  Entries are written up
+ * to cap (arrays may be NULL when cap is 0); *n = candidates timed.  The
+ * environment variable BTE_SWEEP_KERNEL=level|staged restricts the
+ * candidates to one kernel (the temperatures are the same to the bit either
+ * way). */
+bte_status bte_get_sweep_tuning(bte_ctx* ctx, int* group, int* threads, int* ring, int* kernel, float* ms, int cap,
                                 int* n);
 
 /* Diagnostics: the current sweep plan's level order of direction d (no

@@ -64,7 +64,7 @@ class Report(C.Structure):
                 ("kernel_launches", C.c_longlong), ("sweep_group", C.c_int), ("sweep_threads", C.c_int),
                 ("accel_steps", C.c_int), ("accel_reverts", C.c_int), ("sweep_ring", C.c_int),
                 ("sweep_margin", C.c_int), ("dsa_solves", C.c_int), ("dsa_iterations", C.c_longlong),
-                ("ms_dsa", C.c_double), ("sweep_staged", C.c_int),
+                ("ms_dsa", C.c_double), ("sweep_kernel", C.c_int),
                 ("ms_host_setup", C.c_double), ("ms_host_plan", C.c_double), ("ms_host_order", C.c_double),
                 ("ms_host_dsa", C.c_double),
                 ("ms_wall", C.c_double), ("sweep_host_dirs", C.c_int)]
@@ -365,7 +365,7 @@ class Context:
         self._check(_cuda.bte_get_sweep_tuning(self._h, *[c.ctypes.data_as(C.c_void_p) for c in cols], m,
                                                C.byref(n)))
         return [dict(group=int(cols[0][k]), threads=int(cols[1][k]), ring=int(cols[2][k]),
-                     kernel="staged" if cols[3][k] else "level", ms=float(cols[4][k])) for k in range(m)]
+                     kernel=("level", "staged")[int(cols[3][k])], ms=float(cols[4][k])) for k in range(m)]
 
     def level_order(self, d):
         """The sweep plan's level order of direction d: (cells in order, level starts then n)."""

@@ -80,6 +80,8 @@ struct SweepShape {
     bool margin = false;  // acyclic plans: the sweep sums the margin partials (else k_reduce does)
     bool staged = false;  // k_sweep_staged (right-hand side from k_sweep_src, levels staged by bulk copies)
     int cap = 0;          // staged: positions per stage
+    int kind() const { return staged ? 1 : 0; }
+    bool prepass() const { return staged; }  // needs k_sweep_src's right-hand side
 };
 
 // Stage bounds of the staged sweep for one stage width: per direction, its
@@ -1579,7 +1581,7 @@ static bte_status solve_batch_sweep(bte_ctx* ctx, int b0, int nbb, const bte_opt
                 if (s2 != BTE_OK) return s2;
             }
             BTE_CUDA(cudaEventRecord(e0, st));
-            if (cand[k].staged) launch_sweep_src(ctx, nbb, b0, st, ssrc);  // its right-hand side counts too
+            if (cand[k].prepass()) launch_sweep_src(ctx, nbb, b0, st, ssrc);  // its right-hand side counts too
             launch_sweep<false>(ctx, cand[k], nbb, b0, st, sp, ssrc, 1, nullptr);
             BTE_LAUNCHED();
             BTE_CUDA(cudaEventRecord(e1, st));
@@ -1597,7 +1599,7 @@ static bte_status solve_batch_sweep(bte_ctx* ctx, int b0, int nbb, const bte_opt
         // margin only when that saves 3 % of the sweeps and reduction, so a
         // near tie (2D meshes) does not flip between runs.
         bool fuse = false;
-        if (ctx->plan_lagged_dirs == 0 && !ctx->sweep_shape.staged) {
+        if (ctx->plan_lagged_dirs == 0 && !ctx->sweep_shape.prepass()) {
             if (only_margin >= 0) fuse = only_margin == 1;
             else {
                 auto time_best = [&](auto&& launch) -> float {
@@ -1648,14 +1650,14 @@ static bte_status solve_batch_sweep(bte_ctx* ctx, int b0, int nbb, const bte_opt
         bte_status s2 = stage_list(ctx, shape.cap, &sl);
         if (s2 != BTE_OK) return s2;
     }
-    ctx->sweep_margin = shape.margin && !shape.staged && ctx->plan_lagged_dirs == 0;
+    ctx->sweep_margin = shape.margin && !shape.prepass() && ctx->plan_lagged_dirs == 0;
     // algorithmic HBM bytes of a sweep per system and cell: V Omega / D and
     // k / D read, x written (and, with the fused margin, the previous iterate
     // read), plus the level-ordered geometry per direction; ebar and the
     // boundary values come from L2
     const bool margin = ctx->sweep_margin;
     const double sweep_bytes = S * N * (margin ? 4 : 3) * w + geo;
-    if (shape.staged)  // the staged sweep's right-hand side: V Omega / D read, src written (ebar from L2)
+    if (shape.prepass())  // the staged sweep's right-hand side: V Omega / D read, src written (ebar from L2)
         BTE_LAUNCH(KK_RHS, -1, S * N * 2 * w, 0, launch_sweep_src(ctx, nbb, b0, st, ssrc));
     int sweeps = 0;
     for (;;) {
@@ -2229,7 +2231,7 @@ extern "C" bte_status bte_solve(bte_ctx* ctx, const bte_options* opts, bte_repor
     rep.sweep_threads = o.form == BTE_FORM_SWEEP ? ctx->sweep_shape.threads : 0;
     rep.sweep_ring = o.form == BTE_FORM_SWEEP ? ctx->sweep_shape.W : 0;
     rep.sweep_margin = o.form == BTE_FORM_SWEEP && ctx->sweep_margin ? 1 : 0;
-    rep.sweep_staged = o.form == BTE_FORM_SWEEP && ctx->sweep_shape.staged ? 1 : 0;
+    rep.sweep_kernel = o.form == BTE_FORM_SWEEP ? ctx->sweep_shape.kind() : 0;
     rep.ms_wall = since(wall0);
     rep.sweep_host_dirs = o.form == BTE_FORM_SWEEP ? ctx->plan_host_dirs : 0;
     ctx->solved = true;
@@ -2315,17 +2317,17 @@ bte_status bte_get_level_order(bte_ctx* ctx, int d, int* perm, int* lvl, int cap
     return BTE_OK;
 }
 
-bte_status bte_get_sweep_tuning(bte_ctx* ctx, int* group, int* threads, int* ring, int* staged, float* ms, int cap,
+bte_status bte_get_sweep_tuning(bte_ctx* ctx, int* group, int* threads, int* ring, int* kernel, float* ms, int cap,
                                 int* n) {
     if (!ctx || cap < 0) return BTE_ERR_INVALID_ARGUMENT;
     const int m = (int)ctx->sweep_tune_cand.size();
-    if (cap > 0 && (!group || !threads || !ring || !staged || !ms)) return BTE_ERR_INVALID_ARGUMENT;
+    if (cap > 0 && (!group || !threads || !ring || !kernel || !ms)) return BTE_ERR_INVALID_ARGUMENT;
     for (int k = 0; k < m && k < cap; ++k) {
         const SweepShape& c = ctx->sweep_tune_cand[k];
         group[k] = c.G;
         threads[k] = c.threads;
         ring[k] = c.W;
-        staged[k] = c.staged ? 1 : 0;
+        kernel[k] = c.kind();
         ms[k] = ctx->sweep_tune_ms[k];
     }
     if (n) *n = m;

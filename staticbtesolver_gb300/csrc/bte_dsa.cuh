@@ -332,9 +332,16 @@ __global__ void __launch_bounds__(THREADS) k_dsa_pcg(Lo lo, Coarse co, CgWork wk
     double alpha = delta > 0.0 ? gamma / delta : 0.0, beta = 0.0;
     int it = 0;
     bool stop = !(delta > 0.0) || gamma <= tol * tol * gamma0;
+    // the iteration's scalars, formed once per block by thread 0 (FP64
+    // divisions are slow on this part's FP64 pipe) and read by every thread:
+    // alpha and beta, their FP32 forms, the stop flag
+    __shared__ double s_alpha, s_beta;
+    __shared__ float s_fa, s_fb;
+    __shared__ int s_stop;
+    float fa = (float)alpha, fb = (float)beta;
     while (!stop && it < maxit) {
         const int P = it & 1;
-        const float fa = (float)alpha, fma_ = -(float)alpha, fb = (float)beta;
+        const float fma_ = -fa;
         // P^T r_{i+1} of every aggregate from the published sums, then the coarse solve
         const float* got = co.sums + (size_t)3 * co.n_agg * P;
         for (int K = threadIdx.x; K < co.n_agg; K += blockDim.x) {
@@ -380,14 +387,27 @@ __global__ void __launch_bounds__(THREADS) k_dsa_pcg(Lo lo, Coarse co, CgWork wk
             __stcg(co.sums + (size_t)3 * co.n_agg * (P ^ 1) + (size_t)3 * K0 + threadIdx.x, t);
         if (!grid_sum2(gn, dn, wk, nblk, round)) return;
         ++it;
-        const double bnew = gn / gamma;
-        const double den = dn - bnew * gn / alpha;
+        if (threadIdx.x == 0) {  // every thread holds the same gn, dn, gamma, alpha
+            const double bnew = gn / gamma;
+            const double den = dn - bnew * gn / alpha;
+            const bool st = gn <= tol * tol * gamma0 || !(den > 0.0) || !isfinite(den);
+            s_stop = st;
+            if (!st) {
+                s_beta = bnew;
+                s_alpha = gn / den;
+                s_fa = (float)s_alpha;
+                s_fb = (float)bnew;
+            }
+        }
+        __syncthreads();
         gamma = gn;
-        if (gn <= tol * tol * gamma0 || !(den > 0.0) || !isfinite(den)) {
+        if (s_stop) {
             stop = true;
         } else {
-            beta = bnew;
-            alpha = gn / den;
+            beta = s_beta;
+            alpha = s_alpha;
+            fa = s_fa;
+            fb = s_fb;
         }
     }
     for (int c = c_lo + threadIdx.x; c < c_hi; c += blockDim.x) xout[c] = (double)wk.x[c] * lo.dsc[c] * scale;

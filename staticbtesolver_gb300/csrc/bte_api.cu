@@ -64,11 +64,11 @@ struct DevBuf {
 constexpr int kGroup = 8;  // BiCGSTAB iterations launched between host checks
 
 enum KernelKind { KK_P, KK_SPMV1, KK_S, KK_SPMV2, KK_X, KK_INIT, KK_RHS, KK_REDUCE, KK_DIFFUSE, KK_HEAT, KK_SWEEP,
-                  KK_SWEEP_RES, KK_DSA, kNumKinds };
+                  KK_SWEEP_RES, KK_DSA, KK_BICG, kNumKinds };
 const char* kKindNames[kNumKinds] = {"bicg_p_update", "bicg_spmv1",   "bicg_s_update", "bicg_spmv2",
                                      "bicg_x_update", "bicg_init",    "rhs_assembly",  "reduce_margin",
                                      "diffuse_wall",  "heat_flux",    "upwind_sweep",  "sweep_residual",
-                                     "dsa_correction"};
+                                     "dsa_correction", "bicg_persistent"};
 
 }  // namespace
 
@@ -255,7 +255,9 @@ static void prof_resolve(bte_ctx* ctx, const int* active, int n_active) {
         bte_kernel_stat& st = ctx->stats[p.kind];
         st.launches += 1;
         st.ms += ms;
-        const double act = (active && p.iter >= 0 && p.iter < n_active) ? active[p.iter] : 0.0;
+        double act = (active && p.iter >= 0 && p.iter < n_active) ? active[p.iter] : 0.0;
+        if (active && p.iter == -2)  // one launch over every iteration: all active system-iterations
+            for (int k = 0; k < n_active; ++k) act += active[k];
         st.bytes += p.bytes_fixed + p.bytes_per_active * act;
     }
     ctx->pending.clear();
@@ -725,7 +727,10 @@ struct DsaHostPlan {
     bte::DsaCoarse co;
 };
 
-static void dsa_host_plan(int n, int F, const int* nb, const double* W, int nblk, DsaHostPlan& hp) {
+// pre_order / pre_cm (optional): a locality order already computed for the
+// coupling pattern pre_cm ([n][F]); used when the pattern of W is the same.
+static void dsa_host_plan(int n, int F, const int* nb, const double* W, int nblk, DsaHostPlan& hp,
+                          std::vector<int>* pre_order = nullptr, const std::vector<int>* pre_cm = nullptr) {
     HostTimer tm("dsa_host_plan");
     hp.n = n;
     hp.F = F;
@@ -740,7 +745,8 @@ static void dsa_host_plan(int n, int F, const int* nb, const double* W, int nblk
         for (int c = 0; c < n; ++c) cm[(size_t)c * F + f] = W[(size_t)f * n + c] > 0.0 ? nb[(size_t)f * n + c] : -1;
     const int agg_cells = std::max(1, n / (nblk * bte::dsa::AGG));
     tm.lap("scaling");
-    bte::locality_order(n, F, cm.data(), std::max(8, agg_cells / 2), hp.order);
+    if (pre_order && pre_cm && *pre_cm == cm) hp.order.swap(*pre_order);
+    else bte::locality_order(n, F, cm.data(), std::max(8, agg_cells / 2), hp.order);
     tm.lap("locality order");
     const std::vector<int>& order = hp.order;
     std::vector<int>& pos = hp.pos;
@@ -766,11 +772,10 @@ static void dsa_host_plan(int n, int F, const int* nb, const double* W, int nblk
     }
     tm.lap("permuted operator");
     bte::dsa_coarse(n, F, hp.nbv.data(), wd.data(), nblk, bte::dsa::AGG, hp.co);
-    hp.agg.assign(n, 0);
+    hp.agg = hp.co.agg;
     hp.nagg.assign((size_t)F * n, -1);
-    for (int k = 0; k < n; ++k) hp.agg[k] = hp.co.agg_of(k);
     for (size_t q = 0; q < (size_t)F * n; ++q)
-        if (hp.nbv[q] >= 0) hp.nagg[q] = hp.co.agg_of(hp.nbv[q]);
+        if (hp.nbv[q] >= 0) hp.nagg[q] = hp.agg[hp.nbv[q]];
     tm.lap("coarse operator");
 }
 
@@ -946,13 +951,33 @@ static void setup_dsa_host(const bte_ctx* ctx, int nblk, DsaSetupHost& out) {
         fixed[cf] = row < 0 || ctx->bc_type[row] == 1;
     }
     HostTimer tm("setup_dsa_host");
+    // the locality order needs only the coupling pattern, which the topology
+    // gives (an interior face with positive area that both cells name); it
+    // runs on a second thread while the coefficients are computed, and is
+    // used if the coefficients' own pattern is the same (it always is unless
+    // a coefficient is zero)
+    std::vector<int> cm_topo((size_t)n * F, -1), pre_order;
+    for (int c = 0; c < n; ++c)
+        for (int f = 0; f < F; ++f) {
+            const size_t cf = (size_t)c * F + f;
+            const int o = ctx->nbr[cf];
+            if (o < 0 || o >= n || !(ctx->area[cf] > 0.0)) continue;
+            bool back = false;
+            for (int g = 0; g < F; ++g) back |= ctx->nbr[(size_t)o * F + g] == c;
+            if (back) cm_topo[cf] = o;
+        }
+    const int agg_cells = std::max(1, n / (nblk * bte::dsa::AGG));
+    std::thread order_thread(
+        [&] { bte::locality_order(n, F, cm_topo.data(), std::max(8, agg_cells / 2), pre_order); });
     bte::DsaCoefficients co;
     bte::dsa_coefficients(ctx->dim, n, F, ctx->nbr.data(), ctx->area.data(), ctx->normal.data(), ctx->volume.data(),
                           ctx->n_dir, ctx->s.data(), ctx->S.data(), ctx->solid_angle, ctx->n_band, ctx->vg.data(),
                           ctx->tau.data(), ctx->Lr.data(), fixed, kDsaBeta, co);
     tm.lap("coefficients");
+    order_thread.join();
+    tm.lap("locality order (joined)");
     out.n_dirichlet = co.n_dirichlet;
-    if (co.n_dirichlet > 0) dsa_host_plan(n, F, co.nb.data(), co.W.data(), nblk, out.hp);
+    if (co.n_dirichlet > 0) dsa_host_plan(n, F, co.nb.data(), co.W.data(), nblk, out.hp, &pre_order, &cm_topo);
 }
 
 // ... and the device part.
@@ -1178,6 +1203,18 @@ static bte_status build_sweep_plan(bte_ctx* ctx) {
 // Solve all systems of one batch (bands b0 .. b0+nbb-1, every direction) with
 // the plain FP64 BiCGSTAB; x lands in e_curr.
 
+// BTE_KRYLOV=persistent runs the Krylov forms' BiCGSTAB as one persistent
+// launch per batch (k_bicg_persistent: one block per system) instead of one
+// launch per phase with the host checking every kGroup iterations; x is the
+// same to the bit either way.  The phase kernels stay the default: they
+// spread every phase over all chunks of all systems, and on GB300 the
+// persistent form measured 1.3x (square20k) to 3x (square100k) slower per
+// outer iteration -- its per-system parallelism is one block.
+static bool krylov_persistent() {
+    const char* v = std::getenv("BTE_KRYLOV");
+    return v && v[0] == 'p' && v[1] == 'e';
+}
+
 static bte_status solve_batch_plain(bte_ctx* ctx, int b0, int nbb, const bte_options& o, bte_report& rep) {
     {
         const size_t bytes = sizeof(double) * (size_t)ctx->nbb * ctx->n_dir * ctx->Np;
@@ -1231,7 +1268,12 @@ static bte_status solve_batch_plain(bte_ctx* ctx, int b0, int nbb, const bte_opt
     BTE_LAUNCH(KK_INIT, -1, S * N * 7 * w + geo / 2, 0, bte::k_bicg_init<<<grid, bte::THREADS, 0, st>>>(op, v, bs));
     BTE_LAUNCH(KK_INIT, -1, 0, 0, bte::k_bicg_init_scalars<<<(S + 127) / 128, 128, 0, st>>>(bs, nullptr));
     int i = 1;
-    for (;;) {
+    if (krylov_persistent()) {
+        // every iteration of every system in one launch: 25 N w per active
+        // system-iteration (the five phases' vector passes) + the geometry
+        BTE_LAUNCH(KK_BICG, -2, 0, N * 25 * w, bte::k_bicg_persistent<<<S, bte::THREADS, 0, st>>>(op, v, bs, total + 1));
+    }
+    for (; !krylov_persistent();) {
         int last = i;
         for (int g = 0; g < kGroup && i <= total + 1; ++g, ++i) {
             BTE_LAUNCH(KK_P, i, 0, N * 6 * w, bte::k_bicg_p<<<grid, bte::THREADS, 0, st>>>(op, v, bs, i));
@@ -1326,7 +1368,10 @@ static bte_status solve_batch_mixed(bte_ctx* ctx, int b0, int nbb, const bte_opt
         BTE_LAUNCH(KK_INIT, -1, 0, 0,
                    bte::k_bicg_init_scalars<<<(S + 127) / 128, 128, 0, st>>>(bs, ctx->m_skip.as<int>()));
         int i = 1;
-        for (;;) {
+        if (krylov_persistent())
+            BTE_LAUNCH(KK_BICG, -2, 0, N * 25 * w,
+                       bte::k_bicg_persistent<<<S, bte::THREADS, 0, st>>>(op32, v, bs, maxit + 1));
+        for (; !krylov_persistent();) {
             int last = i;
             for (int g = 0; g < kGroup && i <= maxit + 1; ++g, ++i) {
                 BTE_LAUNCH(KK_P, i, 0, N * 6 * w, bte::k_bicg_p<<<grid, bte::THREADS, 0, st>>>(op32, v, bs, i));

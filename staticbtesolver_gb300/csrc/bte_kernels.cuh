@@ -196,15 +196,17 @@ struct CsrOp {
     }
 };
 
-#define BTE_CELL_LOOP(c)                                                     \
-    _Pragma("unroll") for (int _k = 0, c = blockIdx.x * CH + threadIdx.x; _k < CPT; ++_k, c += THREADS)
+#define BTE_CELL_LOOP_K(c, chunk)                                            \
+    _Pragma("unroll") for (int _k = 0, c = (chunk) * CH + threadIdx.x; _k < CPT; ++_k, c += THREADS)
+#define BTE_CELL_LOOP(c) BTE_CELL_LOOP_K(c, blockIdx.x)
 
 // The vector-update kernels load a group of GRP cells' operands into registers
 // before computing and storing any of them, so each thread keeps GRP x (number
 // of operands) loads in flight.
 constexpr int GRP = 4;
-#define BTE_GROUP_LOOP(c0)                                                   \
-    _Pragma("unroll") for (int c0 = blockIdx.x * CH + threadIdx.x; c0 < (int)(blockIdx.x + 1) * CH; c0 += GRP * THREADS)
+#define BTE_GROUP_LOOP_K(c0, chunk)                                          \
+    _Pragma("unroll") for (int c0 = (chunk) * CH + threadIdx.x; c0 < ((chunk) + 1) * CH; c0 += GRP * THREADS)
+#define BTE_GROUP_LOOP(c0) BTE_GROUP_LOOP_K(c0, (int)blockIdx.x)
 
 // FP32 counterpart of FaceFluxOp for the mixed form: per-direction geometry
 // stored in FP32 and pre-scaled by kappa_d = 1 / mean(V Omega_d), so the
@@ -301,11 +303,11 @@ __global__ void k_bicg_init_scalars(BicgState st, const int* skip) {
 // x = q = p = 0, r = b, r_hat = 6.8 b + 0.6; partial r_hat.r for the next rho.
 template <typename Op, typename T>
 __device__ __forceinline__ void bicg_restart_chunk(const Op& op, const BicgVecs<T>& v, const BicgState& st, int y,
-                                                   int par, double (*sm)[NWARP]) {
+                                                   int par, int chunk, double (*sm)[NWARP]) {
     const size_t o = (size_t)y * v.Np;
     T* x = op.x_of(y);
     T acc_t = 0;
-    BTE_CELL_LOOP(c) {
+    BTE_CELL_LOOP_K(c, chunk) {
         // Padded cells get r_hat = 0.6 but keep r = p = q = 0, so they add
         // nothing to any dot product.
         const T bb = v.b[o + c];
@@ -316,17 +318,16 @@ __device__ __forceinline__ void bicg_restart_chunk(const Op& op, const BicgVecs<
     }
     double acc[1] = {(double)acc_t};
     block_sum<1>(acc, sm);
-    if (threadIdx.x == 0) st.P(par ? PK_RWR1 : PK_RWR0, y)[blockIdx.x] = acc[0];
+    if (threadIdx.x == 0) st.P(par ? PK_RWR1 : PK_RWR0, y)[chunk] = acc[0];
 }
 
 // K1 (iteration i): convergence bookkeeping, rho, beta; p = r + beta (p - omega q); ph = M p.
 template <typename Op, typename T>
-__global__ void __launch_bounds__(THREADS) k_bicg_p(Op op, BicgVecs<T> v, BicgState st, int i) {
-    __shared__ double sm[2][NWARP];
-    const int y = blockIdx.y;
+__device__ __forceinline__ void bicg_p_body(const Op& op, const BicgVecs<T>& v, const BicgState& st, int i, int y,
+                                          int chunk, double (*sm)[NWARP]) {
     if (st.done[y]) return;
     const int par = i & 1, pp = par ^ 1;
-    const bool lead = blockIdx.x == 0 && threadIdx.x == 0;
+    const bool lead = chunk == 0 && threadIdx.x == 0;
     double nr;
     bool fresh = false;  // nr is the residual norm of the current x
     if (i > 1 && !(st.flagA[pp * st.S + y] | st.flagB[pp * st.S + y])) {
@@ -349,12 +350,12 @@ __global__ void __launch_bounds__(THREADS) k_bicg_p(Op op, BicgVecs<T> v, BicgSt
         if (lead) st.bestr[par * st.S + y] = best_now;
         if (i > st.maxit * st.cycles || !(nr <= 1.0e300)) {  // limit reached or the iteration blew up
             if (!improved)
-                BTE_CELL_LOOP(c) { xcur[c] = v.xb[ox + c]; }
+                BTE_CELL_LOOP_K(c, chunk) { xcur[c] = v.xb[ox + c]; }
             if (lead) { st.done[y] = 3; st.iters[y] = i - 1; }
             return;
         }
         if (improved)
-            BTE_CELL_LOOP(c) { v.xb[ox + c] = xcur[c]; }
+            BTE_CELL_LOOP_K(c, chunk) { v.xb[ox + c] = xcur[c]; }
     } else if (i > st.maxit) {
         if (lead) { st.done[y] = 3; st.iters[y] = st.maxit; }
         return;
@@ -370,7 +371,7 @@ __global__ void __launch_bounds__(THREADS) k_bicg_p(Op op, BicgVecs<T> v, BicgSt
             st.rho[par * st.S + y] = 1.0; st.alpha[y] = 1.0; st.omega[y] = 1.0;
             st.flagA[par * st.S + y] = 1; st.flagB[par * st.S + y] = 0;
         }
-        bicg_restart_chunk(op, v, st, y, par, sm);
+        bicg_restart_chunk(op, v, st, y, par, chunk, sm);
         return;
     }
     const double beta = (rho_new / st.rho[pp * st.S + y]) * (st.alpha[y] / st.omega[y]);
@@ -387,7 +388,7 @@ __global__ void __launch_bounds__(THREADS) k_bicg_p(Op op, BicgVecs<T> v, BicgSt
     const T* __restrict__ iD = v.invD + o;
     T* __restrict__ p = v.p + o;
     T* __restrict__ ph = v.ph + o;
-    BTE_GROUP_LOOP(c0) {
+    BTE_GROUP_LOOP_K(c0, chunk) {
         T qv[GRP], pv[GRP], rv[GRP], dv[GRP];
 #pragma unroll
         for (int k = 0; k < GRP; ++k) {
@@ -406,11 +407,16 @@ __global__ void __launch_bounds__(THREADS) k_bicg_p(Op op, BicgVecs<T> v, BicgSt
     }
 }
 
+template <typename Op, typename T>
+__global__ void __launch_bounds__(THREADS) k_bicg_p(Op op, BicgVecs<T> v, BicgState st, int i) {
+    __shared__ double sm[2][NWARP];
+    bicg_p_body(op, v, st, i, (int)blockIdx.y, (int)blockIdx.x, sm);
+}
+
 // K2: q = A ph (= A M p); partial r_hat . q
 template <typename Op, typename T>
-__global__ void __launch_bounds__(THREADS) k_bicg_spmv1(Op op, BicgVecs<T> v, BicgState st, int i) {
-    __shared__ double sm[1][NWARP];
-    const int y = blockIdx.y;
+__device__ __forceinline__ void bicg_spmv1_body(const Op& op, const BicgVecs<T>& v, const BicgState& st, int i, int y,
+                                          int chunk, double (*sm)[NWARP]) {
     const int par = i & 1;
     if (st.done[y] | st.flagA[par * st.S + y]) return;
     const size_t o = (size_t)y * v.Np;
@@ -419,31 +425,36 @@ __global__ void __launch_bounds__(THREADS) k_bicg_spmv1(Op op, BicgVecs<T> v, Bi
     const T* __restrict__ rw = v.rw + o;
     T* __restrict__ q = v.q + o;
     T acc_t = 0;
-    BTE_CELL_LOOP(c) {
+    BTE_CELL_LOOP_K(c, chunk) {
         const T qv = op.template apply_pc<T>(y, c, ph, pv);
         q[c] = qv;
         acc_t = fmat(rw[c], qv, acc_t);
     }
     double acc[1] = {(double)acc_t};
     block_sum<1>(acc, sm);
-    if (threadIdx.x == 0) st.P(PK_RWQ, y)[blockIdx.x] = acc[0];
+    if (threadIdx.x == 0) st.P(PK_RWQ, y)[chunk] = acc[0];
+}
+
+template <typename Op, typename T>
+__global__ void __launch_bounds__(THREADS) k_bicg_spmv1(Op op, BicgVecs<T> v, BicgState st, int i) {
+    __shared__ double sm[1][NWARP];
+    bicg_spmv1_body(op, v, st, i, (int)blockIdx.y, (int)blockIdx.x, sm);
 }
 
 // K3: alpha; s = r - alpha q (in place in r); z = M s
 template <typename Op, typename T>
-__global__ void __launch_bounds__(THREADS) k_bicg_s(Op op, BicgVecs<T> v, BicgState st, int i) {
-    __shared__ double sm[1][NWARP];
-    const int y = blockIdx.y;
+__device__ __forceinline__ void bicg_s_body(const Op& op, const BicgVecs<T>& v, const BicgState& st, int i, int y,
+                                          int chunk, double (*sm)[NWARP]) {
     const int par = i & 1;
     if (st.done[y] | st.flagA[par * st.S + y]) return;
-    const bool lead = blockIdx.x == 0 && threadIdx.x == 0;
+    const bool lead = chunk == 0 && threadIdx.x == 0;
     const double temp = sum_parts(st.P(PK_RWQ, y), st.nchunk);
     if (temp < 1e-200 && temp > -1e-200) {
         if (lead) {
             st.rho[par * st.S + y] = 1.0; st.alpha[y] = 1.0; st.omega[y] = 1.0;
             st.flagB[par * st.S + y] = 1;
         }
-        bicg_restart_chunk(op, v, st, y, par, sm);
+        bicg_restart_chunk(op, v, st, y, par, chunk, sm);
         return;
     }
     const double alpha = st.rho[par * st.S + y] / temp;
@@ -454,7 +465,7 @@ __global__ void __launch_bounds__(THREADS) k_bicg_s(Op op, BicgVecs<T> v, BicgSt
     const T* __restrict__ iD = v.invD + o;
     T* __restrict__ r = v.r + o;
     T* __restrict__ z = v.z + o;
-    BTE_GROUP_LOOP(c0) {
+    BTE_GROUP_LOOP_K(c0, chunk) {
         T qv[GRP], rv[GRP], dv[GRP];
 #pragma unroll
         for (int k = 0; k < GRP; ++k) {
@@ -471,11 +482,16 @@ __global__ void __launch_bounds__(THREADS) k_bicg_s(Op op, BicgVecs<T> v, BicgSt
     }
 }
 
+template <typename Op, typename T>
+__global__ void __launch_bounds__(THREADS) k_bicg_s(Op op, BicgVecs<T> v, BicgState st, int i) {
+    __shared__ double sm[1][NWARP];
+    bicg_s_body(op, v, st, i, (int)blockIdx.y, (int)blockIdx.x, sm);
+}
+
 // K4: t = A z (= A M s); partials t.s, t.t
 template <typename Op, typename T>
-__global__ void __launch_bounds__(THREADS) k_bicg_spmv2(Op op, BicgVecs<T> v, BicgState st, int i) {
-    __shared__ double sm[2][NWARP];
-    const int y = blockIdx.y;
+__device__ __forceinline__ void bicg_spmv2_body(const Op& op, const BicgVecs<T>& v, const BicgState& st, int i, int y,
+                                          int chunk, double (*sm)[NWARP]) {
     const int par = i & 1;
     if (st.done[y] | st.flagA[par * st.S + y] | st.flagB[par * st.S + y]) return;
     const size_t o = (size_t)y * v.Np;
@@ -483,7 +499,7 @@ __global__ void __launch_bounds__(THREADS) k_bicg_spmv2(Op op, BicgVecs<T> v, Bi
     const T* __restrict__ sv = v.r + o;  // s, stored in r by K3
     T* __restrict__ t = v.t + o;
     T a0 = 0, a1 = 0;
-    BTE_CELL_LOOP(c) {
+    BTE_CELL_LOOP_K(c, chunk) {
         const T tv = op.template apply_pc<T>(y, c, z, sv);
         t[c] = tv;
         a0 = fmat(tv, sv[c], a0);
@@ -492,19 +508,24 @@ __global__ void __launch_bounds__(THREADS) k_bicg_spmv2(Op op, BicgVecs<T> v, Bi
     double acc[2] = {(double)a0, (double)a1};
     block_sum<2>(acc, sm);
     if (threadIdx.x == 0) {
-        st.P(PK_TS, y)[blockIdx.x] = acc[0];
-        st.P(PK_TT, y)[blockIdx.x] = acc[1];
+        st.P(PK_TS, y)[chunk] = acc[0];
+        st.P(PK_TT, y)[chunk] = acc[1];
     }
+}
+
+template <typename Op, typename T>
+__global__ void __launch_bounds__(THREADS) k_bicg_spmv2(Op op, BicgVecs<T> v, BicgState st, int i) {
+    __shared__ double sm[2][NWARP];
+    bicg_spmv2_body(op, v, st, i, (int)blockIdx.y, (int)blockIdx.x, sm);
 }
 
 // K5: omega; x += alpha ph; x += omega z; r = s - omega t; partials r.r, r_hat.r
 template <typename Op, typename T>
-__global__ void __launch_bounds__(THREADS) k_bicg_x(Op op, BicgVecs<T> v, BicgState st, int i) {
-    __shared__ double sm[2][NWARP];
-    const int y = blockIdx.y;
+__device__ __forceinline__ void bicg_x_body(const Op& op, const BicgVecs<T>& v, const BicgState& st, int i, int y,
+                                          int chunk, double (*sm)[NWARP]) {
     const int par = i & 1;
     if (st.done[y] | st.flagA[par * st.S + y] | st.flagB[par * st.S + y]) return;
-    const bool lead = blockIdx.x == 0 && threadIdx.x == 0;
+    const bool lead = chunk == 0 && threadIdx.x == 0;
     // t.t == 0 means s == 0: the half step already solved the system.  The
     // reference would divide 0 by 0 here (src/bicgstab.hpp:280); omega = 0
     // keeps x += alpha ph, r = s = 0, and the next p-update retires the system.
@@ -521,7 +542,7 @@ __global__ void __launch_bounds__(THREADS) k_bicg_x(Op op, BicgVecs<T> v, BicgSt
     const T* __restrict__ rw = v.rw + o;
     T* __restrict__ r = v.r + o;
     T a0 = 0, a1 = 0;
-    BTE_GROUP_LOOP(c0) {
+    BTE_GROUP_LOOP_K(c0, chunk) {
         T xv[GRP], phv[GRP], zv[GRP], tv[GRP], rv[GRP], wv[GRP];
 #pragma unroll
         for (int k = 0; k < GRP; ++k) {
@@ -543,8 +564,52 @@ __global__ void __launch_bounds__(THREADS) k_bicg_x(Op op, BicgVecs<T> v, BicgSt
     double acc[2] = {(double)a0, (double)a1};
     block_sum<2>(acc, sm);
     if (threadIdx.x == 0) {
-        st.P(par ? PK_RR1 : PK_RR0, y)[blockIdx.x] = acc[0];
-        st.P(par ? PK_RWR1 : PK_RWR0, y)[blockIdx.x] = acc[1];
+        st.P(par ? PK_RR1 : PK_RR0, y)[chunk] = acc[0];
+        st.P(par ? PK_RWR1 : PK_RWR0, y)[chunk] = acc[1];
+    }
+}
+
+template <typename Op, typename T>
+__global__ void __launch_bounds__(THREADS) k_bicg_x(Op op, BicgVecs<T> v, BicgState st, int i) {
+    __shared__ double sm[2][NWARP];
+    bicg_x_body(op, v, st, i, (int)blockIdx.y, (int)blockIdx.x, sm);
+}
+
+// Whole BiCGSTAB solves in one launch, one block per system of the batch
+// (blockIdx.x = y): the phase bodies above run chunk by chunk, with a block
+// barrier after each chunk, so a decision the lead thread records in one chunk
+// (converged, restarted, limit reached) is seen by every thread of the block
+// in the next.  Each chunk then computes exactly what the phase kernels'
+// block for that chunk computes -- none of them depends on another block of
+// the same launch -- so x is the same to the bit.  No host round trip between
+// iterations, a converged system's block just ends.  i_last = the iteration
+// limit + 1 (the p-update of that iteration retires what is left).
+template <typename Op, typename T>
+__global__ void __launch_bounds__(THREADS) k_bicg_persistent(Op op, BicgVecs<T> v, BicgState st, int i_last) {
+    __shared__ double sm[2][NWARP];
+    const int y = blockIdx.x;
+    for (int i = 1; i <= i_last; ++i) {
+        for (int k = 0; k < st.nchunk; ++k) {
+            bicg_p_body(op, v, st, i, y, k, sm);
+            __syncthreads();
+        }
+        if (*(volatile const int*)(st.done + y) || i >= i_last) break;
+        for (int k = 0; k < st.nchunk; ++k) {
+            bicg_spmv1_body(op, v, st, i, y, k, sm);
+            __syncthreads();
+        }
+        for (int k = 0; k < st.nchunk; ++k) {
+            bicg_s_body(op, v, st, i, y, k, sm);
+            __syncthreads();
+        }
+        for (int k = 0; k < st.nchunk; ++k) {
+            bicg_spmv2_body(op, v, st, i, y, k, sm);
+            __syncthreads();
+        }
+        for (int k = 0; k < st.nchunk; ++k) {
+            bicg_x_body(op, v, st, i, y, k, sm);
+            __syncthreads();
+        }
     }
 }
 

@@ -240,6 +240,7 @@ struct DsaCoarse {
     int nblk = 0, per_block = 0, chunk = 0, seg = 0, n_agg = 0;
     std::vector<double> ac;    // [n_agg][n_agg] coarse operator (identity rows for empty aggregates); its
                                // inverse is formed on the device (k_gj_step)
+    std::vector<int> agg;      // [n] agg_of(c), filled without divisions
     std::vector<int> need_ptr; // [nblk+1] aggregates a block's cells and their neighbours belong to
     std::vector<int> need;
     int agg_of(int c) const { const int k = c / chunk; return k * per_block + (c - k * chunk) / seg; }
@@ -255,17 +256,25 @@ inline void dsa_coarse(int n, int F, const int* nb /* [F][n] */, const double* w
     out.chunk = (n + nblk - 1) / nblk;
     out.seg = (out.chunk + per_block - 1) / per_block;
     const int m = out.n_agg = nblk * per_block;
+    std::vector<int>& agg = out.agg;
+    agg.assign(n, 0);
+    for (int k = 0; k < nblk; ++k)
+        for (int a = 0; a < per_block; ++a) {
+            const int lo = k * out.chunk + a * out.seg;
+            const int hi = std::min(std::min(n, (k + 1) * out.chunk), lo + out.seg);
+            for (int c = lo; c < hi; ++c) agg[c] = k * per_block + a;
+        }
     std::vector<double>& Ac = out.ac;
     Ac.assign((size_t)m * m, 0.0);
     std::vector<int> size(m, 0);
     for (int c = 0; c < n; ++c) {
-        const int J = out.agg_of(c);
+        const int J = agg[c];
         ++size[J];
         Ac[(size_t)J * m + J] += 1.0;
         for (int f = 0; f < F; ++f) {
             const int o = nb[(size_t)f * n + c];
             if (o < 0) continue;
-            Ac[(size_t)J * m + out.agg_of(o)] -= w[(size_t)f * n + c];
+            Ac[(size_t)J * m + agg[o]] -= w[(size_t)f * n + c];
         }
     }
     for (int J = 0; J < m; ++J)
@@ -277,12 +286,12 @@ inline void dsa_coarse(int n, int F, const int* nb /* [F][n] */, const double* w
         const int lo = k * out.chunk, hi = std::min(n, lo + out.chunk);
         std::vector<int> list;
         for (int c = lo; c < hi; ++c) {
-            const int J = out.agg_of(c);
+            const int J = agg[c];
             if (seen[J] != k) { seen[J] = k; list.push_back(J); }
             for (int f = 0; f < F; ++f) {
                 const int o = nb[(size_t)f * n + c];
                 if (o < 0) continue;
-                const int K = out.agg_of(o);
+                const int K = agg[o];
                 if (seen[K] != k) { seen[K] = k; list.push_back(K); }
             }
         }

@@ -58,3 +58,33 @@ def test_csr_maxit_reports_unconverged(sbte, oracle_mod, get_case):
     rp, ci, v, b = o.assemble(0, 3, e_prev, np.ones((o.n_cell, o.n_band)))
     x, it, conv = sbte.bicgstab_csr(rp, ci, v, b, maxit=1, tol=1e-14)
     assert not conv and it == 1
+
+
+@pytest.mark.parametrize("name,form_name,kw", [("square16_b8", "FORM_PLAIN", {}), ("square16_b8", "FORM_MIXED", {}),
+                                               ("3DM2DG", "FORM_PLAIN", {}), ("cube4_b2", "FORM_MIXED", {}),
+                                               ("square10_b40", "FORM_PLAIN", {"plain_cycles": 3, "inner_maxit": 40})])
+def test_persistent_bicgstab_matches_phase_kernels(sbte, get_case, monkeypatch, name, form_name, kw):
+    """The Krylov forms' BiCGSTAB as one persistent launch per batch
+    (BTE_KRYLOV=persistent: one block per system, the phase bodies chunk by
+    chunk) and as one launch per phase (the default: the host checking every 8
+    iterations) give the same x to the bit: the same temperatures, margins and
+    inner iteration counts, in FP64 (PLAIN, also with the best-iterate limit of
+    plain_cycles) and FP32 (MIXED)."""
+    c = get_case(name)
+    runs = {}
+    for mode in ("persistent", "phase"):
+        if mode == "persistent":
+            monkeypatch.setenv("BTE_KRYLOV", "persistent")
+        else:
+            monkeypatch.delenv("BTE_KRYLOV", raising=False)
+        ctx = sbte.Context(0).load(sbte.Problem(*c.args()))
+        st, rep = ctx.solve(max_iter=c.max_iter, tol=1e-5, form=getattr(sbte, form_name), profile=True, **kw)
+        runs[mode] = (st, ctx.temperature(), ctx.margins(), rep.as_dict(), ctx.kernel_stats())
+        ctx.close()
+    (s0, T0, m0, r0, k0), (s1, T1, m1, r1, k1) = runs["persistent"], runs["phase"]
+    assert s0 == s1
+    assert k0["bicg_persistent"]["launches"] > 0 and k0["bicg_p_update"]["launches"] == 0
+    assert k1["bicg_persistent"]["launches"] == 0 and k1["bicg_p_update"]["launches"] > 0
+    assert r0["inner_iterations"] == r1["inner_iterations"] and r0["inner_unconverged"] == r1["inner_unconverged"]
+    assert np.array_equal(T0, T1)
+    assert np.array_equal(m0, m1)

@@ -931,22 +931,47 @@ __global__ void __launch_bounds__(1024) k_level_order(const uint8_t* __restrict_
         // bitonic sort of the wave, padded to a power of two (<= cap) with INT_MAX
         int P = 1;
         while (P < m) P <<= 1;
-        for (int i = m + threadIdx.x; i < P; i += blockDim.x) a[i] = INT_MAX;
-        __syncthreads();
-        for (int k = 2; k <= P; k <<= 1)
-            for (int j = k >> 1; j > 0; j >>= 1) {
-                for (int i = threadIdx.x; i < P; i += blockDim.x) {
-                    const int l = i ^ j;
-                    if (l > i) {
-                        const int x = a[i], y = a[l];
-                        if ((x > y) == ((i & k) == 0)) {
-                            a[i] = y;
-                            a[l] = x;
+        if (P <= (int)blockDim.x) {
+            // one element per thread: compare-exchange partners closer than a
+            // warp through shuffles, the others through shared memory
+            const int i = threadIdx.x;
+            int x = i < m ? a[i] : INT_MAX;
+            for (int k = 2; k <= P; k <<= 1)
+                for (int j = k >> 1; j > 0; j >>= 1) {
+                    int y;
+                    if (j >= 32) {
+                        __syncthreads();
+                        if (i < P) a[i] = x;
+                        __syncthreads();
+                        y = i < P ? a[i ^ j] : INT_MAX;
+                    } else {
+                        y = __shfl_xor_sync(0xffffffffu, x, j);
+                    }
+                    const bool lower = (i & j) == 0, up = (i & k) == 0;
+                    // keep the smaller of the pair in the lower slot of an ascending run
+                    if (i < P) x = (lower == up) ? min(x, y) : max(x, y);
+                }
+            __syncthreads();
+            if (i < P) a[i] = x;
+            __syncthreads();
+        } else {
+            for (int i = m + threadIdx.x; i < P; i += blockDim.x) a[i] = INT_MAX;
+            __syncthreads();
+            for (int k = 2; k <= P; k <<= 1)
+                for (int j = k >> 1; j > 0; j >>= 1) {
+                    for (int i = threadIdx.x; i < P; i += blockDim.x) {
+                        const int l = i ^ j;
+                        if (l > i) {
+                            const int x = a[i], y = a[l];
+                            if ((x > y) == ((i & k) == 0)) {
+                                a[i] = y;
+                                a[l] = x;
+                            }
                         }
                     }
+                    __syncthreads();
                 }
-                __syncthreads();
-            }
+        }
         for (int i = threadIdx.x; i < m; i += blockDim.x) pd[pos + i] = a[i];
         if (threadIdx.x == 0) {
             ld[level] = pos;

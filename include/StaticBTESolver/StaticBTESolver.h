@@ -42,6 +42,9 @@ public:
     // 3 Anderson; every: interval or depth).  Learned needs setMlp first.
     void setAccel(int accel, int every);
     void setMlp(const std::vector<float>& params);  // bte_mlp_param_count() values
+    // diffusion-synthetic correction after each outer iteration (bte_options.dsa;
+    // tol/maxit of its low-order solve, 0 = defaults 1e-3 / 4000)
+    void setDsa(bool on, double tol = 0, int maxit = 0);
     void setTolerance(double margin_tol);   // outer stop (reference: 1e-5)
     void setInnerTolerance(double tol);     // inner relative residual (reference: 1e-9)
     void setVerbose(bool verbose);          // print the reference's stdout lines (default true)
@@ -65,6 +68,9 @@ private:
     double T_ref_ = 300;
     int form_ = 0;
     int accel_ = 0, accel_every_ = 8;
+    bool dsa_ = false;
+    double dsa_tol_ = 0;
+    int dsa_maxit_ = 0;
     std::vector<float> mlp_;
     double tol_ = 1e-5, inner_tol_ = 1e-9;
     bool verbose_ = true;

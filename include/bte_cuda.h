@@ -125,7 +125,8 @@ typedef struct bte_report {
     double ms_dsa;             /* device time of the corrections (included in ms_reduce and ms_total) */
     int sweep_kernel;          /* sweep form: the kernel the autotuner chose -- 0 level-synchronous (k_sweep),
                                   1 staged (levels copied to shared memory ahead by bulk copies, right-hand
-                                  side from a level-ordered pre-pass) */
+                                  side from a level-ordered pre-pass), 2 level-synchronous over levels
+                                  split into slices of one position per thread */
     double ms_host_setup;      /* host wall time of this call's set-up after new inputs (uploads, geometry) */
     double ms_host_plan;       /* ... of building the sweep plan (level order, layout) after new geometry */
     double ms_host_order;      /*     of which the level order (host threads over directions) */
@@ -261,10 +262,10 @@ bte_status bte_get_kernel_stats(bte_ctx* ctx, bte_kernel_stat* stats, int cap, i
 /* The sweep autotuner's table from the first sweep of the current plan (empty
  * when the choice came from the per-process cache): candidate k ran with
  * group[k] bands and threads[k] threads per block and ring[k] positions per
- * band, with kernel[k] (0 level-synchronous, 1 staged, as
+ * band, with kernel[k] (0 level-synchronous, 1 staged, 2 split levels, as
  * bte_report.sweep_kernel), in ms[k] milliseconds.  Entries are written up
  * to cap (arrays may be NULL when cap is 0); *n = candidates timed.  The
- * environment variable BTE_SWEEP_KERNEL=level|staged restricts the
+ * environment variable BTE_SWEEP_KERNEL=level|staged|split restricts the
  * candidates to one kernel (the temperatures are the same to the bit either
  * way). */
 bte_status bte_get_sweep_tuning(bte_ctx* ctx, int* group, int* threads, int* ring, int* kernel, float* ms, int cap,

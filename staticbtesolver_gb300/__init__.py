@@ -355,8 +355,8 @@ class Context:
 
     def sweep_tuning(self):
         """The sweep autotuner's candidates on this context's plan, as dicts
-        (bands and threads per block, ring positions per band, kernel "level"
-        or "staged", milliseconds); empty when the shape came from the
+        (bands and threads per block, ring positions per band, kernel "level",
+        "staged" or "split", milliseconds); empty when the shape came from the
         per-process cache."""
         n = C.c_int(0)
         self._check(_cuda.bte_get_sweep_tuning(self._h, None, None, None, None, None, 0, C.byref(n)))
@@ -365,7 +365,7 @@ class Context:
         self._check(_cuda.bte_get_sweep_tuning(self._h, *[c.ctypes.data_as(C.c_void_p) for c in cols], m,
                                                C.byref(n)))
         return [dict(group=int(cols[0][k]), threads=int(cols[1][k]), ring=int(cols[2][k]),
-                     kernel=("level", "staged")[int(cols[3][k])], ms=float(cols[4][k])) for k in range(m)]
+                     kernel=("level", "staged", "split")[int(cols[3][k])], ms=float(cols[4][k])) for k in range(m)]
 
     def level_order(self, d):
         """The sweep plan's level order of direction d: (cells in order, level starts then n)."""

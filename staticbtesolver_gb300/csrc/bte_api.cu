@@ -79,8 +79,9 @@ struct SweepShape {
     size_t smem = 0;
     bool margin = false;  // acyclic plans: the sweep sums the margin partials (else k_reduce does)
     bool staged = false;  // k_sweep_staged (right-hand side from k_sweep_src, levels staged by bulk copies)
-    int cap = 0;          // staged: positions per stage
-    int kind() const { return staged ? 1 : 0; }
+    bool split = false;   // k_sweep over the levels split into slices of cap positions (one per thread)
+    int cap = 0;          // staged, split: positions per stage
+    int kind() const { return staged ? 1 : split ? 2 : 0; }
     bool prepass() const { return staged; }  // needs k_sweep_src's right-hand side
 };
 
@@ -150,7 +151,7 @@ struct bte_ctx {
     // error flag of its bounded waits, stage lists by width; row length n2
     DevBuf p_rec, d_ssrc, d_sweep_err;
     // level-order work: inflow masks, order, positions, level starts, in-degrees, counts
-    DevBuf lo_mask, lo_perm, lo_pos, lo_lvl, lo_indeg, lo_small;
+    DevBuf lo_mask, lo_perm, lo_pos, lo_lvl, lo_indeg, lo_small, lo_down;
     int plan_host_dirs = 0;  // directions the last plan ordered on the host
     std::vector<int> plan_lvl, plan_lvl_off;  // host copies of the level starts
     std::map<int, std::unique_ptr<StageList>> stage_lists;
@@ -727,8 +728,9 @@ struct DsaHostPlan {
     bte::DsaCoarse co;
 };
 
-// pre_order / pre_cm (optional): a locality order already computed for the
-// coupling pattern pre_cm ([n][F]); used when the pattern of W is the same.
+// pre_order (optional): a locality order already computed, used as it is
+// without pre_cm, and with pre_cm (the coupling pattern it was computed for,
+// [n][F]) only when the pattern of W is the same.
 static void dsa_host_plan(int n, int F, const int* nb, const double* W, int nblk, DsaHostPlan& hp,
                           std::vector<int>* pre_order = nullptr, const std::vector<int>* pre_cm = nullptr) {
     HostTimer tm("dsa_host_plan");
@@ -745,7 +747,7 @@ static void dsa_host_plan(int n, int F, const int* nb, const double* W, int nblk
         for (int c = 0; c < n; ++c) cm[(size_t)c * F + f] = W[(size_t)f * n + c] > 0.0 ? nb[(size_t)f * n + c] : -1;
     const int agg_cells = std::max(1, n / (nblk * bte::dsa::AGG));
     tm.lap("scaling");
-    if (pre_order && pre_cm && *pre_cm == cm) hp.order.swap(*pre_order);
+    if (pre_order && pre_order->size() == (size_t)n && (!pre_cm || *pre_cm == cm)) hp.order.swap(*pre_order);
     else bte::locality_order(n, F, cm.data(), std::max(8, agg_cells / 2), hp.order);
     tm.lap("locality order");
     const std::vector<int>& order = hp.order;
@@ -815,12 +817,31 @@ static bte_status dsa_upload(bte_ctx* ctx, DsaHostPlan& hp, cudaStream_t st) {
         BTE_CUDA(cudaMemsetAsync(gbad.p, 0, sizeof(int) * 2, st));
         double* a = ga.as<double>();
         double* b = gb.as<double>();
-        // one cooperative launch (one block per SM) when every block fits, else one launch per step
-        int coop_ok = 0, occ_gj = 0, sms_gj = 0;
+        // one cooperative launch (one block per SM) when every block fits:
+        // kGjBlock pivots per step when the pivot rows fit in shared memory,
+        // else one pivot per step; without cooperative launches, one launch per step
+        int coop_ok = 0, occ_gj = 0, sms_gj = 0, occ_blk = 0, smem_opt = 0;
         BTE_CUDA(cudaDeviceGetAttribute(&coop_ok, cudaDevAttrCooperativeLaunch, ctx->device));
         BTE_CUDA(cudaDeviceGetAttribute(&sms_gj, cudaDevAttrMultiProcessorCount, ctx->device));
+        BTE_CUDA(cudaDeviceGetAttribute(&smem_opt, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device));
         BTE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_gj, bte::dsa::k_gj_all, 1024, 0));
-        if (coop_ok && occ_gj >= 1) {
+        const int kgb = bte::dsa::kGjBlock;
+        const size_t smem_blk = sizeof(double) * (size_t)kgb * (m + kgb + 1);
+        if (coop_ok && smem_blk + 1024 <= (size_t)smem_opt) {
+            BTE_CUDA(cudaFuncSetAttribute(bte::dsa::k_gj_block_all, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)smem_blk));
+            BTE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_blk, bte::dsa::k_gj_block_all, 1024, smem_blk));
+        }
+        if (occ_blk >= 1) {
+            const int nb = std::min(sms_gj, m);
+            int* badp = gbad.as<int>();
+            unsigned* barp = reinterpret_cast<unsigned*>(badp + 1);
+            int mm = m;
+            void* args[] = {&a, &b, &mm, &barp, &badp};
+            BTE_CUDA(cudaLaunchCooperativeKernel((const void*)bte::dsa::k_gj_block_all, dim3(nb), dim3(1024), args,
+                                                 smem_blk, st));
+            if (((m + kgb - 1) / kgb) % 2) std::swap(a, b);  // the inverse is in A after an even number of steps
+        } else if (coop_ok && occ_gj >= 1) {
             const int nb = std::min(sms_gj, m);
             int* badp = gbad.as<int>();
             unsigned* barp = reinterpret_cast<unsigned*>(badp + 1);
@@ -951,24 +972,31 @@ static void setup_dsa_host(const bte_ctx* ctx, int nblk, DsaSetupHost& out) {
         fixed[cf] = row < 0 || ctx->bc_type[row] == 1;
     }
     HostTimer tm("setup_dsa_host");
-    // the locality order needs only the coupling pattern, which the topology
-    // gives (an interior face with positive area that both cells name); it
-    // runs on a second thread while the coefficients are computed, and is
-    // used if the coefficients' own pattern is the same (it always is unless
-    // a coefficient is zero)
-    std::vector<int> cm_topo((size_t)n * F, -1), pre_order;
-    for (int c = 0; c < n; ++c)
-        for (int f = 0; f < F; ++f) {
-            const size_t cf = (size_t)c * F + f;
-            const int o = ctx->nbr[cf];
-            if (o < 0 || o >= n || !(ctx->area[cf] > 0.0)) continue;
-            bool back = false;
-            for (int g = 0; g < F; ++g) back |= ctx->nbr[(size_t)o * F + g] == c;
-            if (back) cm_topo[cf] = o;
-        }
+    // The locality order runs on a second thread while the coefficients are
+    // computed.  With the centroids (bte_set_centroids) it is the Hilbert
+    // curve through them.  Without, it is the bisection of the coupling
+    // pattern, which the topology gives (an interior face with positive area
+    // that both cells name); that order is used if the coefficients' own
+    // pattern is the same (it always is unless a coefficient is zero).
+    const bool by_curve = ctx->centroid.size() == (size_t)3 * n;
+    std::vector<int> cm_topo, pre_order;
+    if (!by_curve) {
+        cm_topo.assign((size_t)n * F, -1);
+        for (int c = 0; c < n; ++c)
+            for (int f = 0; f < F; ++f) {
+                const size_t cf = (size_t)c * F + f;
+                const int o = ctx->nbr[cf];
+                if (o < 0 || o >= n || !(ctx->area[cf] > 0.0)) continue;
+                bool back = false;
+                for (int g = 0; g < F; ++g) back |= ctx->nbr[(size_t)o * F + g] == c;
+                if (back) cm_topo[cf] = o;
+            }
+    }
     const int agg_cells = std::max(1, n / (nblk * bte::dsa::AGG));
-    std::thread order_thread(
-        [&] { bte::locality_order(n, F, cm_topo.data(), std::max(8, agg_cells / 2), pre_order); });
+    std::thread order_thread([&] {
+        if (by_curve) bte::hilbert_order(ctx->dim, n, ctx->centroid.data(), pre_order);
+        else bte::locality_order(n, F, cm_topo.data(), std::max(8, agg_cells / 2), pre_order);
+    });
     bte::DsaCoefficients co;
     bte::dsa_coefficients(ctx->dim, n, F, ctx->nbr.data(), ctx->area.data(), ctx->normal.data(), ctx->volume.data(),
                           ctx->n_dir, ctx->s.data(), ctx->S.data(), ctx->solid_angle, ctx->n_band, ctx->vg.data(),
@@ -977,7 +1005,8 @@ static void setup_dsa_host(const bte_ctx* ctx, int nblk, DsaSetupHost& out) {
     order_thread.join();
     tm.lap("locality order (joined)");
     out.n_dirichlet = co.n_dirichlet;
-    if (co.n_dirichlet > 0) dsa_host_plan(n, F, co.nb.data(), co.W.data(), nblk, out.hp, &pre_order, &cm_topo);
+    if (co.n_dirichlet > 0)
+        dsa_host_plan(n, F, co.nb.data(), co.W.data(), nblk, out.hp, &pre_order, by_curve ? nullptr : &cm_topo);
 }
 
 // ... and the device part.
@@ -997,11 +1026,16 @@ static int sweep_slots(const bte_ctx* ctx) { return std::max(2, std::min(ctx->pl
 
 // Build the sweep plan for every direction from the device's inflow coefficients.
 // BTE_LEVEL_ORDER=host builds every direction's level order on the host
-// (sweep_order.h) instead of on the device (k_level_order); the order is the
-// same either way.
+// (sweep_order.h) instead of on the device (k_level_order), and
+// BTE_LEVEL_ORDER=global keeps the device's in-degrees in global memory even
+// when they fit in shared memory; the order is the same either way.
 static bool level_order_on_host() {
     const char* v = std::getenv("BTE_LEVEL_ORDER");
     return v && v[0] == 'h';
+}
+static bool level_order_global() {
+    const char* v = std::getenv("BTE_LEVEL_ORDER");
+    return v && v[0] == 'g';
 }
 
 static bte_status build_sweep_plan(bte_ctx* ctx) {
@@ -1022,19 +1056,35 @@ static bte_status build_sweep_plan(bte_ctx* ctx) {
     BTE_CUDA(ctx->lo_small.alloc(sizeof(int) * (2 * (size_t)ND + 1)));
     std::vector<int> small(2 * (size_t)ND + 1, 1);  // nlev[ND], status[ND], fmax
     int* d_small = ctx->lo_small.as<int>();
-    const bool host_all = level_order_on_host();
+    // the device order packs a cell index and an edge count into one int
+    const bool host_all = level_order_on_host() || F > 4 || n >= (1 << 28);
     if (!host_all) {
-        BTE_CUDA(ctx->lo_indeg.alloc(sizeof(int) * (size_t)ND * n));
+        BTE_CUDA(ctx->lo_down.alloc(sizeof(int) * (size_t)ND * n * F));
+        const size_t nf = (size_t)n * F;
+        bte::k_downstream<<<dim3((unsigned)((nf + 255) / 256), ND), 256, 0, st>>>(
+            ctx->lo_mask.as<uint8_t>(), ctx->d_nbr.as<int>(), n, F, ctx->lo_down.as<int>());
+        BTE_LAUNCHED();
         int smem_max = 0;
         BTE_CUDA(cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device));
-        int cap = 1;  // frontier capacity: a power of two, two frontiers in at most 128 KB
-        while (cap < n && (size_t)cap * 2 * 2 * sizeof(int) <= std::min<size_t>(128 * 1024, smem_max - 1024)) cap *= 2;
-        const size_t smem = (size_t)2 * cap * sizeof(int);
-        BTE_CUDA(cudaFuncSetAttribute(bte::k_level_order, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        // frontier capacity: a power of two, two frontiers in at most 128 KB,
+        // next to the in-degree bytes when those fit with room for waves of 4,096
+        const size_t budget = (size_t)smem_max - 1024, deg_bytes = sizeof(int) * (((size_t)n + 3) / 4);
+        auto cap_for = [&](size_t room) {
+            int cap = 1;
+            while (cap < n && (size_t)cap * 2 * 2 * sizeof(int) <= std::min<size_t>(128 * 1024, room)) cap *= 2;
+            return cap;
+        };
+        const bool sdeg =
+            !level_order_global() && deg_bytes < budget && cap_for(budget - deg_bytes) >= std::min(n, 4096);
+        const int cap = sdeg ? cap_for(budget - deg_bytes) : cap_for(budget);
+        const size_t smem = (size_t)2 * cap * sizeof(int) + (sdeg ? deg_bytes : 0);
+        auto kern = sdeg ? bte::k_level_order<true> : bte::k_level_order<false>;
+        if (!sdeg) BTE_CUDA(ctx->lo_indeg.alloc(sizeof(int) * (size_t)ND * n));
+        BTE_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         BTE_CUDA(cudaMemsetAsync(d_small + 2 * ND, 0, sizeof(int), st));
-        bte::k_level_order<<<ND, 1024, smem, st>>>(ctx->lo_mask.as<uint8_t>(), ctx->d_nbr.as<int>(), n, F, cap,
-                                                   ctx->lo_indeg.as<int>(), ctx->lo_perm.as<int>(),
-                                                   ctx->lo_lvl.as<int>(), d_small, d_small + ND, d_small + 2 * ND);
+        kern<<<ND, 1024, smem, st>>>(ctx->lo_mask.as<uint8_t>(), ctx->lo_down.as<int>(), n, F, cap,
+                                     sdeg ? nullptr : ctx->lo_indeg.as<int>(), ctx->lo_perm.as<int>(),
+                                     ctx->lo_lvl.as<int>(), d_small, d_small + ND, d_small + 2 * ND);
         BTE_LAUNCHED();
         BTE_CUDA(cudaMemcpyAsync(small.data(), d_small, sizeof(int) * small.size(), cudaMemcpyDeviceToHost, st));
         BTE_CUDA(cudaStreamSynchronize(st));
@@ -1425,12 +1475,13 @@ static int sweep_margin_restriction() {
     if (!v || !*v) return -1;
     return v[0] == '0' ? 0 : v[0] == '1' ? 1 : -1;
 }
-// BTE_SWEEP_KERNEL=level (k_sweep) or staged (k_sweep_staged) restricts the
+// BTE_SWEEP_KERNEL=level (k_sweep), split (k_sweep over levels split into
+// slices of one position per thread) or staged (k_sweep_staged) restricts the
 // autotuner to one sweep kernel (x is the same to the bit either way).
 static int sweep_kernel_restriction() {
     const char* v = std::getenv("BTE_SWEEP_KERNEL");
     if (!v || !*v) return -1;
-    return v[0] == 'l' ? 0 : v[0] == 's' ? 1 : -1;
+    return v[0] == 'l' ? 0 : v[0] == 's' && v[1] == 't' ? 1 : v[0] == 's' && v[1] == 'p' ? 2 : -1;
 }
 // BTE_SWEEP_SHAPE=G,T restricts the autotuner to G bands and T threads per
 // block (a test of a particular shape, e.g. stages narrower than a level);
@@ -1460,32 +1511,45 @@ static size_t staged_smem(int fm, int cap, int G, int W) {
 }
 
 // Candidates of the autotuner for batches of nbb bands: k_sweep (bands per
-// block, threads; at most 128 threads) and k_sweep_staged (at most 256
-// threads; two rounds of the block's positions per stage, a ring of 2048 / G
-// positions per band).
+// block, threads; at most 128 threads) over the levels as they are and over
+// the levels split into slices of one position per thread (a thread's items
+// are then all loaded a level ahead; a wider level costs one more barrier per
+// slice instead), and k_sweep_staged (at most 256 threads; two rounds of the
+// block's positions per stage, a ring of 2048 / G positions per band).
 static std::vector<SweepShape> sweep_candidates(const bte_ctx* ctx, int nbb, int only_kernel, int only_margin,
                                                 int only_shape) {
     static const int cand[][2] = {{1, 64}, {1, 128}, {2, 64}, {2, 128}, {4, 64}, {4, 128}, {8, 128}, {16, 128}};
     static const int staged[][2] = {{1, 128}, {1, 256}, {2, 128}, {2, 256}, {4, 64},
                                     {4, 128}, {4, 256}, {8, 256}};
     std::vector<SweepShape> out;
-    for (const auto& c : cand) {
-        if (only_kernel == 1) break;
-        if (only_shape >= 0 && only_shape != c[0] * 10000 + c[1]) continue;
-        SweepShape sh;
-        sh.G = std::max(1, std::min(c[0], nbb));
-        sh.threads = c[1];
-        sh.W = sweep_ring(sh.G);
-        sh.smem = sizeof(double) * (size_t)sh.G * sh.W;
-        bool dup = false;
-        for (const SweepShape& o : out) dup |= !o.staged && o.G == sh.G && o.threads == sh.threads;
-        if (!dup) out.push_back(sh);
-    }
+    for (int split = 0; split < 2; ++split)
+        for (const auto& c : cand) {
+            if (only_kernel == 1 || only_kernel == (split ? 0 : 2)) break;
+            if (only_shape >= 0 && only_shape != c[0] * 10000 + c[1]) continue;
+            // split levels only in the 128-thread shapes of up to 4 bands (the
+            // others were never faster unsplit)
+            if (split && only_shape < 0 && (c[1] != 128 || c[0] > 4)) continue;
+            SweepShape sh;
+            sh.G = std::max(1, std::min(c[0], nbb));
+            sh.threads = c[1];
+            sh.W = sweep_ring(sh.G);
+            sh.smem = sizeof(double) * (size_t)sh.G * sh.W;
+            if (split) {
+                int gp = 1;
+                while (gp < sh.G) gp <<= 1;
+                sh.split = true;
+                sh.cap = sh.threads / gp;
+            }
+            bool dup = false;
+            for (const SweepShape& o : out)
+                dup |= !o.staged && o.split == sh.split && o.G == sh.G && o.threads == sh.threads;
+            if (!dup) out.push_back(sh);
+        }
     int smem_max = 0;
     cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device);
     for (const auto& c : staged) {
         // the staged kernel leaves the margin to k_reduce
-        if (only_kernel == 0 || only_margin == 1) break;
+        if ((only_kernel >= 0 && only_kernel != 1) || only_margin == 1) break;
         if (only_shape >= 0 && only_shape != c[0] * 10000 + c[1]) continue;
         SweepShape sh;
         sh.staged = true;
@@ -1549,8 +1613,14 @@ static void launch_sweep(const bte_ctx* ctx, const SweepShape& sh, int nbb, int 
 #undef BTE_STAGED_FM
         return;
     }
-#define BTE_SWEEP_FM(FM)                                                                                         \
-    bte::k_sweep<MARGIN, FM><<<grid, sh.threads, sh.smem, st>>>(sp, voi, kinv, src, ctx->e_curr, first_sweep, sh.G, \
+    bte::SweepPlan spl = sp;
+    if (sh.split) {  // the same kernel over the levels split into slices of cap positions
+        const StageList* sl = ctx->stage_lists.find(sh.cap)->second.get();
+        spl.lvl = sl->stages.as<int>();
+        spl.lvl_off = sl->off.as<int>();
+    }
+#define BTE_SWEEP_FM(FM)                                                                                          \
+    bte::k_sweep<MARGIN, FM><<<grid, sh.threads, sh.smem, st>>>(spl, voi, kinv, src, ctx->e_curr, first_sweep, sh.G, \
                                                                 sh.W, nbb, b0, ctx->n_band, ctx->n_dir, ctx->Np, mpart)
     if (fm == 2) BTE_SWEEP_FM(2);
     else if (fm == 3) BTE_SWEEP_FM(3);
@@ -1620,7 +1690,7 @@ static bte_status solve_batch_sweep(bte_ctx* ctx, int b0, int nbb, const bte_opt
         BTE_CUDA(cudaEventCreate(&e1));
         float best = 1e30f;
         for (size_t k = 0; k < cand.size(); ++k) {
-            if (cand[k].staged) {
+            if (cand[k].staged || cand[k].split) {
                 const StageList* sl = nullptr;
                 bte_status s2 = stage_list(ctx, cand[k].cap, &sl);
                 if (s2 != BTE_OK) return s2;
@@ -1690,7 +1760,7 @@ static bte_status solve_batch_sweep(bte_ctx* ctx, int b0, int nbb, const bte_opt
         g_sweep_tune[tkey] = ctx->sweep_shape;
     }
     const SweepShape shape = ctx->sweep_shape;
-    if (shape.staged) {  // a shape from the per-process cache: this plan's stage list may not exist yet
+    if (shape.staged || shape.split) {  // a shape from the per-process cache: this plan's stage list may not exist yet
         const StageList* sl = nullptr;
         bte_status s2 = stage_list(ctx, shape.cap, &sl);
         if (s2 != BTE_OK) return s2;

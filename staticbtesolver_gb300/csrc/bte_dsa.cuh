@@ -499,6 +499,109 @@ __global__ void __launch_bounds__(1024) k_gj_all(double* A, double* B, int m, un
     }
 }
 
+// The same inversion kGjBlock pivots at a time: ceil(m / kGjBlock) grid
+// barriers instead of m.  A step with pivot set K (rows and columns K0 ..
+// K0 + kb - 1, P = A[K,K]) is the kb scalar steps of k_gj_all at once:
+//   B[K,K] = P^-1,  B[K,j] = P^-1 A[K,j],  B[i,K] = -A[i,K] P^-1,
+//   B[i,j] = A[i,j] - (A[i,K] P^-1) A[K,j]   (i, j outside K);
+// every block forms P^-1 in shared memory by the scalar steps, then updates
+// its rows (rows by block, columns by thread) from the pivot rows A[K,:],
+// which it holds in shared memory.  Rounding differs from the scalar steps'
+// (a kb-term sum per entry instead of kb updates).  Dynamic shared memory:
+// kGjBlock * (m + kGjBlock + 1) doubles.  Barriers, buffers and *bad as in
+// k_gj_all; the inverse is in A when the number of steps is even, else in B.
+constexpr int kGjBlock = 16;
+__global__ void __launch_bounds__(1024) k_gj_block_all(double* A, double* B, int m, unsigned* bar, int* bad) {
+    extern __shared__ double gsm[];
+    double* sR = gsm;                                   // [kGjBlock][m] pivot rows A[K,:]
+    double* sP = gsm + (size_t)kGjBlock * m;           // [kGjBlock][kGjBlock] P, then P^-1
+    double* sT = sP + kGjBlock * kGjBlock;             // [kGjBlock] A[i,K] P^-1 of the current row
+    __shared__ int s_abort;
+    const unsigned nblk = gridDim.x;
+    const int tid = threadIdx.x;
+    double* src = A;
+    double* dst = B;
+    int step = 0;
+    for (int K0 = 0; K0 < m; K0 += kGjBlock, ++step) {
+        const int kb = min(kGjBlock, m - K0);
+        for (int q = tid; q < kb * m; q += blockDim.x) {
+            const int r = q / m, j = q - r * m;
+            sR[q] = __ldcg(src + (size_t)(K0 + r) * m + j);
+        }
+        __syncthreads();
+        // P^-1 by kb scalar steps (each thread one entry; read, barrier, write)
+        const int pr = tid / kb, pc = tid - pr * kb;
+        const bool pin = tid < kb * kb;
+        if (pin) sP[pr * kGjBlock + pc] = sR[(size_t)pr * m + K0 + pc];
+        __syncthreads();
+        for (int k = 0; k < kb; ++k) {
+            const double p = sP[k * kGjBlock + k];
+            if (tid == 0 && !(p > 0.0) && blockIdx.x == 0) atomicExch(bad, 1);
+            double v = 0.0;
+            if (pin) {
+                const double rp = 1.0 / p;
+                const double aik = sP[pr * kGjBlock + k], akj = sP[k * kGjBlock + pc];
+                if (pr == k) v = pc == k ? rp : akj * rp;
+                else if (pc == k) v = -aik * rp;
+                else v = fma(-aik, akj * rp, sP[pr * kGjBlock + pc]);
+            }
+            __syncthreads();
+            if (pin) sP[pr * kGjBlock + pc] = v;
+            __syncthreads();
+        }
+        for (int i = blockIdx.x; i < m; i += nblk) {
+            const bool piv = i >= K0 && i < K0 + kb;
+            if (!piv && tid < kb) {  // t = A[i,K] P^-1
+                double t = 0.0;
+                for (int l = 0; l < kb; ++l) t = fma(__ldcg(src + (size_t)i * m + K0 + l), sP[l * kGjBlock + tid], t);
+                sT[tid] = t;
+            }
+            __syncthreads();
+            for (int j = tid; j < m; j += blockDim.x) {
+                const bool jk = j >= K0 && j < K0 + kb;
+                double v;
+                if (piv) {
+                    const int r = i - K0;
+                    if (jk) {
+                        v = sP[r * kGjBlock + (j - K0)];
+                    } else {
+                        v = 0.0;
+                        for (int l = 0; l < kb; ++l) v = fma(sP[r * kGjBlock + l], sR[(size_t)l * m + j], v);
+                    }
+                } else if (jk) {
+                    v = -sT[j - K0];
+                } else {
+                    double acc = 0.0;
+                    for (int l = 0; l < kb; ++l) acc = fma(sT[l], sR[(size_t)l * m + j], acc);
+                    v = __ldcg(src + (size_t)i * m + j) - acc;
+                }
+                __stcg(dst + (size_t)i * m + j, v);
+            }
+            __syncthreads();
+        }
+        if (tid == 0) {
+            s_abort = 0;
+            __threadfence();
+            atomicAdd(bar, 1u);
+            const unsigned target = (unsigned)(step + 1) * nblk;
+            long long polls = 0;
+            while (ld_acquire(bar) < target) {
+                if (++polls > kBarrierPolls || *(volatile int*)bad == 2) {
+                    atomicExch(bad, 2);
+                    s_abort = 1;
+                    break;
+                }
+                __nanosleep(20);
+            }
+        }
+        __syncthreads();
+        if (s_abort) return;
+        double* t = src;
+        src = dst;
+        dst = t;
+    }
+}
+
 __global__ void k_to_float(const double* __restrict__ a, float* __restrict__ out, size_t n) {
     const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (q < n) out[q] = (float)a[q];

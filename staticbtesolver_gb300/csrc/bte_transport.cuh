@@ -880,28 +880,60 @@ __global__ void k_inflow_mask(const double* __restrict__ fc, int F, int n, size_
     mask[(size_t)d * n + c] = m;
 }
 
+// Downstream edges of every direction's upwind graph, for k_level_order.
+// mask[d][c] bit f: face f of c is an inflow face; an edge u -> c exists once
+// per such face g of c with nbr[c][g] == u.  down[d][u][f] = (k << 28) | c
+// when c = nbr[u][f] is named by no earlier face of u and k >= 1 edges run
+// u -> c, else -1.  Needs n < 2^28 and F <= 4.
+__global__ void k_downstream(const uint8_t* __restrict__ mask, const int* __restrict__ nbr, int n, int F,
+                             int* __restrict__ down) {
+    const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;  // u * F + f
+    const int d = blockIdx.y;
+    if (q >= (size_t)n * F) return;
+    const int u = (int)(q / F), f = (int)(q - (size_t)u * F);
+    const int c = nbr[q];
+    int out = -1;
+    if (c >= 0 && c < n) {
+        bool dup = false;
+        for (int f2 = 0; f2 < f; ++f2) dup |= nbr[(size_t)u * F + f2] == c;
+        if (!dup) {
+            const unsigned mc = mask[(size_t)d * n + c];
+            int k = 0;
+            for (int g = 0; g < F; ++g) k += ((mc >> g) & 1u) && nbr[(size_t)c * F + g] == u;
+            if (k > 0) out = (k << 28) | c;
+        }
+    }
+    down[(size_t)d * n * F + q] = out;
+}
+
 // Level order of every direction's upwind graph on the device, one block per
 // direction: Kahn's algorithm in waves (a wave is the cells whose inflow
 // neighbours all lie in earlier waves), each wave sorted by cell index -- the
 // order bte::level_order (sweep_order.h) builds on the host, for acyclic
-// graphs.  mask[d][c] bit f: face f of c is an inflow face; an edge u -> c
-// exists once per such face g of c with nbr[c][g] == u.  Both frontiers live
-// in dynamic shared memory, cap cells each (cap a power of two); a direction
+// graphs.  The edges come from k_downstream.  Both frontiers live in dynamic
+// shared memory, cap cells each (cap a power of two); with SDEG the
+// remaining in-degrees do too, one byte per cell (a cell has at most F <= 4
+// inflow faces, so a byte never borrows from its neighbour), else in indeg
+// [n_dir][n] in global memory.  Each thread loads the edges of its wave item
+// before the wave is sorted, so the loads overlap the sort.  A direction
 // whose graph has a cycle (status 1: cells left when no cell is free) or a
 // wave wider than cap (status 2) is left to the host.  Outputs: perm[d][pos],
 // lvl[d][0 .. nlev] (level starts, then n), the largest inflow count over
-// all directions in *fmax; indeg [n_dir][n] is work memory.
-__global__ void __launch_bounds__(1024) k_level_order(const uint8_t* __restrict__ mask, const int* __restrict__ nbr,
+// all directions in *fmax.
+template <bool SDEG>
+__global__ void __launch_bounds__(1024) k_level_order(const uint8_t* __restrict__ mask, const int* __restrict__ down,
                                                       int n, int F, int cap, int* __restrict__ indeg,
                                                       int* __restrict__ perm, int* __restrict__ lvl,
                                                       int* __restrict__ nlev, int* __restrict__ status,
                                                       int* __restrict__ fmax) {
-    extern __shared__ int fr[];  // [2][cap]
+    extern __shared__ int fr[];  // [2][cap], then with SDEG [ceil(n / 4)] words of in-degrees
+    unsigned* sdeg = reinterpret_cast<unsigned*>(fr + 2 * (size_t)cap);
     __shared__ int cnt[2];
     __shared__ int s_over;
     const int d = blockIdx.x;
     const uint8_t* md = mask + (size_t)d * n;
-    int* ind = indeg + (size_t)d * n;
+    int* ind = SDEG ? nullptr : indeg + (size_t)d * n;
+    const int* dd = down + (size_t)d * n * F;
     int* pd = perm + (size_t)d * n;
     int* ld = lvl + (size_t)d * (n + 1);
     if (threadIdx.x == 0) {
@@ -911,14 +943,29 @@ __global__ void __launch_bounds__(1024) k_level_order(const uint8_t* __restrict_
     }
     __syncthreads();
     int fm = 0;
-    for (int c = threadIdx.x; c < n; c += blockDim.x) {
-        const int k = __popc((unsigned)md[c]);
+    auto seed = [&](int c, int k) {
         fm = max(fm, k);
-        ind[c] = k;
         if (k == 0) {
             const int slot = atomicAdd(&cnt[0], 1);
             if (slot < cap) fr[slot] = c;
             else s_over = 1;
+        }
+    };
+    if (SDEG) {
+        for (int w = threadIdx.x; w < (n + 3) / 4; w += blockDim.x) {
+            unsigned word = 0;
+            for (int q = 0; q < 4 && 4 * w + q < n; ++q) {
+                const int k = __popc((unsigned)md[4 * w + q]);
+                word |= (unsigned)k << (8 * q);
+                seed(4 * w + q, k);
+            }
+            sdeg[w] = word;
+        }
+    } else {
+        for (int c = threadIdx.x; c < n; c += blockDim.x) {
+            const int k = __popc((unsigned)md[c]);
+            ind[c] = k;
+            seed(c, k);
         }
     }
     if (fm > 0) atomicMax(fmax, fm);
@@ -928,13 +975,23 @@ __global__ void __launch_bounds__(1024) k_level_order(const uint8_t* __restrict_
         const int m = cnt[cur];
         if (m == 0 || s_over) break;
         int* a = fr + (size_t)cur * cap;
+        int* b = fr + (size_t)(cur ^ 1) * cap;
         // bitonic sort of the wave, padded to a power of two (<= cap) with INT_MAX
         int P = 1;
         while (P < m) P <<= 1;
-        if (P <= (int)blockDim.x) {
+        const bool regs = P <= (int)blockDim.x;
+        const int i = threadIdx.x;
+        int dn[4] = {-1, -1, -1, -1};  // the edges of this thread's (unsorted) item
+        if (regs && i < m) {
+            const int u = a[i];
+#pragma unroll
+            for (int f = 0; f < 4; ++f)
+                if (f < F) dn[f] = dd[(size_t)u * F + f];
+        }
+        if (threadIdx.x == 0) cnt[cur ^ 1] = 0;  // read last before the previous wave's final barrier
+        if (regs) {
             // one element per thread: compare-exchange partners closer than a
             // warp through shuffles, the others through shared memory
-            const int i = threadIdx.x;
             int x = i < m ? a[i] : INT_MAX;
             for (int k = 2; k <= P; k <<= 1)
                 for (int j = k >> 1; j > 0; j >>= 1) {
@@ -955,16 +1012,16 @@ __global__ void __launch_bounds__(1024) k_level_order(const uint8_t* __restrict_
             if (i < P) a[i] = x;
             __syncthreads();
         } else {
-            for (int i = m + threadIdx.x; i < P; i += blockDim.x) a[i] = INT_MAX;
+            for (int t = m + threadIdx.x; t < P; t += blockDim.x) a[t] = INT_MAX;
             __syncthreads();
             for (int k = 2; k <= P; k <<= 1)
                 for (int j = k >> 1; j > 0; j >>= 1) {
-                    for (int i = threadIdx.x; i < P; i += blockDim.x) {
-                        const int l = i ^ j;
-                        if (l > i) {
-                            const int x = a[i], y = a[l];
-                            if ((x > y) == ((i & k) == 0)) {
-                                a[i] = y;
+                    for (int t = threadIdx.x; t < P; t += blockDim.x) {
+                        const int l = t ^ j;
+                        if (l > t) {
+                            const int x = a[t], y = a[l];
+                            if ((x > y) == ((t & k) == 0)) {
+                                a[t] = y;
                                 a[l] = x;
                             }
                         }
@@ -972,31 +1029,32 @@ __global__ void __launch_bounds__(1024) k_level_order(const uint8_t* __restrict_
                     __syncthreads();
                 }
         }
-        for (int i = threadIdx.x; i < m; i += blockDim.x) pd[pos + i] = a[i];
-        if (threadIdx.x == 0) {
-            ld[level] = pos;
-            cnt[cur ^ 1] = 0;
-        }
-        __syncthreads();
-        int* b = fr + (size_t)(cur ^ 1) * cap;
-        for (int i = threadIdx.x; i < m; i += blockDim.x) {
-            const int u = a[i];
-            for (int f = 0; f < F; ++f) {
-                const int c = nbr[(size_t)u * F + f];
-                if (c < 0 || c >= n) continue;
-                bool dup = false;  // c reached through an earlier face of u
-                for (int f2 = 0; f2 < f; ++f2) dup |= nbr[(size_t)u * F + f2] == c;
-                if (dup) continue;
-                const unsigned mc = md[c];
-                for (int g = 0; g < F; ++g) {
-                    if (!((mc >> g) & 1u) || nbr[(size_t)c * F + g] != u) continue;
-                    if (atomicSub(&ind[c], 1) == 1) {
-                        const int slot = atomicAdd(&cnt[cur ^ 1], 1);
-                        if (slot < cap) b[slot] = c;
-                        else s_over = 1;
-                    }
-                }
+        for (int t = threadIdx.x; t < m; t += blockDim.x) pd[pos + t] = a[t];
+        if (threadIdx.x == 0) ld[level] = pos;
+        // release the wave's downstream cells into the other frontier
+        auto relax = [&](int e) {
+            if (e < 0) return;
+            const int c = e & 0x0fffffff, k = e >> 28;
+            bool freed;
+            if (SDEG) {
+                const unsigned sh = 8u * (unsigned)(c & 3);
+                const unsigned old = atomicSub(&sdeg[c >> 2], (unsigned)k << sh);
+                freed = ((old >> sh) & 0xffu) == (unsigned)k;
+            } else {
+                freed = atomicSub(&ind[c], k) == k;
             }
+            if (freed) {
+                const int slot = atomicAdd(&cnt[cur ^ 1], 1);
+                if (slot < cap) b[slot] = c;
+                else s_over = 1;
+            }
+        };
+        if (regs) {
+#pragma unroll
+            for (int f = 0; f < 4; ++f) relax(dn[f]);
+        } else {
+            for (int t = threadIdx.x; t < m; t += blockDim.x)
+                for (int f = 0; f < F; ++f) relax(dd[(size_t)a[t] * F + f]);
         }
         pos += m;
         ++level;

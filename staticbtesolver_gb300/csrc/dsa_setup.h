@@ -141,8 +141,9 @@ inline void dsa_coefficients(int dim, int n, int F, const int* nbr, const double
 // A_c = P^T A P), which resolves every mode longer than an aggregate.  The
 // kernel gives each block one contiguous range of cells and splits it into
 // `per_block` contiguous aggregates, so the cells are first put in an order in
-// which contiguous ranges are compact: recursive bisection of the face
-// adjacency graph by breadth-first distance.
+// which contiguous ranges are compact: a Hilbert curve through the centroids
+// (hilbert_order) when they are known, else recursive bisection of the face
+// adjacency graph by breadth-first distance (locality_order).
 
 // order[k] = the cell at position k.  Each range of more than `leaf` cells is
 // ordered by breadth-first distance from the farthest cell (found by a first
@@ -231,6 +232,102 @@ inline void locality_order(int n, int F, const int* nbr /* [n][F], < 0 none */, 
             next.push_back({mid, r.e});
         }
         ranges.swap(next);
+    }
+}
+
+// Position of a point on a Hilbert curve through a 2^b x 2^b (x 2^b) grid:
+// the published transpose algorithm of J. Skilling, "Programming the Hilbert
+// curve", AIP Conf. Proc. 707 (2004) 381 -- undo the excess work of the
+// Gray-code walk from the top bit down, Gray-encode, then read the key's bits
+// from the transposed coordinates, most significant first.  x[0..dim-1] < 2^b,
+// dim * b <= 64.  Consecutive keys are neighbouring grid cells.
+inline unsigned long long hilbert_key(unsigned x[3], int dim, int b) {
+    const unsigned top = 1u << (b - 1);
+    for (unsigned q = top; q > 1; q >>= 1) {
+        const unsigned low = q - 1;
+        for (int i = 0; i < dim; ++i) {
+            if (x[i] & q) {
+                x[0] ^= low;
+            } else {
+                const unsigned t = (x[0] ^ x[i]) & low;
+                x[0] ^= t;
+                x[i] ^= t;
+            }
+        }
+    }
+    for (int i = 1; i < dim; ++i) x[i] ^= x[i - 1];
+    unsigned t = 0;
+    for (unsigned q = top; q > 1; q >>= 1)
+        if (x[dim - 1] & q) t ^= q - 1;
+    for (int i = 0; i < dim; ++i) x[i] ^= t;
+    unsigned long long key = 0;
+    for (int q = b - 1; q >= 0; --q)
+        for (int i = 0; i < dim; ++i) key = (key << 1) | ((x[i] >> q) & 1u);
+    return key;
+}
+
+// Locality order from the cells' centroids ([n][3]; dim 1, 2 or 3 used): the
+// cells sorted by their position on a Hilbert curve through the bounding box
+// (one scale for every axis, 2^21 steps along the longest side), ties by cell
+// index.  A range of the curve is a compact, mostly connected piece of the
+// domain.  On a 100k-triangle square its 608 aggregates need 120 conjugate-
+// gradient iterations where recursive bisection's need 167-206 (to a 1e-3
+// relative residual), and it cuts a third fewer faces between the blocks.
+// Keys are formed on host threads; the sort is a stable radix sort, so the
+// order does not depend on the thread count.
+inline void hilbert_order(int dim, int n, const double* centroid, std::vector<int>& order) {
+    order.resize(n);
+    if (n <= 0) return;
+    dim = std::max(1, std::min(dim, 3));
+    const int b = dim == 1 ? 32 : 21;
+    double lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+    for (int i = 0; i < dim; ++i) lo[i] = hi[i] = centroid[i];
+    for (int c = 0; c < n; ++c)
+        for (int i = 0; i < dim; ++i) {
+            lo[i] = std::min(lo[i], centroid[3 * (size_t)c + i]);
+            hi[i] = std::max(hi[i], centroid[3 * (size_t)c + i]);
+        }
+    double ext = 0.0;
+    for (int i = 0; i < dim; ++i) ext = std::max(ext, hi[i] - lo[i]);
+    const double steps = std::ldexp(1.0, b);
+    const double scale = ext > 0.0 ? steps / ext : 0.0;
+    const double cap = steps - 1.0;
+    std::vector<unsigned long long> key(n);
+    auto keys = [&](int c0, int c1) {
+        for (int c = c0; c < c1; ++c) {
+            unsigned x[3] = {0, 0, 0};
+            for (int i = 0; i < dim; ++i) {
+                const double v = (centroid[3 * (size_t)c + i] - lo[i]) * scale;
+                x[i] = (unsigned)std::min(std::max(v, 0.0), cap);
+            }
+            key[c] = dim == 1 ? (unsigned long long)x[0] : hilbert_key(x, dim, b);
+        }
+    };
+    const int nt = (int)std::max(1u, std::min(8u, std::thread::hardware_concurrency()));
+    if (nt > 1 && n >= 65536) {
+        std::vector<std::thread> th;
+        for (int t = 0; t < nt; ++t)
+            th.emplace_back(keys, (int)((long long)n * t / nt), (int)((long long)n * (t + 1) / nt));
+        for (auto& t : th) t.join();
+    } else {
+        keys(0, n);
+    }
+    // least significant digit first, 16 bits per pass, over the key bits in use
+    const int bits = dim * b;
+    std::vector<int> tmp(n);
+    std::iota(order.begin(), order.end(), 0);
+    std::vector<int> cnt(1 << 16);
+    for (int sh = 0; sh < bits; sh += 16) {
+        std::fill(cnt.begin(), cnt.end(), 0);
+        for (int k = 0; k < n; ++k) ++cnt[(key[order[k]] >> sh) & 0xffff];
+        int run = 0;
+        for (int& v : cnt) {
+            const int c = v;
+            v = run;
+            run += c;
+        }
+        for (int k = 0; k < n; ++k) tmp[cnt[(key[order[k]] >> sh) & 0xffff]++] = order[k];
+        order.swap(tmp);
     }
 }
 

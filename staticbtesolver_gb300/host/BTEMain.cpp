@@ -6,6 +6,8 @@
 //   --inner-tol X        inner relative residual (default 1e-9)
 //   --accel none|aitken|anderson, --accel-every N
 //                        outer-iteration acceleration (default none: the reference's iteration)
+//   --dsa                diffusion-synthetic correction after each outer iteration
+//                        (diffusive problems; the margin and its stop are unchanged)
 //   --tempcell FILE      write the cell temperatures as the reference's Tempcell.dat
 //                        ("x/L_x y/L_y [z/L_z] T" per cell, src/StaticBTESolver.cpp:818-831)
 #include <getopt.h>
@@ -38,9 +40,11 @@ extern "C" int sbte_main(int argc, char** argv) {
                                        {"tempcell", required_argument, nullptr, 1004},
                                        {"accel", required_argument, nullptr, 1005},
                                        {"accel-every", required_argument, nullptr, 1006},
+                                       {"dsa", no_argument, nullptr, 1007},
                                        {nullptr, 0, nullptr, 0}};
     std::string geo, bandfile, bcfile, tempcell;
     int accel = 0, accel_every = 8;
+    bool dsa = false;
     double L_x = 0, L_y = 0, L_z = 0, T_ref = 300, tol = 1e-5, inner_tol = 1e-9;
     int DM = 3, ntheta = 4, nphi = 4, maxIter = 10000, form = 0;
     bool has_bc = false;
@@ -73,6 +77,7 @@ extern "C" int sbte_main(int argc, char** argv) {
                 break;
             }
             case 1006: accel_every = std::stoi(optarg); break;
+            case 1007: dsa = true; break;
             default: std::cerr << "Unknown option " << c << std::endl; return 1;
         }
     }
@@ -112,6 +117,7 @@ extern "C" int sbte_main(int argc, char** argv) {
         solver.setTolerance(tol);
         solver.setInnerTolerance(inner_tol);
         solver.setAccel(accel, accel_every);
+        solver.setDsa(dsa);
         solver.solve(maxIter);
         rc = (solver.status() == 0 || solver.status() == 6) ? 0 : 1;
         if (rc == 0 && !tempcell.empty() && !solver.writeTempcell(tempcell)) {

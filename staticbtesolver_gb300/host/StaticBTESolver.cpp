@@ -41,6 +41,11 @@ void StaticBTESolver::setAccel(int accel, int every) {
     accel_every_ = every;
 }
 void StaticBTESolver::setMlp(const std::vector<float>& params) { mlp_ = params; }
+void StaticBTESolver::setDsa(bool on, double tol, int maxit) {
+    dsa_ = on;
+    dsa_tol_ = tol;
+    dsa_maxit_ = maxit;
+}
 void StaticBTESolver::setTolerance(double tol) { tol_ = tol; }
 void StaticBTESolver::setInnerTolerance(double tol) { inner_tol_ = tol; }
 void StaticBTESolver::setVerbose(bool v) { verbose_ = v; }
@@ -81,6 +86,9 @@ void StaticBTESolver::solve(int max_iter) {
     o.form = form_;
     o.accel = accel_;
     o.accel_every = accel_every_;
+    o.dsa = dsa_ ? 1 : 0;
+    o.dsa_tol = dsa_tol_;
+    o.dsa_maxit = dsa_maxit_;
     if (accel_ == 1 || accel_ == 2) {  // the per-cell extrapolations use the centroids
         status_ = bte_set_centroids(ctx_, P.centroid.data());
         if (status_ == BTE_OK && accel_ == 1) {

@@ -40,6 +40,15 @@ extern "C" void order_c(int n, int F, const int* nbr, int leaf, int* out) {
     bte::locality_order(n, F, nbr, leaf, o);
     std::copy(o.begin(), o.end(), out);
 }
+extern "C" void hilbert_c(int dim, int n, const double* cen, int* out) {
+    std::vector<int> o;
+    bte::hilbert_order(dim, n, cen, o);
+    std::copy(o.begin(), o.end(), out);
+}
+extern "C" unsigned long long hkey_c(int dim, int b, unsigned x0, unsigned x1, unsigned x2) {
+    unsigned x[3] = {x0, x1, x2};
+    return bte::hilbert_key(x, dim, b);
+}
 extern "C" int coarse_c(int n, int F, const int* nb, const double* w, int nblk, int per, double* ac, int* geo,
                         int* need_ptr, int* need) {
     bte::DsaCoarse co;
@@ -62,6 +71,8 @@ def lib(tmp_path_factory):
     subprocess.run(["g++", "-O2", "-std=c++17", "-shared", "-fPIC", "-o", str(out), str(src)], check=True)
     L = C.CDLL(str(out))
     L.dsa_c.restype = C.c_int
+    L.hkey_c.restype = C.c_ulonglong
+    L.hkey_c.argtypes = [C.c_int, C.c_int, C.c_uint, C.c_uint, C.c_uint]
     return L
 
 
@@ -213,3 +224,68 @@ def test_locality_order_and_coarse_operator(lib, oracle_mod, get_case, name):
     # compact aggregates: many couplings stay inside an aggregate
     inside = (agg[rows[msk]] == agg[nbp[msk]]).mean()
     assert inside > 0.4, inside  # a random numbering keeps ~1/32 inside
+
+
+def _hilbert_keys(q, b):
+    """NumPy restatement of the transpose algorithm (J. Skilling, AIP Conf.
+    Proc. 707 (2004) 381) for integer points q [n][dim] < 2^b."""
+    x = [q[:, i].astype(np.uint64) for i in range(q.shape[1])]
+    dim = len(x)
+    Q = 1 << (b - 1)
+    while Q > 1:
+        low = np.uint64(Q - 1)
+        for i in range(dim):
+            hit = (x[i] & np.uint64(Q)) != 0
+            t = (x[0] ^ x[i]) & low
+            x0 = np.where(hit, x[0] ^ low, x[0] ^ t)
+            if i > 0:
+                x[i] = np.where(hit, x[i], x[i] ^ t)
+            x[0] = x0
+        Q >>= 1
+    for i in range(1, dim):
+        x[i] = x[i] ^ x[i - 1]
+    t = np.zeros_like(x[0])
+    Q = 1 << (b - 1)
+    while Q > 1:
+        t = np.where((x[dim - 1] & np.uint64(Q)) != 0, t ^ np.uint64(Q - 1), t)
+        Q >>= 1
+    x = [xi ^ t for xi in x]
+    key = np.zeros_like(x[0])
+    for q_ in range(b - 1, -1, -1):
+        for i in range(dim):
+            key = (key << np.uint64(1)) | ((x[i] >> np.uint64(q_)) & np.uint64(1))
+    return key
+
+
+@pytest.mark.parametrize("dim,b", [(2, 4), (3, 3)])
+def test_hilbert_key_walks_grid_neighbours(lib, dim, b):
+    """Sorted by key, the cells of a 2^b grid form a path of unit steps that
+    visits every cell once (the defining property of the curve)."""
+    side = 1 << b
+    pts = np.stack(np.meshgrid(*[np.arange(side)] * dim, indexing="ij"), -1).reshape(-1, dim)
+    keys = np.array([lib.hkey_c(dim, b, *(list(map(int, p)) + [0] * (3 - dim))) for p in pts], np.uint64)
+    assert np.array_equal(np.sort(keys), np.arange(side ** dim, dtype=np.uint64))
+    path = pts[np.argsort(keys)]
+    assert (np.abs(np.diff(path, axis=0)).sum(1) == 1).all()
+    np.testing.assert_array_equal(_hilbert_keys(pts, b), keys)
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_hilbert_order_matches_restatement(lib, dim):
+    """hilbert_order on 70,000 random centroids (host threads and radix
+    passes) equals a stable sort of the restated keys, ties by cell index."""
+    rng = np.random.default_rng(dim)
+    n = 70000
+    cen = np.zeros((n, 3))
+    cen[:, :dim] = rng.uniform(-1e-6, 3e-6, (n, dim))
+    cen[:, 0] *= 0.5  # a box longer in y: one scale for every axis
+    cen[100:200] = cen[5000]  # ties
+    out = np.zeros(n, np.int32)
+    lib.hilbert_c(dim, n, cen.ctypes.data_as(C.c_void_p), out.ctypes.data_as(C.c_void_p))
+    b = 21
+    lo = cen[:, :dim].min(0)
+    ext = (cen[:, :dim].max(0) - lo).max()
+    steps = float(1 << b)
+    q = np.minimum(np.maximum((cen[:, :dim] - lo) * (steps / ext), 0.0), steps - 1).astype(np.uint64)
+    want = np.argsort(_hilbert_keys(q, b), kind="stable")
+    np.testing.assert_array_equal(out, want)

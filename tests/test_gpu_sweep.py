@@ -143,8 +143,9 @@ def _odd_slab(c):
                                         ("3DM2DG", None), ("cube5_b8", "4,64"), ("square16_b8/cycles", None),
                                         ("slab1d/odd", None), ("2Dcase5", None)])
 def test_sweep_kernels_agree(sbte, get_case, monkeypatch, tmp_path, name, shape):
-    """The two sweep kernels compute the same x to the bit: the
-    level-synchronous one and the staged one (levels copied into shared memory
+    """The sweep kernels compute the same x to the bit: the
+    level-synchronous one, the same over levels split into slices of one
+    position per thread, and the staged one (levels copied into shared memory
     ahead of use by bulk copies, right-hand side formed beforehand in level
     order).  Same temperatures, margins (summed by k_reduce here) and
     iteration counts, on 1D, 2D and 3D plans, with lagged edges, with an odd
@@ -164,7 +165,7 @@ def test_sweep_kernels_agree(sbte, get_case, monkeypatch, tmp_path, name, shape)
     runs = {}
     if shape:
         monkeypatch.setenv("BTE_SWEEP_SHAPE", shape)
-    for kernel in ("level", "staged"):
+    for kernel in ("level", "staged", "split"):
         monkeypatch.setenv("BTE_SWEEP_KERNEL", kernel)
         if name.endswith("/cycles"):
             ctx = sbte.Context(0).set_arrays(_rewired(sbte, c, n_swaps=10))
@@ -175,7 +176,7 @@ def test_sweep_kernels_agree(sbte, get_case, monkeypatch, tmp_path, name, shape)
         runs[kernel] = (st, ctx.temperature(), ctx.margins(), rep.as_dict(), ctx.sweep_tuning())
         ctx.close()
     s0, T0, m0, r0, t0 = runs["level"]
-    for kid, kernel in ((1, "staged"),):
+    for kid, kernel in ((1, "staged"), (2, "split")):
         s1, T1, m1, r1, t1 = runs[kernel]
         assert s0 == s1 and s0 in (0, 6)
         assert r0["sweep_kernel"] == 0 and r1["sweep_kernel"] == kid, (r0, r1)
@@ -188,17 +189,19 @@ def test_sweep_kernels_agree(sbte, get_case, monkeypatch, tmp_path, name, shape)
 
 
 @pytest.mark.parametrize("name", ["square16_b8", "2DM2DG", "3DM2DG", "cube5_b8", "square16_b8/cycles", "slab1d/odd",
-                                  "2Dcase5"])
+                                  "2Dcase5", "2Dcase5/global", "cube5_b8/global", "square100k"])
 def test_device_level_order_matches_host(sbte, get_case, monkeypatch, tmp_path, name):
     """The sweep plan's level order built on the device (k_level_order: one
     block per direction, Kahn's waves, each wave sorted by cell index in
-    shared memory) is the host's (sweep_order.h, BTE_LEVEL_ORDER=host) entry
-    for entry.  Directions whose upwind graph has a cycle are ordered on the
-    host in both runs (they need the host's cycle breaking)."""
+    shared memory; in-degrees in shared memory, or with /global in global
+    memory, BTE_LEVEL_ORDER=global) is the host's (sweep_order.h,
+    BTE_LEVEL_ORDER=host) entry for entry.  Directions whose upwind graph has
+    a cycle are ordered on the host in both runs (they need the host's cycle
+    breaking)."""
     from staticbtesolver_gb300 import synth
 
     base = name.split("/")[0]
-    if base.startswith("cube"):
+    if base.startswith("cube") or base == "square100k":
         p = synth.make_problem(base, str(tmp_path))
         args = (p.geo, p.bc_file, p.band_file, p.DM, p.num_theta, p.num_phi, p.T_ref, p.L_x, p.L_y, p.L_z)
         c = None
@@ -209,6 +212,8 @@ def test_device_level_order_matches_host(sbte, get_case, monkeypatch, tmp_path, 
     for where in ("device", "host"):
         if where == "host":
             monkeypatch.setenv("BTE_LEVEL_ORDER", "host")
+        elif name.endswith("/global"):
+            monkeypatch.setenv("BTE_LEVEL_ORDER", "global")
         else:
             monkeypatch.delenv("BTE_LEVEL_ORDER", raising=False)
         if name.endswith("/cycles"):

@@ -190,6 +190,8 @@ struct bte_ctx {
     std::vector<int> dsa_order;  // position -> cell of the low-order solve's numbering
     int dsa_chunk = 0, dsa_seg = 0, dsa_n_agg = 0;
     bool dsa_stage = false;  // rows of the coarse inverse staged in shared memory
+    bool dsa_topo = false;   // each block's couplings staged in shared memory
+    int dsa_rows = 0;        // the longest need list (staged rows of the coarse inverse)
     size_t dsa_smem = 0;     // dynamic shared memory of k_dsa_pcg
     // results
     double* e_curr = nullptr;
@@ -877,10 +879,16 @@ static bte_status dsa_upload(bte_ctx* ctx, DsaHostPlan& hp, cudaStream_t st) {
     BTE_CUDA(cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device));
     const size_t staged = sizeof(float) * (2 + (size_t)rows) * co.n_agg;
     ctx->dsa_stage = staged + 16384 <= (size_t)smem_max;
+    ctx->dsa_rows = rows;
     ctx->dsa_smem = ctx->dsa_stage ? staged : sizeof(float) * 2 * (size_t)co.n_agg;
-    BTE_CUDA(cudaFuncSetAttribute(bte::dsa::k_dsa_pcg, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)ctx->dsa_smem));
-    BTE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, bte::dsa::k_dsa_pcg, kDsaThreads, ctx->dsa_smem));
+    // and the blocks' couplings after them, when those fit too
+    const size_t with_topo = sizeof(float) * (bte::dsa::dsa_topo_offset(co.n_agg, ctx->dsa_stage ? rows : 0) +
+                                              bte::dsa::dsa_topo_words(co.chunk, F));
+    ctx->dsa_topo = with_topo + 16384 <= (size_t)smem_max;
+    if (ctx->dsa_topo) ctx->dsa_smem = with_topo;
+    auto pcg = ctx->dsa_topo ? bte::dsa::k_dsa_pcg<true> : bte::dsa::k_dsa_pcg<false>;
+    BTE_CUDA(cudaFuncSetAttribute(pcg, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ctx->dsa_smem));
+    BTE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, pcg, kDsaThreads, ctx->dsa_smem));
     if (occ < 1 || nblk > occ * sms) return fail(ctx, BTE_ERR_CUDA, "dsa: the low-order kernel cannot be resident");
     BTE_CUDA(upload(ctx->d_lo_nb, nbv, st));
     BTE_CUDA(upload(ctx->d_lo_w, w, st));
@@ -934,8 +942,8 @@ static bte_status dsa_launch(bte_ctx* ctx, int n, int F, double tol, int maxit) 
     BTE_CUDA(cudaMemsetAsync(ctx->cg_bar.p, 0, sizeof(unsigned) * 2, st));
     bte::dsa::Lo lo{n, F, ctx->d_lo_nb.as<int>(), ctx->d_lo_w.as<float>(), ctx->d_lo_dsc.as<double>(),
                     ctx->d_lo_agg.as<int>(), ctx->d_lo_nagg.as<int>()};
-    bte::dsa::Coarse co{ctx->dsa_chunk, ctx->dsa_seg, ctx->dsa_n_agg, ctx->dsa_stage ? 1 : 0,
-                        ctx->d_co_ainv.as<float>(),
+    bte::dsa::Coarse co{ctx->dsa_chunk, ctx->dsa_seg, ctx->dsa_n_agg, ctx->dsa_stage ? 1 : 0, ctx->dsa_rows,
+                        ctx->dsa_topo ? 1 : 0, ctx->d_co_ainv.as<float>(),
                         ctx->d_co_need_ptr.as<int>(), ctx->d_co_need.as<int>(), ctx->d_co_sums.as<float>(),
                         ctx->d_co_sums0.as<double>()};
     bte::dsa::CgWork wk{ctx->cg_r.as<float>(), ctx->cg_aw.as<float>(), ctx->cg_s.as<float>(), ctx->cg_x.as<float>(),
@@ -944,8 +952,8 @@ static bte_status dsa_launch(bte_ctx* ctx, int n, int F, double tol, int maxit) 
     const double* b = ctx->d_dsa_b.as<double>();
     double* x = ctx->d_dsa_x.as<double>();
     void* args[] = {&lo, &co, &wk, &b, &tol, &maxit, &x};
-    BTE_CUDA(cudaLaunchCooperativeKernel((const void*)bte::dsa::k_dsa_pcg, dim3(ctx->dsa_blocks), dim3(kDsaThreads),
-                                         args, ctx->dsa_smem, st));
+    const void* pcg = ctx->dsa_topo ? (const void*)bte::dsa::k_dsa_pcg<true> : (const void*)bte::dsa::k_dsa_pcg<false>;
+    BTE_CUDA(cudaLaunchCooperativeKernel(pcg, dim3(ctx->dsa_blocks), dim3(kDsaThreads), args, ctx->dsa_smem, st));
     BTE_LAUNCHED();
     return BTE_OK;
 }

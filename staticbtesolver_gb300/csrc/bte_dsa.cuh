@@ -55,6 +55,8 @@ constexpr int AGG = 4;
 struct Coarse {
     int chunk, seg, n_agg;
     int stage;             // nonzero: the block's rows of ainv are copied to shared memory once
+    int rows;              // the longest need list (rows of ainv a block stages)
+    int topo;              // nonzero: each block's cells' nb, nagg, w and agg are copied to shared memory once
     const float* ainv;     // [n_agg][n_agg]
     const int* need_ptr;   // [nblk+1]
     const int* need;       // aggregates of a block's cells and of their neighbours
@@ -118,7 +120,12 @@ __device__ __forceinline__ void block_sum2(double& a, double& b) {
 // (other parity), never round r+2 (that needs every block past round r+1).
 // The wait is bounded: after kBarrierPolls polls a block records an error and
 // the call reports failure, so a kernel never spins forever.
-__device__ __forceinline__ bool grid_sum2(double& a, double& b, const CgWork& wk, unsigned nblk, unsigned& round) {
+// after(): run by every thread once the barrier is passed, before the sums
+// are read (loads of other published values overlap those of the partials);
+// fin(a, b): run by thread 0 with the sums, before the block's final barrier.
+template <typename After, typename Fin>
+__device__ __forceinline__ bool grid_sum2(double& a, double& b, const CgWork& wk, unsigned nblk, unsigned& round,
+                                          After&& after, Fin&& fin) {
     __shared__ int s_ok;
     __shared__ double s_a, s_b;
     block_sum2(a, b);
@@ -142,6 +149,7 @@ __device__ __forceinline__ bool grid_sum2(double& a, double& b, const CgWork& wk
         }
     }
     __syncthreads();
+    after();
     if (threadIdx.x < 32) {
         double x = 0.0, y = 0.0;
 #pragma unroll 4
@@ -157,12 +165,16 @@ __device__ __forceinline__ bool grid_sum2(double& a, double& b, const CgWork& wk
         if (threadIdx.x == 0) {
             s_a = x;
             s_b = y;
+            fin(x, y);
         }
     }
     __syncthreads();
     a = s_a;
     b = s_b;
     return s_ok != 0;
+}
+__device__ __forceinline__ bool grid_sum2(double& a, double& b, const CgWork& wk, unsigned nblk, unsigned& round) {
+    return grid_sum2(a, b, wk, nblk, round, [] {}, [](double, double) {});
 }
 
 // r_{i+1} of cell c from the previous iteration's parity copies: the one
@@ -222,21 +234,33 @@ __device__ __forceinline__ void coarse_rows(const Coarse& co, const float* rows,
     }
 }
 
+// Shared-memory layout of k_dsa_pcg: the couplings start after (2 + rows)
+// n_agg floats, rounded up to 16 bytes, and take 3 F + 1 words per cell of
+// a block's range.
+__host__ __device__ constexpr size_t dsa_topo_offset(int n_agg, int rows) {
+    return (((size_t)(2 + rows) * n_agg + 3) / 4) * 4;
+}
+__host__ __device__ constexpr size_t dsa_topo_words(int chunk, int F) { return (size_t)(3 * F + 1) * chunk; }
+
 // Solve A x = b (A = the low-order operator before scaling, both in the
 // solve's numbering) for b[n] (FP64) into xout[n] (FP64): preconditioned
 // conjugate gradients, M^-1 = I + P A_c^-1 P^T on the scaled operator,
 // relative tolerance tol on sqrt(r.M r), at most maxit iterations.  Launched
 // cooperatively with one block per cell range of the coarse set-up, every
 // block resident.  Dynamic shared memory: (2 + rows) n_agg floats, rows = the
-// longest need list when co.stage, else 0.
+// longest need list when co.stage, else 0; with co.topo then
+// dsa_topo_words(chunk, F) words, the block's cells' couplings (neighbour
+// position, its aggregate, weight) and aggregates, so a cell's neighbour
+// values are one dependent load away instead of two.
 //
 // The coarse correction needs P^T r_{i+1} of every aggregate before any block
 // can form u_{i+1} = M^-1 r_{i+1}; it follows without another barrier from
 // the aggregate sums the owners published with the last dot products:
 //   P^T r_{i+1} = P^T r_i - alpha_i (P^T w_i + beta_i P^T s_{i-1}).
+template <bool TOPO>
 __global__ void __launch_bounds__(THREADS) k_dsa_pcg(Lo lo, Coarse co, CgWork wk, const double* __restrict__ b,
                                                     double tol, int maxit, double* __restrict__ xout) {
-    extern __shared__ float smem[];
+    extern __shared__ __align__(16) float smem[];
     float* sR = smem;              // [n_agg] P^T r of every aggregate
     float* sX = smem + co.n_agg;   // [n_agg] coarse solution (the needed entries)
     float* sA = smem + 2 * co.n_agg;  // the block's rows of A_c^-1 (stage)
@@ -252,6 +276,27 @@ __global__ void __launch_bounds__(THREADS) k_dsa_pcg(Lo lo, Coarse co, CgWork wk
     const unsigned nblk = gridDim.x;
     const int c_lo = blockIdx.x * co.chunk, c_hi = min(n, c_lo + co.chunk);
     const int K0 = blockIdx.x * AGG;  // this block's first aggregate
+    // the block's couplings, [F][chunk] each, by local cell c - c_lo
+    const int ch = co.chunk;
+    int* tNb = reinterpret_cast<int*>(smem + dsa_topo_offset(co.n_agg, co.stage ? co.rows : 0));
+    int* tNagg = tNb + (size_t)F * ch;
+    float* tW = reinterpret_cast<float*>(tNagg + (size_t)F * ch);
+    int* tAgg = reinterpret_cast<int*>(tW + (size_t)F * ch);
+    if (TOPO) {
+        for (int q = threadIdx.x; q < F * ch; q += blockDim.x) {
+            const int f = q / ch, c = c_lo + (q - f * ch);
+            if (c >= c_hi) continue;
+            tNb[q] = lo.nb[(size_t)f * n + c];
+            tNagg[q] = lo.nagg[(size_t)f * n + c];
+            tW[q] = lo.w[(size_t)f * n + c];
+        }
+        for (int c = c_lo + threadIdx.x; c < c_hi; c += blockDim.x) tAgg[c - c_lo] = lo.agg[c];
+        __syncthreads();
+    }
+    auto nb_of = [&](int f, int c) { return TOPO ? tNb[f * ch + (c - c_lo)] : lo.nb[(size_t)f * n + c]; };
+    auto nagg_of = [&](int f, int c) { return TOPO ? tNagg[f * ch + (c - c_lo)] : lo.nagg[(size_t)f * n + c]; };
+    auto w_of = [&](int f, int c) { return TOPO ? tW[f * ch + (c - c_lo)] : lo.w[(size_t)f * n + c]; };
+    auto agg_of = [&](int c) { return TOPO ? tAgg[c - c_lo] : lo.agg[c]; };
     // phase 0: ||D^-1/2 b|| and the aggregate sums of D^-1/2 b
     double nrm2 = 0.0, unused = 0.0;
     {
@@ -303,13 +348,13 @@ __global__ void __launch_bounds__(THREADS) k_dsa_pcg(Lo lo, Coarse co, CgWork wk
         float acc[AGG][3] = {};
         for (int c = c_lo + threadIdx.x; c < c_hi; c += blockDim.x) {
             const float rc = (float)(lo.dsc[c] * b[c] * inv);
-            const float uc = rc + sX[lo.agg[c]];
+            const float uc = rc + sX[agg_of(c)];
             float wc = uc;
             for (int f = 0; f < F; ++f) {
-                const int o = lo.nb[(size_t)f * n + c];
+                const int o = nb_of(f, c);
                 if (o < 0) continue;
-                const float uo = (float)(lo.dsc[o] * b[o] * inv) + sX[lo.nagg[(size_t)f * n + c]];
-                wc = __fmaf_rn(-lo.w[(size_t)f * n + c], uo, wc);
+                const float uo = (float)(lo.dsc[o] * b[o] * inv) + sX[nagg_of(f, c)];
+                wc = __fmaf_rn(-w_of(f, c), uo, wc);
             }
             __stcg(wk.r + c, rc);
             __stcg(wk.aw + c, wc);
@@ -327,7 +372,24 @@ __global__ void __launch_bounds__(THREADS) k_dsa_pcg(Lo lo, Coarse co, CgWork wk
         const float t = block_sum_aggs(acc, red);
         if (threadIdx.x < 3 * AGG) __stcg(pub + (size_t)3 * K0 + threadIdx.x, t);
     }
-    if (!grid_sum2(gamma, delta, wk, nblk, round)) return;
+    // the aggregate sums (r, A u, s) published before a barrier, loaded into
+    // registers as soon as the barrier is passed (aggregates threadIdx.x +
+    // q blockDim.x; any beyond KPT blockDim are loaded where they are used)
+    constexpr int KPT = 4;
+    float nr[KPT] = {}, nw[KPT] = {}, ns[KPT] = {};
+    auto load_sums = [&](int Pn) {
+        const float* got = co.sums + (size_t)3 * co.n_agg * Pn;
+#pragma unroll
+        for (int q = 0; q < KPT; ++q) {
+            const int K = threadIdx.x + q * blockDim.x;
+            if (K < co.n_agg) {
+                nr[q] = __ldcg(got + 3 * K);
+                nw[q] = __ldcg(got + 3 * K + 1);
+                ns[q] = __ldcg(got + 3 * K + 2);
+            }
+        }
+    };
+    if (!grid_sum2(gamma, delta, wk, nblk, round, [&] { load_sums(0); }, [](double, double) {})) return;
     const double gamma0 = gamma;
     double alpha = delta > 0.0 ? gamma / delta : 0.0, beta = 0.0;
     int it = 0;
@@ -343,8 +405,13 @@ __global__ void __launch_bounds__(THREADS) k_dsa_pcg(Lo lo, Coarse co, CgWork wk
         const int P = it & 1;
         const float fma_ = -fa;
         // P^T r_{i+1} of every aggregate from the published sums, then the coarse solve
+#pragma unroll
+        for (int q = 0; q < KPT; ++q) {
+            const int K = threadIdx.x + q * blockDim.x;
+            if (K < co.n_agg) sR[K] = __fmaf_rn(fma_, __fmaf_rn(fb, ns[q], nw[q]), nr[q]);
+        }
         const float* got = co.sums + (size_t)3 * co.n_agg * P;
-        for (int K = threadIdx.x; K < co.n_agg; K += blockDim.x) {
+        for (int K = threadIdx.x + KPT * blockDim.x; K < co.n_agg; K += blockDim.x) {
             const float sr = __ldcg(got + 3 * K), sw = __ldcg(got + 3 * K + 1), ss = __ldcg(got + 3 * K + 2);
             sR[K] = __fmaf_rn(fma_, __fmaf_rn(fb, ss, sw), sr);
         }
@@ -362,14 +429,14 @@ __global__ void __launch_bounds__(THREADS) k_dsa_pcg(Lo lo, Coarse co, CgWork wk
             wk.p[c] = pc;
             wk.x[c] = __fmaf_rn(fa, pc, wk.x[c]);
             const float rn = __fmaf_rn(fma_, si, ri);
-            const int ac = lo.agg[c];
+            const int ac = agg_of(c);
             const float un = rn + sX[ac];
             float wn = un;
             for (int f = 0; f < F; ++f) {
-                const int o = lo.nb[(size_t)f * n + c];
+                const int o = nb_of(f, c);
                 if (o < 0) continue;
-                const float uo = next_residual(wk, P, o, fma_, fb, n) + sX[lo.nagg[(size_t)f * n + c]];
-                wn = __fmaf_rn(-lo.w[(size_t)f * n + c], uo, wn);
+                const float uo = next_residual(wk, P, o, fma_, fb, n) + sX[nagg_of(f, c)];
+                wn = __fmaf_rn(-w_of(f, c), uo, wn);
             }
             __stcg(wk.s + (size_t)P * n + c, si);
             __stcg(wk.r + (size_t)(P ^ 1) * n + c, rn);
@@ -385,21 +452,22 @@ __global__ void __launch_bounds__(THREADS) k_dsa_pcg(Lo lo, Coarse co, CgWork wk
         const float t = block_sum_aggs(acc, red);
         if (threadIdx.x < 3 * AGG)
             __stcg(co.sums + (size_t)3 * co.n_agg * (P ^ 1) + (size_t)3 * K0 + threadIdx.x, t);
-        if (!grid_sum2(gn, dn, wk, nblk, round)) return;
-        ++it;
-        if (threadIdx.x == 0) {  // every thread holds the same gn, dn, gamma, alpha
-            const double bnew = gn / gamma;
-            const double den = dn - bnew * gn / alpha;
-            const bool st = gn <= tol * tol * gamma0 || !(den > 0.0) || !isfinite(den);
+        // thread 0 forms the next scalars from the sums inside the barrier's
+        // last step (every thread holds the same gamma and alpha)
+        auto scalars = [&](double g, double dd) {
+            const double bnew = g / gamma;
+            const double den = dd - bnew * g / alpha;
+            const bool st = g <= tol * tol * gamma0 || !(den > 0.0) || !isfinite(den);
             s_stop = st;
             if (!st) {
                 s_beta = bnew;
-                s_alpha = gn / den;
+                s_alpha = g / den;
                 s_fa = (float)s_alpha;
                 s_fb = (float)bnew;
             }
-        }
-        __syncthreads();
+        };
+        if (!grid_sum2(gn, dn, wk, nblk, round, [&] { load_sums(P ^ 1); }, scalars)) return;
+        ++it;
         gamma = gn;
         if (s_stop) {
             stop = true;

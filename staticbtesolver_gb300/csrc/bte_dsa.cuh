@@ -88,6 +88,12 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
     asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
     return v;
 }
+// Counts the calling block in on a barrier counter: a release at GPU scope,
+// so every write the block made before its last __syncthreads is visible to
+// a block that reads the new count with ld_acquire.
+__device__ __forceinline__ void red_release_add(unsigned* p, unsigned v) {
+    asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
 
 // Block sum of two doubles in a fixed order; valid in thread 0.
 __device__ __forceinline__ void block_sum2(double& a, double& b) {
@@ -134,13 +140,14 @@ __device__ __forceinline__ bool grid_sum2(double& a, double& b, const CgWork& wk
     if (threadIdx.x == 0) {
         __stcg(part + 2 * blockIdx.x, a);
         __stcg(part + 2 * blockIdx.x + 1, b);
-        __threadfence();
-        atomicAdd(wk.bar, 1u);
+        red_release_add(wk.bar, 1u);
         const unsigned target = round * nblk;
         s_ok = 1;
         long long k = 0;
+        // the error flag is read every 64th poll only: a load after the
+        // acquire load waits for it, and would double every poll's latency
         while (ld_acquire(wk.bar) < target) {
-            if (++k > kBarrierPolls || *(volatile int*)(wk.stat + 1)) {
+            if ((++k & 63) == 0 && (k > kBarrierPolls || *(volatile int*)(wk.stat + 1))) {
                 atomicExch(wk.stat + 1, 1);
                 s_ok = 0;
                 break;
@@ -546,12 +553,11 @@ __global__ void __launch_bounds__(1024) k_gj_all(double* A, double* B, int m, un
         __syncthreads();
         if (threadIdx.x == 0) {
             s_abort = 0;
-            __threadfence();
-            atomicAdd(bar, 1u);
+            red_release_add(bar, 1u);
             const unsigned target = (unsigned)(k + 1) * nblk;
             long long polls = 0;
             while (ld_acquire(bar) < target) {
-                if (++polls > kBarrierPolls || *(volatile int*)bad == 2) {
+                if ((++polls & 63) == 0 && (polls > kBarrierPolls || *(volatile int*)bad == 2)) {
                     atomicExch(bad, 2);
                     s_abort = 1;
                     break;
@@ -649,12 +655,11 @@ __global__ void __launch_bounds__(1024) k_gj_block_all(double* A, double* B, int
         }
         if (tid == 0) {
             s_abort = 0;
-            __threadfence();
-            atomicAdd(bar, 1u);
+            red_release_add(bar, 1u);
             const unsigned target = (unsigned)(step + 1) * nblk;
             long long polls = 0;
             while (ld_acquire(bar) < target) {
-                if (++polls > kBarrierPolls || *(volatile int*)bad == 2) {
+                if ((++polls & 63) == 0 && (polls > kBarrierPolls || *(volatile int*)bad == 2)) {
                     atomicExch(bad, 2);
                     s_abort = 1;
                     break;

@@ -82,7 +82,8 @@ typedef struct bte_options {
     int accel_every;      /* 1, 2: outer iterations between extrapolations (>= 4);
                              3: Anderson depth (1..8) */
     int keep_history;     /* nonzero: keep T after every outer iteration (bte_get_history) */
-    int dsa;              /* nonzero: diffusion-synthetic acceleration of the outer iteration (below) */
+    int dsa;              /* nonzero: diffusion-synthetic acceleration of the outer iteration (below);
+                             with BTE_FORM_MIXED the inner solves then run to min(inner_tol, 1e-11) */
     double dsa_tol;       /* relative residual of its low-order solve (0: 1e-3) */
     int dsa_maxit;        /* iteration limit of its low-order solve (0: 4000) */
     int plain_cycles;     /* BTE_FORM_PLAIN: 0 or 1 = the reference's semantics (a system stops at

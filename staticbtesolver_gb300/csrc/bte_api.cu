@@ -714,6 +714,8 @@ static bte_status setup_mixed(bte_ctx* ctx) {
 // cells: 0.17-0.29 error reduction per outer iteration.
 constexpr double kDsaBeta = 0.25;
 constexpr int kDsaThreads = bte::dsa::THREADS;
+// Inner tolerance of the mixed form under the correction (at most).
+constexpr double kDsaMixedInnerTol = 1e-11;
 
 // Upload a low-order operator (nb, W as bte_dsa_solve takes them) in its
 // symmetrically scaled form, in a locality order of the cells with the
@@ -1034,9 +1036,10 @@ static int sweep_slots(const bte_ctx* ctx) { return std::max(2, std::min(ctx->pl
 
 // Build the sweep plan for every direction from the device's inflow coefficients.
 // BTE_LEVEL_ORDER=host builds every direction's level order on the host
-// (sweep_order.h) instead of on the device (k_level_order), and
-// BTE_LEVEL_ORDER=global keeps the device's in-degrees in global memory even
-// when they fit in shared memory; the order is the same either way.
+// (sweep_order.h) instead of on the device (k_level_order_smem, or
+// k_level_order when its state does not fit in shared memory), and
+// BTE_LEVEL_ORDER=global takes k_level_order even when it would; the order is
+// the same either way.
 static bool level_order_on_host() {
     const char* v = std::getenv("BTE_LEVEL_ORDER");
     return v && v[0] == 'h';
@@ -1074,25 +1077,32 @@ static bte_status build_sweep_plan(bte_ctx* ctx) {
         BTE_LAUNCHED();
         int smem_max = 0;
         BTE_CUDA(cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device));
-        // frontier capacity: a power of two, two frontiers in at most 128 KB,
-        // next to the in-degree bytes when those fit with room for waves of 4,096
-        const size_t budget = (size_t)smem_max - 1024, deg_bytes = sizeof(int) * (((size_t)n + 3) / 4);
-        auto cap_for = [&](size_t room) {
-            int cap = 1;
-            while (cap < n && (size_t)cap * 2 * 2 * sizeof(int) <= std::min<size_t>(128 * 1024, room)) cap *= 2;
-            return cap;
-        };
-        const bool sdeg =
-            !level_order_global() && deg_bytes < budget && cap_for(budget - deg_bytes) >= std::min(n, 4096);
-        const int cap = sdeg ? cap_for(budget - deg_bytes) : cap_for(budget);
-        const size_t smem = (size_t)2 * cap * sizeof(int) + (sdeg ? deg_bytes : 0);
-        auto kern = sdeg ? bte::k_level_order<true> : bte::k_level_order<false>;
-        if (!sdeg) BTE_CUDA(ctx->lo_indeg.alloc(sizeof(int) * (size_t)ND * n));
-        BTE_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         BTE_CUDA(cudaMemsetAsync(d_small + 2 * ND, 0, sizeof(int), st));
-        kern<<<ND, 1024, smem, st>>>(ctx->lo_mask.as<uint8_t>(), ctx->lo_down.as<int>(), n, F, cap,
-                                     sdeg ? nullptr : ctx->lo_indeg.as<int>(), ctx->lo_perm.as<int>(),
-                                     ctx->lo_lvl.as<int>(), d_small, d_small + ND, d_small + 2 * ND);
+        // the whole state in shared memory when it fits (in-degree bytes and
+        // two cell bitmaps), else the in-degrees in global memory
+        // (and the wave list: up to 8,192 cells, at least 2,048)
+        const size_t smem_state = sizeof(unsigned) * (((size_t)n + 3) / 4 + 2 * (((size_t)n + 31) / 32));
+        const size_t room = (size_t)smem_max - 1024;
+        const int wcap = smem_state < room ? (int)std::min<size_t>({(size_t)8192, (size_t)n, (room - smem_state) / 4}) : 0;
+        if (!level_order_global() && wcap >= std::min(n, 2048)) {
+            const size_t smem = smem_state + sizeof(int) * (size_t)wcap;
+            BTE_CUDA(cudaFuncSetAttribute(bte::k_level_order_smem, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)smem));
+            bte::k_level_order_smem<<<ND, 1024, smem, st>>>(ctx->lo_mask.as<uint8_t>(), ctx->lo_down.as<int>(), n, F,
+                                                            wcap, ctx->lo_perm.as<int>(), ctx->lo_lvl.as<int>(),
+                                                            d_small, d_small + ND, d_small + 2 * ND);
+        } else {
+            // frontier capacity: a power of two, two frontiers in at most 128 KB
+            int cap = 1;
+            while (cap < n && (size_t)cap * 2 * 2 * sizeof(int) <= std::min<size_t>(128 * 1024, smem_max - 1024))
+                cap *= 2;
+            const size_t smem = (size_t)2 * cap * sizeof(int);
+            BTE_CUDA(ctx->lo_indeg.alloc(sizeof(int) * (size_t)ND * n));
+            BTE_CUDA(cudaFuncSetAttribute(bte::k_level_order, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            bte::k_level_order<<<ND, 1024, smem, st>>>(ctx->lo_mask.as<uint8_t>(), ctx->lo_down.as<int>(), n, F, cap,
+                                                       ctx->lo_indeg.as<int>(), ctx->lo_perm.as<int>(),
+                                                       ctx->lo_lvl.as<int>(), d_small, d_small + ND, d_small + 2 * ND);
+        }
         BTE_LAUNCHED();
         BTE_CUDA(cudaMemcpyAsync(small.data(), d_small, sizeof(int) * small.size(), cudaMemcpyDeviceToHost, st));
         BTE_CUDA(cudaStreamSynchronize(st));
@@ -1896,6 +1906,12 @@ extern "C" bte_status bte_solve(bte_ctx* ctx, const bte_options* opts, bte_repor
         return fail(ctx, BTE_ERR_INVALID_ARGUMENT, "bte_solve: bad dsa_tol / dsa_maxit");
     const double dsa_tol = o.dsa_tol > 0 ? o.dsa_tol : 1e-3;
     const int dsa_maxit = o.dsa_maxit > 0 ? o.dsa_maxit : 4000;
+    // The correction amplifies an inner solve's error by up to 1 / (1 - rho),
+    // rho the source iteration's contraction (~1e5 on a 1e-4 m square).  The
+    // mixed form's refinement stops just under inner_tol, and at 1e-9 its
+    // margins then cycle between 1e-2 and 20 on that square; at 1e-11 it
+    // stops in the 9 outer iterations of the FP64 forms.
+    if (o.dsa && o.form == BTE_FORM_MIXED) o.inner_tol = std::min(o.inner_tol, kDsaMixedInnerTol);
     BTE_CUDA(cudaSetDevice(ctx->device));
     bte_report rep;
     std::memset(&rep, 0, sizeof(rep));

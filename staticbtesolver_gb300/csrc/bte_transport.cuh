@@ -910,29 +910,154 @@ __global__ void k_downstream(const uint8_t* __restrict__ mask, const int* __rest
 // direction: Kahn's algorithm in waves (a wave is the cells whose inflow
 // neighbours all lie in earlier waves), each wave sorted by cell index -- the
 // order bte::level_order (sweep_order.h) builds on the host, for acyclic
-// graphs.  The edges come from k_downstream.  Both frontiers live in dynamic
-// shared memory, cap cells each (cap a power of two); with SDEG the
-// remaining in-degrees do too, one byte per cell (a cell has at most F <= 4
-// inflow faces, so a byte never borrows from its neighbour), else in indeg
-// [n_dir][n] in global memory.  Each thread loads the edges of its wave item
-// before the wave is sorted, so the loads overlap the sort.  A direction
-// whose graph has a cycle (status 1: cells left when no cell is free) or a
-// wave wider than cap (status 2) is left to the host.  Outputs: perm[d][pos],
-// lvl[d][0 .. nlev] (level starts, then n), the largest inflow count over
-// all directions in *fmax.
-template <bool SDEG>
+// graphs.  The edges come from k_downstream.
+//
+// k_level_order_smem keeps the whole state in shared memory: the remaining
+// in-degrees, one byte per cell (a cell has at most F <= 4 inflow faces, so a
+// byte never borrows from its neighbour), two bitmaps of cells, the current
+// wave and the next, and the wave's list (cap cells).  Thread t owns a
+// contiguous range of bitmap words, so reading the wave's bits thread by
+// thread, in bit order, lists it by cell index: after one block scan of the
+// threads' counts each thread writes its cells' positions and list entries,
+// then one thread per wave cell releases its downstream cells into the other
+// bitmap.  Four block barriers per wave; a wave wider than cap sets status 2.
+// Dynamic shared memory: 4 (ceil(n / 4) + 2 ceil(n / 32) + cap) bytes.
+// Outputs: perm[d][pos], lvl[d][0 .. nlev] (level starts, then n), the
+// largest inflow count over all directions in *fmax; status 1: a cycle (cells
+// left when no cell is free) or 2 (a wave wider than cap), the direction is
+// left to the host.
+__global__ void __launch_bounds__(1024) k_level_order_smem(const uint8_t* __restrict__ mask,
+                                                           const int* __restrict__ down, int n, int F, int cap,
+                                                           int* __restrict__ perm, int* __restrict__ lvl,
+                                                           int* __restrict__ nlev, int* __restrict__ status,
+                                                           int* __restrict__ fmax) {
+    extern __shared__ unsigned sw[];
+    const int nd = (n + 3) / 4, nw = (n + 31) / 32;
+    unsigned* deg = sw;         // [nd], 4 cells per word
+    unsigned* bmA = sw + nd;    // [nw]
+    unsigned* bmB = bmA + nw;   // [nw]
+    int* wave = reinterpret_cast<int*>(bmB + nw);  // [cap] the wave's cells in order
+    __shared__ int wsum[32];
+    const int d = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int nwarps = (int)(blockDim.x >> 5);
+    const uint8_t* md = mask + (size_t)d * n;
+    const int* dd = down + (size_t)d * n * F;
+    int* pd = perm + (size_t)d * n;
+    int* ld = lvl + (size_t)d * (n + 1);
+    int fm = 0;
+    for (int w = tid; w < nd; w += blockDim.x) {
+        unsigned word = 0;
+        for (int q = 0; q < 4 && 4 * w + q < n; ++q) {
+            const int k = __popc((unsigned)md[4 * w + q]);
+            word |= (unsigned)k << (8 * q);
+            fm = max(fm, k);
+        }
+        deg[w] = word;
+    }
+    for (int w = tid; w < nw; w += blockDim.x) {
+        unsigned bits = 0;
+        for (int b = 0; b < 32 && 32 * w + b < n; ++b)
+            if (md[32 * w + b] == 0) bits |= 1u << b;
+        bmA[w] = bits;
+        bmB[w] = 0u;
+    }
+    if (fm > 0) atomicMax(fmax, fm);
+    __syncthreads();
+    const int per = (nw + (int)blockDim.x - 1) / (int)blockDim.x;
+    const int w0 = min(nw, tid * per), w1 = min(nw, w0 + per);
+    unsigned* cur = bmA;
+    unsigned* nxt = bmB;
+    int pos = 0, level = 0;
+    bool over = false;
+    for (;;) {
+        // block exclusive scan of the threads' wave-cell counts, in thread order
+        int cnt = 0;
+        for (int w = w0; w < w1; ++w) cnt += __popc(cur[w]);
+        int x = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) wsum[warp] = x;
+        __syncthreads();
+        if (warp == 0) {
+            int v = lane < nwarps ? wsum[lane] : 0;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, v, o);
+                if (lane >= o) v += y;
+            }
+            wsum[lane] = v;
+        }
+        __syncthreads();
+        const int total = wsum[nwarps - 1];
+        if (total == 0 || total > cap) {
+            over = total > cap;
+            break;
+        }
+        // the wave's cells, by cell index, into its positions and the list
+        int o = x - cnt + (warp > 0 ? wsum[warp - 1] : 0);
+        for (int w = w0; w < w1; ++w) {
+            unsigned bits = cur[w];
+            while (bits) {
+                const int u = 32 * w + __ffs(bits) - 1;
+                bits &= bits - 1;
+                pd[pos + o] = u;
+                wave[o++] = u;
+            }
+            cur[w] = 0u;
+        }
+        if (tid == 0) ld[level] = pos;
+        __syncthreads();
+        // release the downstream cells, one wave cell per thread
+        for (int i = tid; i < total; i += blockDim.x) {
+            const int u = wave[i];
+            int e[4];
+#pragma unroll
+            for (int f = 0; f < 4; ++f) e[f] = f < F ? dd[(size_t)u * F + f] : -1;
+#pragma unroll
+            for (int f = 0; f < 4; ++f) {
+                if (e[f] < 0) continue;
+                const int c = e[f] & 0x0fffffff, k = e[f] >> 28;
+                const unsigned sh = 8u * (unsigned)(c & 3);
+                const unsigned old = atomicSub(&deg[c >> 2], (unsigned)k << sh);
+                if (((old >> sh) & 0xffu) == (unsigned)k) atomicOr(&nxt[c >> 5], 1u << (c & 31));
+            }
+        }
+        pos += total;
+        ++level;
+        unsigned* t = cur;
+        cur = nxt;
+        nxt = t;
+        __syncthreads();
+    }
+    if (tid == 0) {
+        const int stat = over ? 2 : (pos < n ? 1 : 0);
+        status[d] = stat;
+        nlev[d] = level;
+        if (stat == 0) ld[level] = n;
+    }
+}
+
+// k_level_order keeps the in-degrees in global memory, indeg [n_dir][n], for
+// meshes whose state does not fit in shared memory: both frontiers live in
+// dynamic shared memory, cap cells each (cap a power of two), each wave is
+// sorted there (bitonic), and a wave wider than cap sets status 2 (the
+// direction is left to the host).  Each thread loads the edges of its wave
+// item before the wave is sorted, so the loads overlap the sort.  Outputs
+// as k_level_order_smem's.
 __global__ void __launch_bounds__(1024) k_level_order(const uint8_t* __restrict__ mask, const int* __restrict__ down,
                                                       int n, int F, int cap, int* __restrict__ indeg,
                                                       int* __restrict__ perm, int* __restrict__ lvl,
                                                       int* __restrict__ nlev, int* __restrict__ status,
                                                       int* __restrict__ fmax) {
-    extern __shared__ int fr[];  // [2][cap], then with SDEG [ceil(n / 4)] words of in-degrees
-    unsigned* sdeg = reinterpret_cast<unsigned*>(fr + 2 * (size_t)cap);
+    extern __shared__ int fr[];  // [2][cap]
     __shared__ int cnt[2];
     __shared__ int s_over;
     const int d = blockIdx.x;
     const uint8_t* md = mask + (size_t)d * n;
-    int* ind = SDEG ? nullptr : indeg + (size_t)d * n;
+    int* ind = indeg + (size_t)d * n;
     const int* dd = down + (size_t)d * n * F;
     int* pd = perm + (size_t)d * n;
     int* ld = lvl + (size_t)d * (n + 1);
@@ -951,22 +1076,10 @@ __global__ void __launch_bounds__(1024) k_level_order(const uint8_t* __restrict_
             else s_over = 1;
         }
     };
-    if (SDEG) {
-        for (int w = threadIdx.x; w < (n + 3) / 4; w += blockDim.x) {
-            unsigned word = 0;
-            for (int q = 0; q < 4 && 4 * w + q < n; ++q) {
-                const int k = __popc((unsigned)md[4 * w + q]);
-                word |= (unsigned)k << (8 * q);
-                seed(4 * w + q, k);
-            }
-            sdeg[w] = word;
-        }
-    } else {
-        for (int c = threadIdx.x; c < n; c += blockDim.x) {
-            const int k = __popc((unsigned)md[c]);
-            ind[c] = k;
-            seed(c, k);
-        }
+    for (int c = threadIdx.x; c < n; c += blockDim.x) {
+        const int k = __popc((unsigned)md[c]);
+        ind[c] = k;
+        seed(c, k);
     }
     if (fm > 0) atomicMax(fmax, fm);
     __syncthreads();
@@ -1035,15 +1148,7 @@ __global__ void __launch_bounds__(1024) k_level_order(const uint8_t* __restrict_
         auto relax = [&](int e) {
             if (e < 0) return;
             const int c = e & 0x0fffffff, k = e >> 28;
-            bool freed;
-            if (SDEG) {
-                const unsigned sh = 8u * (unsigned)(c & 3);
-                const unsigned old = atomicSub(&sdeg[c >> 2], (unsigned)k << sh);
-                freed = ((old >> sh) & 0xffu) == (unsigned)k;
-            } else {
-                freed = atomicSub(&ind[c], k) == k;
-            }
-            if (freed) {
+            if (atomicSub(&ind[c], k) == k) {
                 const int slot = atomicAdd(&cnt[cur ^ 1], 1);
                 if (slot < cap) b[slot] = c;
                 else s_over = 1;

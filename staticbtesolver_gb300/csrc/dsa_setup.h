@@ -66,68 +66,61 @@ inline void dsa_coefficients(int dim, int n, int F, const int* nbr, const double
         gabs *= 0.5;
         return area[(size_t)c * F + f] / solid_angle * (gabs * a1 + beta * a2 * q / delta);
     };
-    // each stored face's coefficient (the expensive part: a sum over the
-    // directions) in parallel, then the scatter in cell order
-    std::vector<double> wv((size_t)n * F, 0.0);
-    auto stored = [&](int c, int f, double* delta) -> bool {
-        const size_t cf = (size_t)c * F + f;
-        const int o = nbr[cf];
-        const double A = area[cf];
-        if (!(A > 0.0)) return false;
-        if (o < 0 || o >= n) {
-            if (!(o < 0 && dirichlet[cf])) return false;
-            *delta = hfac * volume[c] / A;
-            return true;
-        }
-        if (o <= c) return false;  // evaluated once, from the lower-numbered cell
-        *delta = hfac * (volume[c] + volume[o]) / A;
-        return true;
-    };
-    {
-        const int nth = std::max(1, std::min(16, (int)std::thread::hardware_concurrency()));
-        const int T = std::max(1, std::min(nth, n / 8192));
-        auto run = [&](int t) {
-            for (int c = t; c < n; c += T)
-                for (int f = 0; f < F; ++f) {
-                    double delta = 0.0;
-                    if (stored(c, f, &delta)) wv[(size_t)c * F + f] = coefficient(c, f, delta);
+    // Each stored face's coefficient (the expensive part: a sum over the
+    // directions) and its two slots, cells split over host threads.  A face
+    // between c and o > c is stored by c: its own slot (c, f) and the mirror
+    // slot (o, back), back the first face of o that names c; no other face
+    // writes either slot (a second face of c naming o, on a degenerate mesh,
+    // rewrites the same mirror on the same thread), so the threads never
+    // share one.  The diagonal is then each cell's slots summed in face order.
+    const int nth = std::max(1, std::min(16, (int)std::thread::hardware_concurrency()));
+    const int T = std::max(1, std::min(nth, n / 8192));
+    std::vector<int> fixed_count(T, 0);
+    auto run = [&](int t) {
+        for (int c = t; c < n; c += T)
+            for (int f = 0; f < F; ++f) {
+                const size_t cf = (size_t)c * F + f;
+                const int o = nbr[cf];
+                const double A = area[cf];
+                if (!(A > 0.0)) continue;
+                if (o < 0 || o >= n) {
+                    if (o < 0 && dirichlet[cf]) {
+                        out.W[(size_t)f * n + c] = coefficient(c, f, hfac * volume[c] / A);
+                        ++fixed_count[t];
+                    }
+                    continue;
                 }
-        };
-        if (T == 1) run(0);
-        else {
-            std::vector<std::thread> pool;
-            for (int t = 0; t < T; ++t) pool.emplace_back(run, t);
-            for (auto& th : pool) th.join();
-        }
-    }
-    for (int c = 0; c < n; ++c)
-        for (int f = 0; f < F; ++f) {
-            const size_t cf = (size_t)c * F + f;
-            const int o = nbr[cf];
-            const double A = area[cf];
-            if (!(A > 0.0)) continue;
-            if (o < 0 || o >= n) {
-                if (o < 0 && dirichlet[cf]) {
-                    const double w = wv[cf];
-                    out.W[(size_t)f * n + c] = w;
-                    out.diag[c] += w;
-                    ++out.n_dirichlet;
-                }
-                continue;
+                if (o <= c) continue;  // evaluated once, from the lower-numbered cell
+                int back = -1;
+                for (int g = 0; g < F; ++g)
+                    if (nbr[(size_t)o * F + g] == c) { back = g; break; }
+                if (back < 0) continue;  // a one-sided link (no face of o names c): left out
+                const double w = coefficient(c, f, hfac * (volume[c] + volume[o]) / A);
+                out.W[(size_t)f * n + c] = w;
+                out.nb[(size_t)f * n + c] = o;
+                out.W[(size_t)back * n + o] = w;
+                out.nb[(size_t)back * n + o] = c;
             }
-            if (o <= c) continue;  // evaluated once, from the lower-numbered cell
-            int back = -1;
-            for (int g = 0; g < F; ++g)
-                if (nbr[(size_t)o * F + g] == c) { back = g; break; }
-            if (back < 0) continue;  // a one-sided link (no face of o names c): left out
-            const double w = wv[cf];
-            out.W[(size_t)f * n + c] = w;
-            out.nb[(size_t)f * n + c] = o;
-            out.W[(size_t)back * n + o] = w;
-            out.nb[(size_t)back * n + o] = c;
-            out.diag[c] += w;
-            out.diag[o] += w;
+    };
+    auto diag = [&](int t) {
+        for (int c = t; c < n; c += T) {
+            double sum = 0.0;
+            for (int f = 0; f < F; ++f) sum += out.W[(size_t)f * n + c];
+            out.diag[c] = sum;
         }
+    };
+    if (T == 1) {
+        run(0);
+        diag(0);
+    } else {
+        std::vector<std::thread> pool;
+        for (int t = 0; t < T; ++t) pool.emplace_back(run, t);
+        for (auto& th : pool) th.join();
+        pool.clear();
+        for (int t = 0; t < T; ++t) pool.emplace_back(diag, t);
+        for (auto& th : pool) th.join();
+    }
+    for (int k : fixed_count) out.n_dirichlet += k;
 }
 
 // ---------------------------------------------------------------------------

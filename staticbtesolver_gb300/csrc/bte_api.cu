@@ -1025,10 +1025,25 @@ static bte_status setup_dsa_device(bte_ctx* ctx, DsaSetupHost& h, cudaStream_t s
     if (h.n_dirichlet > 0) {
         bte_status s = dsa_upload(ctx, h.hp, st);
         if (s != BTE_OK) return s;
-        BTE_CUDA(ctx->d_Tsrc.alloc(sizeof(double) * ctx->Np));
         BTE_CUDA(cudaStreamSynchronize(st));
     }
     return BTE_OK;
+}
+
+// The wall faces held at a fixed temperature that the low-order operator
+// couples to (setup_dsa_host's count, without the coefficients): known
+// before its set-up ends, so the solve can start while it runs.
+static int dsa_wall_faces(const bte_ctx* ctx) {
+    int count = 0;
+    for (size_t cf = 0; cf < (size_t)ctx->n * ctx->F; ++cf) {
+        const int code = ctx->nbr[cf];
+        if (code >= 0 || !(ctx->area[cf] > 0.0)) continue;
+        int row = -1;
+        for (int i = 0; i < ctx->n_bc; ++i)
+            if (ctx->bc_index[i] == code) { row = i; break; }
+        count += row < 0 || ctx->bc_type[row] == 1;
+    }
+    return count;
 }
 
 // Face slots the sweep is instantiated for (2 in 1D and 2D, 3 in 3D).
@@ -1978,14 +1993,29 @@ extern "C" bte_status bte_solve(bte_ctx* ctx, const bte_options* opts, bte_repor
         bte_status s = setup_mixed(ctx);
         if (s != BTE_OK) return s;
     }
-    if (need_dsa) {
-        if (dsa_thread.joinable()) dsa_thread.join();
+    // The low-order set-up on its thread may still run: the solve starts, and
+    // the thread is joined before the first correction (after the first
+    // outer iteration), or after the loop.  Its device part is complete when
+    // it returns (it synchronises its stream).
+    bool dsa_pending = dsa_thread.joinable();
+    auto join_dsa = [&]() -> bte_status {
+        if (!dsa_pending) return BTE_OK;
+        dsa_thread.join();
+        dsa_pending = false;
+        rep.ms_host_dsa = since(t_dsa);  // (overlaps the plan's time and the first iteration's)
         if (dsa_status != BTE_OK) return dsa_status;
         ctx->dsa_ready = true;
-        rep.ms_host_dsa = since(t_dsa);  // (overlaps the plan's time when both were built)
+        return BTE_OK;
+    };
+    if (need_dsa && !dsa_pending) {
+        if (dsa_status != BTE_OK) return dsa_status;
+        ctx->dsa_ready = true;
+        rep.ms_host_dsa = since(t_dsa);
     }
     // without a wall held at a fixed temperature the low-order operator is singular: dsa is ignored
-    const bool dsa_on = o.dsa && ctx->dsa_walls > 0;
+    const int dsa_walls = dsa_pending ? dsa_wall_faces(ctx) : ctx->dsa_walls;
+    const bool dsa_on = o.dsa && dsa_walls > 0;
+    if (dsa_on) BTE_CUDA(ctx->d_Tsrc.alloc(sizeof(double) * ctx->Np));
     cudaStream_t st = ctx->stream;
     const int NB = ctx->n_band, ND = ctx->n_dir;
     const size_t Np = ctx->Np;
@@ -1997,7 +2027,8 @@ extern "C" bte_status bte_solve(bte_ctx* ctx, const bte_options* opts, bte_repor
         // the source of the first outer iteration is ebar = 0, i.e. T = T_ref
         bte::dsa::k_fill<<<(unsigned)((Np + 255) / 256), 256, 0, st>>>(ctx->d_T.as<double>(), ctx->T_ref, (int)Np);
         BTE_LAUNCHED();
-        BTE_CUDA(cudaMemsetAsync(ctx->cg_stat.p, 0, sizeof(int) * 4, st));
+        // (the low-order work memory exists once its set-up is joined)
+        if (!dsa_pending) BTE_CUDA(cudaMemsetAsync(ctx->cg_stat.p, 0, sizeof(int) * 4, st));
     }
     ctx->margins.clear();
     double Lr_sum = 0;
@@ -2254,6 +2285,13 @@ extern "C" bte_status bte_solve(bte_ctx* ctx, const bte_options* opts, bte_repor
             // this iteration's change, then T += x (and ebar, and the boundary
             // cells' intensities the walls reflect next)
             const int n = ctx->n;
+            if (dsa_pending) {
+                bte_status js = join_dsa();
+                if (js != BTE_OK) return js;
+                if (ctx->dsa_walls != dsa_walls)
+                    return fail(ctx, BTE_ERR_STATE, "dsa: the set-up found another count of fixed-temperature faces");
+                BTE_CUDA(cudaMemsetAsync(ctx->cg_stat.p, 0, sizeof(int) * 4, st));
+            }
             BTE_CUDA(cudaEventRecord(ev[7], st));
             BTE_LAUNCH(KK_DSA, -1, 3.0 * n * 8.0, 0,
                        bte::dsa::k_dsa_rhs<<<(n + 255) / 256, 256, 0, st>>>(
@@ -2332,6 +2370,8 @@ extern "C" bte_status bte_solve(bte_ctx* ctx, const bte_options* opts, bte_repor
         BTE_CUDA(cudaEventSynchronize(ev[6]));
         add_accel_time();
     }
+    // a low-order set-up that no correction needed (the solve stopped first)
+    if (dsa_pending) (void)join_dsa();
     if (o.max_iter == 0) result = BTE_OK;
     // heat flux (src/StaticBTESolver.cpp:323-370)
     if (ctx->nbf > 0) {
@@ -2346,7 +2386,8 @@ extern "C" bte_status bte_solve(bte_ctx* ctx, const bte_options* opts, bte_repor
                                         ctx->n_bc, ctx->dim, ctx->d_qband.as<double>(), ctx->d_q.as<double>());
     BTE_LAUNCHED();
     int dsa_stat[4] = {0, 0, 0, 0};
-    if (dsa_on) BTE_CUDA(cudaMemcpyAsync(dsa_stat, ctx->cg_stat.p, sizeof(dsa_stat), cudaMemcpyDeviceToHost, st));
+    if (dsa_on && rep.dsa_solves > 0)
+        BTE_CUDA(cudaMemcpyAsync(dsa_stat, ctx->cg_stat.p, sizeof(dsa_stat), cudaMemcpyDeviceToHost, st));
     int sweep_err = 0;
     if (o.form == BTE_FORM_SWEEP && ctx->d_sweep_err.p)
         BTE_CUDA(cudaMemcpyAsync(&sweep_err, ctx->d_sweep_err.p, sizeof(int), cudaMemcpyDeviceToHost, st));

@@ -12,7 +12,9 @@ Meshes are on the unit square / unit cube; the physical size comes from the
 * 2D: a jittered (n+1) x (n+1) point grid (interior points moved by
   U(-j, j) h in x and y, edge points slide along their edge, corners fixed),
   triangulated and then made Delaunay by Lawson edge flips.  Boundary
-  entities 0..3 = left, bottom, right, top.
+  entities 0..3 = left, bottom, right, top; optional circular pores (the
+  triangles whose centroid lies inside are removed), whose walls are
+  entity 4.
 * 3D: a jittered (n+1)^3 lattice, each cube split into the 6 Kuhn tetrahedra
   (conforming across cubes), with a positive-volume guard; optional
   cylindrical pore along z (cells whose centroid lies inside are removed and
@@ -143,11 +145,13 @@ def _morton_order(xy: np.ndarray, bits: int = 16) -> np.ndarray:
     return np.argsort(code, kind="stable")
 
 
-def square_mesh(n: int, jitter: float = 0.3, seed: int = 20261203, delaunay: bool = True):
+def square_mesh(n: int, jitter: float = 0.3, seed: int = 20261203, delaunay: bool = True, pores=()):
     """Jittered (n+1)^2 grid on [0,1]^2, Delaunay-triangulated (2 n^2 triangles).
 
     delaunay=False keeps the first valid diagonal of every quad instead (a valid
-    triangulation whose upwind graphs may contain cycles)."""
+    triangulation whose upwind graphs may contain cycles).  pores: circles
+    (cx, cy, r) in unit coordinates; triangles whose centroid lies inside one
+    are removed and the edges they leave open form entity 4."""
     rng = np.random.default_rng(seed)
     h = 1.0 / n
     ii, jj = np.meshgrid(np.arange(n + 1), np.arange(n + 1), indexing="ij")
@@ -182,6 +186,12 @@ def square_mesh(n: int, jitter: float = 0.3, seed: int = 20261203, delaunay: boo
         k = int(np.argmin(r))
         out.append(r[k:] + r[:k])
     tris = np.array(out, dtype=np.int64)
+    if len(pores):
+        cen = P[tris].mean(axis=1)
+        keep = np.ones(len(tris), dtype=bool)
+        for cx, cy, r in pores:
+            keep &= (cen[:, 0] - cx) ** 2 + (cen[:, 1] - cy) ** 2 > r ** 2
+        tris = tris[keep]
     tris = tris[_morton_order(P[tris].mean(axis=1))]
     segs, ents = [], []
     for j in range(n):  # left x=0
@@ -192,6 +202,19 @@ def square_mesh(n: int, jitter: float = 0.3, seed: int = 20261203, delaunay: boo
         segs.append([pid(n, j), pid(n, j + 1)]); ents.append(2)
     for i in range(n):  # top y=1
         segs.append([pid(i, n), pid(i + 1, n)]); ents.append(3)
+    if len(pores):
+        # pore walls: interior edges left with one triangle, in sorted order
+        E = np.sort(np.concatenate([tris[:, [0, 1]], tris[:, [1, 2]], tris[:, [2, 0]]]), axis=1)
+        uniq, cnt = np.unique(E, axis=0, return_counts=True)
+        outer = {tuple(sorted(s_)) for s_ in segs}
+        for e in uniq[cnt == 1]:
+            if tuple(e) not in outer:
+                segs.append([int(e[0]), int(e[1])]); ents.append(4)
+        used = np.unique(tris.ravel())
+        remap = -np.ones(len(P), dtype=np.int64)
+        remap[used] = np.arange(len(used))
+        segs = remap[np.array(segs)]
+        return dict(dim=2, points=P[used], tri=remap[tris], seg=segs, seg_ent=np.array(ents))
     return dict(dim=2, points=P, tri=tris, seg=np.array(segs), seg_ent=np.array(ents))
 
 
@@ -339,6 +362,8 @@ def make_problem(name: str, out_dir: str, seed: int = 20261203) -> Problem:
       square100k        2D square 1e-4 m (diffusive), 2 x 224^2 triangles, 32 directions, 20 bands.
       cube1m            3D cube 1e-6 m, 6 x 55^3 tetrahedra minus a cylindrical pore of
                         radius 0.2 (diffuse wall), 128 directions, 40 bands.
+      squarepores       2D square 1e-6 m, 2 x 48^2 triangles minus three circular pores
+                        (diffuse walls, entity 4), 32 directions, 8 bands.
       square<N>_b<B>    2D square 1e-7 m with 2 N^2 triangles and B bands (small parity cases).
       cube<N>_b<B>      3D cube 1e-8 m with 6 N^3 tetrahedra and B bands.
       nondelaunay<N>_b<B>  as square<N>_b<B> without the Delaunay edge flips.
@@ -348,8 +373,8 @@ def make_problem(name: str, out_dir: str, seed: int = 20261203) -> Problem:
     band_file = os.path.join(out_dir, f"{name}.band.dat")
     bc_file = os.path.join(out_dir, f"{name}.bc.dat")
 
-    def square(n, n_band, side, bc_rows=None, delaunay=True):
-        write_mphtxt(geo, square_mesh(n, seed=seed, delaunay=delaunay))
+    def square(n, n_band, side, bc_rows=None, delaunay=True, pores=()):
+        write_mphtxt(geo, square_mesh(n, seed=seed, delaunay=delaunay, pores=pores))
         write_band_file(band_file, debye_bands(n_band))
         write_bc_file(bc_file, bc_rows or [(0, 1, 301.0), (1, 2, 300.0), (2, 1, 299.0), (3, 2, 300.0)])
         return Problem(name, geo, band_file, bc_file, 2, 8, 8, 300.0, 1000, side, side, 0.0)
@@ -377,6 +402,12 @@ def make_problem(name: str, out_dir: str, seed: int = 20261203) -> Problem:
         return p
     if name == "cube1m":
         return cube(55, 40, 1e-6, pore=0.2)
+    if name == "squarepores":
+        # three pores with diffuse walls in a 1e-6 m square (the moderately
+        # diffusive regime), 2 x 48^2 triangles before the pores, 8 bands
+        pores = ((0.3, 0.3, 0.12), (0.68, 0.42, 0.15), (0.4, 0.75, 0.1))
+        return square(48, 8, 1e-6, pores=pores,
+                      bc_rows=[(0, 1, 301.0), (1, 2, 300.0), (2, 1, 299.0), (3, 2, 300.0), (4, 2, 300.0)])
     if name.startswith("nondelaunay") and "_b" in name:
         n, b = name[len("nondelaunay"):].split("_b")
         return square(int(n), int(b), 1e-7, delaunay=False)

@@ -13,8 +13,11 @@ checked against it:
     oracle restatement reaches the iteration's limit through oracle/dsa.py
     (its own outer iterations interleaved with a SciPy diffusion correction)
     -> T_fixed, certified by one more uncorrected oracle step.
+  * squarepores: the same on a 1e-6 m square with three circular pores
+    (synth.make_problem("squarepores"): 3,925 triangles, pore walls diffuse,
+    entity 4), a non-convex domain with inner walls.
 
-Usage:  python tests/golden/diffusive/make_diffusive.py
+Usage:  python tests/golden/diffusive/make_diffusive.py [name ...]
 """
 from __future__ import annotations
 
@@ -33,16 +36,19 @@ from oracle import dsa as D  # noqa: E402
 from oracle import oracle as O  # noqa: E402
 from staticbtesolver_gb300 import synth  # noqa: E402
 
-CASES = {"square12_b8": dict(n=12, bands=8, side=1e-6)}
+WALLS = [(0, 1, 301.0), (1, 2, 300.0), (2, 1, 299.0), (3, 2, 300.0)]
+PORES = ((0.3, 0.3, 0.12), (0.68, 0.42, 0.15), (0.4, 0.75, 0.1))  # as synth's squarepores
+CASES = {"square12_b8": dict(n=12, bands=8, side=1e-6),
+         "squarepores": dict(n=48, bands=8, side=1e-6, pores=PORES, rows=WALLS + [(4, 2, 300.0)])}
 
 
-def make(name, n, bands, side):
+def make(name, n, bands, side, pores=(), rows=WALLS):
     d = os.path.join(HERE, name)
     os.makedirs(d, exist_ok=True)
     geo = os.path.join(d, "mesh.mphtxt")
-    synth.write_mphtxt(geo, synth.square_mesh(n))
+    synth.write_mphtxt(geo, synth.square_mesh(n, pores=pores))
     synth.write_band_file(os.path.join(d, "band.dat"), synth.debye_bands(bands))
-    synth.write_bc_file(os.path.join(d, "inputbc.dat"), [(0, 1, 301.0), (1, 2, 300.0), (2, 1, 299.0), (3, 2, 300.0)])
+    synth.write_bc_file(os.path.join(d, "inputbc.dat"), rows)
     args = (geo, os.path.join(d, "inputbc.dat"), os.path.join(d, "band.dat"), 2, 8, 8, 300.0, side, side, 0.0)
     o = O.Oracle(*args)
     t0 = time.time()
@@ -72,6 +78,8 @@ def make(name, n, bands, side):
 def main():
     O.build()
     for name, kw in CASES.items():
+        if len(sys.argv) > 1 and name not in sys.argv[1:]:
+            continue
         make(name, **kw)
 
 

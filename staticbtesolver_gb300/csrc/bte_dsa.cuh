@@ -15,7 +15,8 @@
 // conjugate gradients in the Chronopoulos-Gear form on the symmetrically
 // Jacobi-scaled operator (unit diagonal), with a two-level preconditioner
 // (the identity plus a coarse correction on aggregates of cells), FP32
-// vectors, FP64 dot products, and one grid barrier per iteration, which also
+// vectors, dot products summed in FP64 over the block and the grid (each
+// thread's one or two cells in FP32), and one grid barrier per iteration, which also
 // completes the iteration's two dot products.  One barrier suffices because r,
 // w = A u and s are kept in two parity copies: after a barrier every block
 // recomputes the new residual of its cells' neighbours from the previous
@@ -351,6 +352,7 @@ __global__ void __launch_bounds__(THREADS) k_dsa_pcg(Lo lo, Coarse co, CgWork wk
     __syncthreads();
     float* pub = co.sums;  // parity 0
     double gamma = 0.0, delta = 0.0;
+    float gp = 0.0f, dp = 0.0f;  // a thread's partial dot products (its one or two cells), FP32
     {
         float acc[AGG][3] = {};
         for (int c = c_lo + threadIdx.x; c < c_hi; c += blockDim.x) {
@@ -369,8 +371,8 @@ __global__ void __launch_bounds__(THREADS) k_dsa_pcg(Lo lo, Coarse co, CgWork wk
             wk.u[c] = uc;
             wk.x[c] = 0.0f;
             wk.p[c] = 0.0f;
-            gamma = fma((double)rc, (double)uc, gamma);
-            delta = fma((double)wc, (double)uc, delta);
+            gp = __fmaf_rn(rc, uc, gp);
+            dp = __fmaf_rn(wc, uc, dp);
             const int a = (c - c_lo) / co.seg;
 #pragma unroll
             for (int k = 0; k < AGG; ++k)
@@ -378,6 +380,8 @@ __global__ void __launch_bounds__(THREADS) k_dsa_pcg(Lo lo, Coarse co, CgWork wk
         }
         const float t = block_sum_aggs(acc, red);
         if (threadIdx.x < 3 * AGG) __stcg(pub + (size_t)3 * K0 + threadIdx.x, t);
+        gamma = gp;
+        delta = dp;
     }
     // the aggregate sums (r, A u, s) published before a barrier, loaded into
     // registers as soon as the barrier is passed (aggregates threadIdx.x +
@@ -425,7 +429,7 @@ __global__ void __launch_bounds__(THREADS) k_dsa_pcg(Lo lo, Coarse co, CgWork wk
         __syncthreads();
         coarse_rows(co, sA, sR, sX);
         __syncthreads();
-        double gn = 0.0, dn = 0.0;
+        float gq = 0.0f, dq = 0.0f;
         float acc[AGG][3] = {};
         for (int c = c_lo + threadIdx.x; c < c_hi; c += blockDim.x) {
             const float so = __ldcg(wk.s + (size_t)(P ^ 1) * n + c);
@@ -449,8 +453,8 @@ __global__ void __launch_bounds__(THREADS) k_dsa_pcg(Lo lo, Coarse co, CgWork wk
             __stcg(wk.r + (size_t)(P ^ 1) * n + c, rn);
             __stcg(wk.aw + (size_t)(P ^ 1) * n + c, wn);
             wk.u[c] = un;
-            gn = fma((double)rn, (double)un, gn);
-            dn = fma((double)wn, (double)un, dn);
+            gq = __fmaf_rn(rn, un, gq);
+            dq = __fmaf_rn(wn, un, dq);
             const int a = ac - K0;
 #pragma unroll
             for (int k = 0; k < AGG; ++k)
@@ -473,6 +477,7 @@ __global__ void __launch_bounds__(THREADS) k_dsa_pcg(Lo lo, Coarse co, CgWork wk
                 s_fb = (float)bnew;
             }
         };
+        double gn = gq, dn = dq;  // summed over the block and the grid in FP64
         if (!grid_sum2(gn, dn, wk, nblk, round, [&] { load_sums(P ^ 1); }, scalars)) return;
         ++it;
         gamma = gn;

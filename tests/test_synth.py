@@ -52,6 +52,33 @@ def test_pore_carving():
     assert len(m["tet"]) < 6 * 8 ** 3
 
 
+def test_square_pores():
+    """Circular pores in the square: positive triangles, every edge shared by
+    two triangles or listed as boundary, each pore wall (entity 4) a closed
+    loop (every wall vertex on exactly two wall edges), no unused point."""
+    pores = ((0.3, 0.3, 0.12), (0.68, 0.42, 0.15), (0.4, 0.75, 0.1))
+    m = synth.square_mesh(48, pores=pores)
+    P, T = m["points"], m["tri"]
+    area = 0.5 * ((P[T[:, 1], 0] - P[T[:, 0], 0]) * (P[T[:, 2], 1] - P[T[:, 0], 1])
+                  - (P[T[:, 1], 1] - P[T[:, 0], 1]) * (P[T[:, 2], 0] - P[T[:, 0], 0]))
+    assert (area > 0).all()
+    holes = sum(np.pi * r * r for _, _, r in pores)
+    assert abs(area.sum() - (1.0 - holes)) < 0.02
+    edges = {}
+    for t in T:
+        for k in range(3):
+            e = tuple(sorted((int(t[k]), int(t[(k + 1) % 3]))))
+            edges[e] = edges.get(e, 0) + 1
+    bnd = {tuple(sorted(map(int, s))) for s in m["seg"]}
+    assert all(n == 2 or (n == 1 and e in bnd) for e, n in edges.items())
+    assert all(edges.get(e) == 1 for e in bnd)
+    wall = m["seg"][m["seg_ent"] == 4]
+    assert len(wall) > 0
+    deg = np.bincount(wall.ravel(), minlength=len(P))
+    assert set(np.unique(deg[deg > 0])) == {2}
+    assert len(np.unique(T.ravel())) == len(P)
+
+
 def test_debye_bands():
     b = synth.debye_bands(40)
     assert abs(b["C"].sum() - 1.627e6) < 1e-6

@@ -391,45 +391,4 @@ inline void dsa_coarse(int n, int F, const int* nb /* [F][n] */, const double* w
     }
 }
 
-// Where each coupling of the low-order operator finds its neighbour when a
-// block keeps its own cells' state in shared memory: src[f][c] = the
-// neighbour's local index (0 .. chunk-1) when it is one of the block's cells,
-// chunk + h when it is the block's halo cell h (halo[halo_ptr[k] + h], a cell
-// of another block), -1 for no coupling.  Halo cells are sorted by index.
-struct DsaHalo {
-    int hmax = 0;                // longest halo of a block
-    std::vector<int> src;        // [F][n]
-    std::vector<int> halo_ptr;   // [nblk+1]
-    std::vector<int> halo;       // permuted cell numbers
-};
-
-inline void dsa_halo(int n, int F, const int* nb /* [F][n] */, int nblk, int chunk, DsaHalo& out) {
-    out.src.assign((size_t)F * n, -1);
-    out.halo_ptr.assign(nblk + 1, 0);
-    out.halo.clear();
-    out.hmax = 0;
-    std::vector<int> slot(n, -1);
-    for (int k = 0; k < nblk; ++k) {
-        const int lo = k * chunk, hi = std::min(n, lo + chunk);
-        std::vector<int> ext;
-        for (int c = lo; c < hi; ++c)
-            for (int f = 0; f < F; ++f) {
-                const int o = nb[(size_t)f * n + c];
-                if (o >= 0 && (o < lo || o >= hi)) ext.push_back(o);
-            }
-        std::sort(ext.begin(), ext.end());
-        ext.erase(std::unique(ext.begin(), ext.end()), ext.end());
-        for (size_t h = 0; h < ext.size(); ++h) slot[ext[h]] = (int)h;
-        for (int c = lo; c < hi; ++c)
-            for (int f = 0; f < F; ++f) {
-                const int o = nb[(size_t)f * n + c];
-                if (o < 0) continue;
-                out.src[(size_t)f * n + c] = (o >= lo && o < hi) ? o - lo : chunk + slot[o];
-            }
-        out.halo.insert(out.halo.end(), ext.begin(), ext.end());
-        out.halo_ptr[k + 1] = (int)out.halo.size();
-        out.hmax = std::max(out.hmax, (int)ext.size());
-    }
-}
-
 }  // namespace bte

@@ -153,13 +153,13 @@ def test_dsa_is_bitwise_reproducible(sbte, tmp_path):
     assert a.report["dsa_iterations"] == b.report["dsa_iterations"] > 0
 
 
-def _diffusive_fixture():
+def _diffusive_fixture(name="square12_b8"):
     import json
     import os
 
     from conftest import GOLDEN
 
-    d = os.path.join(GOLDEN, "diffusive", "square12_b8")
+    d = os.path.join(GOLDEN, "diffusive", name)
     meta = json.load(open(os.path.join(d, "expected.json")))
     ref = dict(np.load(os.path.join(d, "ref.npz")))
     args = (os.path.join(d, "mesh.mphtxt"), os.path.join(d, "inputbc.dat"), os.path.join(d, "band.dat"), meta["DM"],
@@ -167,12 +167,17 @@ def _diffusive_fixture():
     return args, meta, ref
 
 
-def test_dsa_matches_oracle_fixed_point(sbte):
-    """tests/golden/diffusive/square12_b8: the oracle's own outer iterations,
+DIFFUSIVE = ["square12_b8", "squarepores"]
+
+
+@pytest.mark.parametrize("name", DIFFUSIVE)
+def test_dsa_matches_oracle_fixed_point(sbte, name):
+    """tests/golden/diffusive/<name>: the oracle's own outer iterations,
     interleaved with a CPU diffusion correction, reach the iteration's fixed
     point (certified by one more plain oracle step); the GPU's accelerated
-    solve lands on it."""
-    args, meta, ref = _diffusive_fixture()
+    solve lands on it.  squarepores has three circular pores with diffuse
+    walls: inner walls, a non-convex domain, aggregates cut by the pores."""
+    args, meta, ref = _diffusive_fixture(name)
     assert ref["cert_dT"] < 1e-11
     tight = _run(sbte, args, max_iter=200, tol=1e-11, form=sbte.FORM_SWEEP, dsa=True, dsa_tol=1e-4)
     assert tight.report["converged"]
@@ -184,13 +189,14 @@ def test_dsa_matches_oracle_fixed_point(sbte):
     assert rel_l2(std.T - 300.0, ref["T_fixed"] - 300.0) < 1e-5
 
 
-def test_plain_iteration_matches_reference_build_on_long_run(sbte):
+@pytest.mark.parametrize("name", DIFFUSIVE)
+def test_plain_iteration_matches_reference_build_on_long_run(sbte, name):
     """The same fixture run by the reference's own CPU solver: its plain
     iteration stops at margin <= 1e-5 after thousands of outer iterations,
     still ~5e-5 from the fixed point.  The GPU's unaccelerated iteration
     reproduces that run (same count, same field), and the accelerated one is
     closer to the fixed point than the reference's own answer."""
-    args, meta, ref = _diffusive_fixture()
+    args, meta, ref = _diffusive_fixture(name)
     if "T_refbuild" not in ref:
         pytest.skip("fixture made without the reference build")
     n_ref = int(ref["n_iter_refbuild"])
@@ -201,6 +207,20 @@ def test_plain_iteration_matches_reference_build_on_long_run(sbte):
     d_ref = rel_l2(ref["T_refbuild"] - 300.0, ref["T_fixed"] - 300.0)
     acc = _run(sbte, args, max_iter=200, tol=1e-5, form=sbte.FORM_SWEEP, dsa=True)
     assert rel_l2(acc.T - 300.0, ref["T_fixed"] - 300.0) < d_ref
+
+
+@pytest.mark.parametrize("form", ["SWEEP", "PLAIN"])
+def test_porous_square_first_iterations_match_oracle(sbte, form):
+    """tests/golden/diffusive/squarepores: three circular pores with diffuse
+    walls (inner walls, a non-convex domain).  The first five plain outer
+    iterations match the oracle's (its GMRES inner solves stop at 1e-9)."""
+    args, meta, ref = _diffusive_fixture("squarepores")
+    res = _run(sbte, args, max_iter=5, tol=0.0, form=getattr(sbte, "FORM_" + form))
+    assert res.report["n_iter"] == 5
+    assert rel_l2(res.T - 300.0, ref["T_it5"] - 300.0) < 1e-7
+    np.testing.assert_allclose(res.margins, ref["margins_it5"], rtol=1e-6)
+    big = np.abs(ref["q_it5"]) > 1e-3 * np.abs(ref["q_it5"]).max()
+    np.testing.assert_allclose(res.q[big], ref["q_it5"][big], rtol=1e-6)
 
 
 def test_square100k_reaches_oracle_fixed_point(sbte, tmp_path):

@@ -713,6 +713,14 @@ static bte_status setup_mixed(bte_ctx* ctx) {
 // on 2D squares from thick (Lambda/h ~ 1e-3) to mixed (Lambda/h up to ~8)
 // cells: 0.17-0.29 error reduction per outer iteration.
 constexpr double kDsaBeta = 0.25;
+// BTE_DSA_BETA=x replaces it (a study of the low-order operator; the
+// transport iteration and its fixed point do not depend on it).
+static double dsa_beta() {
+    const char* v = std::getenv("BTE_DSA_BETA");
+    if (!v || !*v) return kDsaBeta;
+    const double b = std::atof(v);
+    return b >= 0.0 && std::isfinite(b) ? b : kDsaBeta;
+}
 constexpr int kDsaThreads = bte::dsa::THREADS;
 // Inner tolerance of the mixed form under the correction (at most).
 constexpr double kDsaMixedInnerTol = 1e-11;
@@ -1010,7 +1018,7 @@ static void setup_dsa_host(const bte_ctx* ctx, int nblk, DsaSetupHost& out) {
     bte::DsaCoefficients co;
     bte::dsa_coefficients(ctx->dim, n, F, ctx->nbr.data(), ctx->area.data(), ctx->normal.data(), ctx->volume.data(),
                           ctx->n_dir, ctx->s.data(), ctx->S.data(), ctx->solid_angle, ctx->n_band, ctx->vg.data(),
-                          ctx->tau.data(), ctx->Lr.data(), fixed, kDsaBeta, co);
+                          ctx->tau.data(), ctx->Lr.data(), fixed, dsa_beta(), co);
     tm.lap("coefficients");
     order_thread.join();
     tm.lap("locality order (joined)");

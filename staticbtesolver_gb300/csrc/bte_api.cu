@@ -78,11 +78,10 @@ struct SweepShape {
     int G = 2, threads = 128, W = 2048;
     size_t smem = 0;
     bool margin = false;  // acyclic plans: the sweep sums the margin partials (else k_reduce does)
-    bool staged = false;  // k_sweep_staged (right-hand side from k_sweep_src, levels staged by bulk copies)
+    bool staged = false;  // k_sweep_staged (levels staged by bulk copies, right-hand side formed a stage ahead)
     bool split = false;   // k_sweep over the levels split into slices of cap positions (one per thread)
     int cap = 0;          // staged, split: positions per stage
     int kind() const { return staged ? 1 : split ? 2 : 0; }
-    bool prepass() const { return staged; }  // needs k_sweep_src's right-hand side
 };
 
 // Stage bounds of the staged sweep for one stage width: per direction, its
@@ -149,7 +148,7 @@ struct bte_ctx {
     DevBuf d_bcell, d_bidx, d_bsum;
     // staged sweep: plan records, level-ordered right-hand side of a batch,
     // error flag of its bounded waits, stage lists by width; row length n2
-    DevBuf p_rec, d_ssrc, d_sweep_err;
+    DevBuf p_rec, d_sweep_err;
     // level-order work: inflow masks, order, positions, level starts, in-degrees, counts
     DevBuf lo_mask, lo_perm, lo_pos, lo_lvl, lo_indeg, lo_small, lo_down;
     int plan_host_dirs = 0;  // directions the last plan ordered on the host
@@ -1243,19 +1242,18 @@ static bte_status build_sweep_plan(bte_ctx* ctx) {
         BTE_CUDA(ctx->p_rec.alloc((size_t)rb * ND * n));
         const dim3 g((n + 255) / 256, ND);
         if (fmx == 2)
-            bte::k_sweep_records<2><<<g, 256, 0, st>>>(ctx->p_cell.as<int>(), ctx->p_nb.as<int>(),
+            bte::k_sweep_records<2><<<g, 256, 0, st>>>(ctx->p_cell.as<int>(), ctx->p_bidx.as<int>(), ctx->p_nb.as<int>(),
                                                        ctx->p_fc.as<double>(), n, F, ND,
                                                        ctx->p_rec.as<unsigned char>());
         else if (fmx == 3)
-            bte::k_sweep_records<3><<<g, 256, 0, st>>>(ctx->p_cell.as<int>(), ctx->p_nb.as<int>(),
+            bte::k_sweep_records<3><<<g, 256, 0, st>>>(ctx->p_cell.as<int>(), ctx->p_bidx.as<int>(), ctx->p_nb.as<int>(),
                                                        ctx->p_fc.as<double>(), n, F, ND,
                                                        ctx->p_rec.as<unsigned char>());
         else
-            bte::k_sweep_records<4><<<g, 256, 0, st>>>(ctx->p_cell.as<int>(), ctx->p_nb.as<int>(),
+            bte::k_sweep_records<4><<<g, 256, 0, st>>>(ctx->p_cell.as<int>(), ctx->p_bidx.as<int>(), ctx->p_nb.as<int>(),
                                                        ctx->p_fc.as<double>(), n, F, ND,
                                                        ctx->p_rec.as<unsigned char>());
         BTE_LAUNCHED();
-        BTE_CUDA(ctx->d_ssrc.alloc(sizeof(double) * (size_t)ctx->nbb * ND * ctx->n2));
         BTE_CUDA(ctx->d_sweep_err.alloc(sizeof(int)));
         BTE_CUDA(cudaMemsetAsync(ctx->d_sweep_err.p, 0, sizeof(int), st));
         int smem_max = 0;
@@ -1645,9 +1643,9 @@ static void launch_sweep(const bte_ctx* ctx, const SweepShape& sh, int nbb, int 
         const bte::StagedPlan pl{ctx->p_rec.as<unsigned char>(), sl->stages.as<int>(), sl->off.as<int>(),
                                  ctx->p_cell.as<int>(), ctx->n, ctx->n2, sh.cap};
 #define BTE_STAGED_FM(FM)                                                                                          \
-    bte::k_sweep_staged<FM><<<grid, sh.threads, sh.smem, st>>>(pl, kinv, ctx->d_ssrc.as<double>(), src.x_old,      \
-                                                               ctx->e_curr, first_sweep, sh.G, sh.W, nbb, b0,      \
-                                                               ctx->n_dir, ctx->Np, ctx->d_sweep_err.as<int>())
+    bte::k_sweep_staged<FM><<<grid, sh.threads, sh.smem, st>>>(pl, kinv, voi, src, src.x_old, ctx->e_curr,          \
+                                                               first_sweep, sh.G, sh.W, nbb, b0, ctx->n_dir,        \
+                                                               ctx->Np, ctx->d_sweep_err.as<int>())
         if (fm == 2) BTE_STAGED_FM(2);
         else if (fm == 3) BTE_STAGED_FM(3);
         else BTE_STAGED_FM(4);
@@ -1667,13 +1665,6 @@ static void launch_sweep(const bte_ctx* ctx, const SweepShape& sh, int nbb, int 
     else if (fm == 3) BTE_SWEEP_FM(3);
     else BTE_SWEEP_FM(4);
 #undef BTE_SWEEP_FM
-}
-
-// The staged sweep's right-hand side of the batch in level order (k_sweep_src).
-static void launch_sweep_src(const bte_ctx* ctx, int nbb, int b0, cudaStream_t st, const bte::SweepSrc& src) {
-    const dim3 g((ctx->n + 255) / 256, nbb * ctx->n_dir);
-    bte::k_sweep_src<<<g, 256, 0, st>>>(ctx->p_cell.as<int>(), ctx->p_bidx.as<int>(), ctx->p_voi.as<double>(), src,
-                                        ctx->n, ctx->n2, ctx->n_dir, nbb, b0, ctx->Np, ctx->d_ssrc.as<double>());
 }
 
 // Solve all systems of one batch by upwind sweeps (exact in one sweep when no
@@ -1737,7 +1728,6 @@ static bte_status solve_batch_sweep(bte_ctx* ctx, int b0, int nbb, const bte_opt
                 if (s2 != BTE_OK) return s2;
             }
             BTE_CUDA(cudaEventRecord(e0, st));
-            if (cand[k].prepass()) launch_sweep_src(ctx, nbb, b0, st, ssrc);  // its right-hand side counts too
             launch_sweep<false>(ctx, cand[k], nbb, b0, st, sp, ssrc, 1, nullptr);
             BTE_LAUNCHED();
             BTE_CUDA(cudaEventRecord(e1, st));
@@ -1755,7 +1745,7 @@ static bte_status solve_batch_sweep(bte_ctx* ctx, int b0, int nbb, const bte_opt
         // margin only when that saves 3 % of the sweeps and reduction, so a
         // near tie (2D meshes) does not flip between runs.
         bool fuse = false;
-        if (ctx->plan_lagged_dirs == 0 && !ctx->sweep_shape.prepass()) {
+        if (ctx->plan_lagged_dirs == 0 && !ctx->sweep_shape.staged) {  // (the staged kernel leaves it to k_reduce)
             if (only_margin >= 0) fuse = only_margin == 1;
             else {
                 auto time_best = [&](auto&& launch) -> float {
@@ -1806,15 +1796,13 @@ static bte_status solve_batch_sweep(bte_ctx* ctx, int b0, int nbb, const bte_opt
         bte_status s2 = stage_list(ctx, shape.cap, &sl);
         if (s2 != BTE_OK) return s2;
     }
-    ctx->sweep_margin = shape.margin && !shape.prepass() && ctx->plan_lagged_dirs == 0;
+    ctx->sweep_margin = shape.margin && !shape.staged && ctx->plan_lagged_dirs == 0;
     // algorithmic HBM bytes of a sweep per system and cell: V Omega / D and
     // k / D read, x written (and, with the fused margin, the previous iterate
     // read), plus the level-ordered geometry per direction; ebar and the
     // boundary values come from L2
     const bool margin = ctx->sweep_margin;
     const double sweep_bytes = S * N * (margin ? 4 : 3) * w + geo;
-    if (shape.prepass())  // the staged sweep's right-hand side: V Omega / D read, src written (ebar from L2)
-        BTE_LAUNCH(KK_RHS, -1, S * N * 2 * w, 0, launch_sweep_src(ctx, nbb, b0, st, ssrc));
     int sweeps = 0;
     for (;;) {
         if (margin) {

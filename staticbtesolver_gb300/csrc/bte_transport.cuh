@@ -530,36 +530,38 @@ __global__ void __launch_bounds__(128, 5) k_sweep(SweepPlan sp, const double* __
 
 // ---------------------------------------------------------------------------
 // Staged sweep: the substitution of k_sweep with every operand of a level
-// already in shared memory when the level starts.
+// already in shared memory or in registers when the level starts.
 //
 // k_sweep's items wait on two dependent loads each level (the cell index, then
 // the cell's ebar and boundary value): load latency along the level chain,
-// not HBM or the FP64 pipe, sets its time.  Here the right-hand side is formed
-// beforehand in level order by k_sweep_src (src = ebar voi + bs/D per system
-// and position, the same fma as k_sweep's), so everything a level reads is a
-// contiguous slice of a position-indexed array: the level's plan records
-// (cell, upstream positions, face coefficients), and per band k/D and src.
-// One thread copies those slices for stage s + 3 into one of three
-// shared-memory buffers with 1-D bulk copies (cp.async.bulk, completion on an
-// mbarrier) while the block solves stage s.  A stage is a level, or a slice of
-// at most `cap` positions of a wider one (positions of one level never depend
-// on each other, so splitting a level keeps the substitution exact).  The
-// arithmetic is k_sweep's term for term, so x is the same to the bit.
+// not HBM or the FP64 pipe, sets its time.  Here everything a stage reads by
+// position is a contiguous slice of a position-indexed array: the plan
+// records (cell, boundary row, upstream positions, face coefficients) and per
+// band k/D and V Omega/D.  One thread copies those slices for stage s + 3 into
+// one of three shared-memory buffers with 1-D bulk copies (cp.async.bulk,
+// completion on an mbarrier) while the block solves stage s.  The gathers by
+// cell (ebar, the boundary value) of stage s + 1's items are issued while
+// stage s is solved, from the cells in its records, and their right-hand
+// sides src = ebar voi + bs/D (the fma k_sweep forms) are kept in registers.
+// A stage is a level, or a slice of at most `cap` positions of a wider one
+// (positions of one level never depend on each other, so splitting a level
+// keeps the substitution exact).  The arithmetic is k_sweep's term for term,
+// so x is the same to the bit.
 
-// Record of one position in a direction's level order: ints (cell, upstream
-// positions of the FM face slots, padding to 16 bytes), then the FM face
-// coefficients (FP64, padding to 16 bytes).
+// Record of one position in a direction's level order: ints (cell, its
+// boundary row or -1, upstream positions of the FM face slots, padding to 16
+// bytes), then the FM face coefficients (FP64, padding to 16 bytes).
 template <int FM>
 struct SweepRecLayout {
-    static constexpr int ints = 4 * ((FM + 4) / 4);    // 1 + FM rounded up to 4
+    static constexpr int ints = 4 * ((FM + 5) / 4);    // 2 + FM rounded up to 4
     static constexpr int dbls = 2 * ((FM + 1) / 2);    // FM rounded up to 2
-    static constexpr int bytes = 4 * ints + 8 * dbls;  // 32 (FM 2), 48 (FM 3), 64 (FM 4)
+    static constexpr int bytes = 4 * ints + 8 * dbls;  // 32 (FM 2), 64 (FM 3, 4)
 };
 
 // rec[d][j] from the level-ordered plan arrays (k_sweep_layout's output).
 template <int FM>
-__global__ void k_sweep_records(const int* __restrict__ cell, const int* __restrict__ nb,
-                                const double* __restrict__ fc, int n, int F, int n_dir,
+__global__ void k_sweep_records(const int* __restrict__ cell, const int* __restrict__ bidx,
+                                const int* __restrict__ nb, const double* __restrict__ fc, int n, int F, int n_dir,
                                 unsigned char* __restrict__ rec) {
     using L = SweepRecLayout<FM>;
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
@@ -569,33 +571,14 @@ __global__ void k_sweep_records(const int* __restrict__ cell, const int* __restr
     int* ri = reinterpret_cast<int*>(r);
     double* rd = reinterpret_cast<double*>(r + 4 * L::ints);
     ri[0] = cell[(size_t)d * n + j];
+    ri[1] = bidx[(size_t)d * n + j];
     for (int f = 0; f < FM; ++f) {
         const bool in = f < F;
-        ri[1 + f] = in ? nb[((size_t)d * F + f) * n + j] : -1;
+        ri[2 + f] = in ? nb[((size_t)d * F + f) * n + j] : -1;
         rd[f] = in ? fc[((size_t)d * F + f) * n + j] : 0.0;
     }
-    for (int k = 1 + FM; k < L::ints; ++k) ri[k] = -1;
+    for (int k = 2 + FM; k < L::ints; ++k) ri[k] = -1;
     for (int k = FM; k < L::dbls; ++k) rd[k] = 0.0;
-}
-
-// src[bl][d][j] = ebar[b][cell] voi[b][d][j] + bs[d][bl][row]/D (row = the
-// cell's boundary row, 0 without one) for the batch's bands bl = b - b0: the
-// right-hand side k_sweep forms inside its level loop, in the same fma.
-// Rows of voi and src are n2 (n rounded up to even) long.
-__global__ void k_sweep_src(const int* __restrict__ cell, const int* __restrict__ bidx,
-                            const double* __restrict__ voi, SweepSrc src, int n, int n2, int n_dir, int nbb, int b0,
-                            size_t Np, double* __restrict__ out) {
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    const int s = blockIdx.y;  // bl * n_dir + d
-    if (j >= n) return;
-    const int bl = s / n_dir, d = s - bl * n_dir;
-    const int b = b0 + bl;
-    const size_t pj = (size_t)d * n + j;
-    const int c = cell[pj];
-    const int bi = bidx[pj];
-    const double bs = bi >= 0 ? src.bsum[((size_t)d * nbb + bl) * src.nbcell + bi] : 0.0;
-    const double eb = src.ebar[(size_t)b * Np + c];
-    out[(size_t)s * n2 + j] = fma(eb, voi[((size_t)b * n_dir + d) * n2 + j], bs);
 }
 
 // Shared-memory barrier and bulk-copy primitives (PTX ISA: mbarrier,
@@ -654,7 +637,7 @@ struct StagedPlan {
 };
 
 // Bytes of one stage buffer: cap records, then per band of the block k/D and
-// src slices of cap + 2 doubles (a slice starts at an even position).
+// V Omega/D slices of cap + 2 doubles (a slice starts at an even position).
 template <int FM>
 __host__ __device__ constexpr size_t staged_buffer_bytes(int cap, int G) {
     return (size_t)cap * SweepRecLayout<FM>::bytes + sizeof(double) * 2 * (size_t)G * (cap + 2);
@@ -669,16 +652,17 @@ __host__ __device__ constexpr size_t staged_smem_bytes(int cap, int G, int W) {
 
 // One block sweeps direction blockIdx.y for the batch's bands blockIdx.x * G
 // .. + G - 1 (thread t serves band t mod gp, positions t / gp, t / gp +
-// blockDim / gp, ... of each stage, as in k_sweep).  x = e_curr, x_old =
-// e_prev ([band][n_dir][Np]); kinv [band][n_dir][n2] (all bands), srcv
-// [batch band][n_dir][n2] (k_sweep_src).  The ring keeps the last W solved
-// positions per band: a position p is still there during the stage [j0, j1)
-// whenever p >= j1 - W.  A stage's copies that have not landed after
-// kStagePolls polls set *err; the block then waits (bounded) for its copies
-// in flight and returns (x is then not valid; the host reports the error).
+// blockDim / gp, ... of each stage, as in k_sweep; cap = 2 blockDim / gp, so a
+// thread has at most two items per stage).  x = e_curr, x_old = e_prev
+// ([band][n_dir][Np]); kinv and voi [band][n_dir][n2] (all bands); src: ebar
+// and the boundary parts.  The ring keeps the last W solved positions per
+// band: a position p is still there during the stage [j0, j1) whenever
+// p >= j1 - W.  A stage's copies that have not landed after kStagePolls polls
+// set *err; the block then waits (bounded) for its copies in flight and
+// returns (x is then not valid; the host reports the error).
 template <int FM>
 __global__ void __launch_bounds__(256) k_sweep_staged(StagedPlan sp, const double* __restrict__ kinv,
-                                                      const double* __restrict__ srcv,
+                                                      const double* __restrict__ voi, SweepSrc src,
                                                       const double* __restrict__ x_old, double* x, int first_sweep,
                                                       int G, int W, int nbb, int b0, int n_dir, size_t Np, int* err) {
     using L = SweepRecLayout<FM>;
@@ -704,6 +688,8 @@ __global__ void __launch_bounds__(256) k_sweep_staged(StagedPlan sp, const doubl
     const int n = sp.n, n2 = sp.n2;
     double* xb = x + ((size_t)(b0 + bb) * n_dir + d) * Np;
     const double* xo = x_old + ((size_t)(b0 + bb) * n_dir + d) * Np;
+    const double* eb = src.ebar + (size_t)(b0 + bb) * Np;
+    const double* bsb = src.bsum + ((size_t)d * nbb + bb) * src.nbcell;
     double* rg = ring + (size_t)bl * W;
     const int* cell_d = sp.cell + (size_t)d * n;
     const unsigned char* rec_d = sp.rec + (size_t)d * n * L::bytes;
@@ -725,10 +711,43 @@ __global__ void __launch_bounds__(256) k_sweep_staged(StagedPlan sp, const doubl
         bulk_load(B, rec_d + (size_t)j0 * L::bytes, rb, &bar[q]);
         double* kv = reinterpret_cast<double*>(B + rec_bytes);
         for (int g = 0; g < gn; ++g) {
-            const size_t sys_all = (size_t)(b0 + g0 + g) * n_dir + d;
-            const size_t sys_batch = (size_t)(g0 + g) * n_dir + d;
-            bulk_load(kv + (size_t)g * vlen, kinv + sys_all * n2 + ja, vb, &bar[q]);
-            bulk_load(kv + (size_t)(G + g) * vlen, srcv + sys_batch * n2 + ja, vb, &bar[q]);
+            const size_t sys = (size_t)(b0 + g0 + g) * n_dir + d;
+            bulk_load(kv + (size_t)g * vlen, kinv + sys * n2 + ja, vb, &bar[q]);
+            bulk_load(kv + (size_t)(G + g) * vlen, voi + sys * n2 + ja, vb, &bar[q]);
+        }
+    };
+    // a stage's buffer, once its copies have landed (bounded polls)
+    auto wait_stage = [&](int s) -> bool {
+        long long k = 0;
+        while (!mbar_try_wait(&bar[s % 3], (unsigned)(s / 3) & 1u))
+            if (++k > kStagePolls) return false;
+        return true;
+    };
+    // the cell-indexed loads of this thread's (at most two) items of stage s
+    // (issued a stage ahead), then their right-hand sides
+    double geb[2] = {0.0, 0.0}, gbs[2] = {0.0, 0.0}, rhs[2] = {0.0, 0.0};
+    auto gather = [&](int s) {
+        const int q = s % 3;
+        const unsigned char* B = bufs + (size_t)q * buf_bytes;
+        const int j0 = hdr[2 * q], j1 = hdr[2 * q + 1];
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            const int j = j0 + tpos + k * per_round;
+            if (j >= j1) continue;
+            const int2 cb = *reinterpret_cast<const int2*>(B + (size_t)(j - j0) * L::bytes);
+            geb[k] = eb[cb.x];
+            gbs[k] = cb.y >= 0 ? bsb[cb.y] : 0.0;
+        }
+    };
+    auto form_rhs = [&](int s) {
+        const int q = s % 3;
+        const unsigned char* B = bufs + (size_t)q * buf_bytes;
+        const int j0 = hdr[2 * q], j1 = hdr[2 * q + 1], ja = j0 & ~1;
+        const double* vv = reinterpret_cast<const double*>(B + rec_bytes) + (size_t)(G + bl) * vlen;
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            const int j = j0 + tpos + k * per_round;
+            if (j < j1) rhs[k] = fma(geb[k], vv[j - ja], gbs[k]);
         }
     };
     if (threadIdx.x == 0) {
@@ -749,27 +768,33 @@ __global__ void __launch_bounds__(256) k_sweep_staged(StagedPlan sp, const doubl
     }
     __syncthreads();  // the headers of the first stages
     bool failed = false;
+    if (ns > 0) {
+        failed = !wait_stage(0);
+        if (!failed && serves) {
+            gather(0);
+            form_rhs(0);
+        }
+    }
+    failed = __syncthreads_or(failed);
     int s = 0;
-    for (; s < ns; ++s) {
+    for (; s < ns && !failed; ++s) {
         const int q = s % 3;
-        const unsigned par = (unsigned)(s / 3) & 1u;
         // thread 0: the end of stage s + 3, loaded now and used after this stage
         const int next_end = threadIdx.x == 0 ? stg[min(s + 4, ns)] : 0;
-        long long k = 0;
-        while (!mbar_try_wait(&bar[q], par)) {
-            if (++k > kStagePolls) {
-                failed = true;
-                break;
-            }
-        }
+        // stage s + 1: its buffer, and the gathers of its items
+        const bool ahead = s + 1 < ns;
+        if (ahead && !wait_stage(s + 1)) failed = true;
+        if (ahead && !failed && serves) gather(s + 1);
         if (!failed && serves) {
             const unsigned char* B = bufs + (size_t)q * buf_bytes;
             const double* kv = reinterpret_cast<const double*>(B + rec_bytes) + (size_t)bl * vlen;
-            const double* sv = reinterpret_cast<const double*>(B + rec_bytes) + (size_t)(G + bl) * vlen;
             const int j0 = hdr[2 * q], j1 = hdr[2 * q + 1];
             const int ja = j0 & ~1;
             const int keep = j1 - W;  // oldest position still readable from the ring
-            for (int j = j0 + tpos; j < j1; j += per_round) {
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
+                const int j = j0 + tpos + k * per_round;
+                if (j >= j1) continue;
                 const unsigned char* r = B + (size_t)(j - j0) * L::bytes;
                 int iv[L::ints];
                 double dv[L::dbls];
@@ -790,7 +815,7 @@ __global__ void __launch_bounds__(256) k_sweep_staged(StagedPlan sp, const doubl
                 double off = 0.0;
 #pragma unroll
                 for (int f = 0; f < FM; ++f) {
-                    const int u = iv[1 + f];
+                    const int u = iv[2 + f];
                     if (u == -1) continue;
                     double xu;
                     if (u >= 0) xu = u >= keep ? rg[u & (W - 1)] : xb[cell_d[u]];
@@ -800,11 +825,12 @@ __global__ void __launch_bounds__(256) k_sweep_staged(StagedPlan sp, const doubl
                     }
                     off = fma(dv[f], xu, off);
                 }
-                const double v = fma(-kv[j - ja], off, sv[j - ja]);
+                const double v = fma(-kv[j - ja], off, rhs[k]);
                 xb[iv[0]] = v;
                 rg[j & (W - 1)] = v;
             }
         }
+        if (ahead && !failed && serves) form_rhs(s + 1);
         if (__syncthreads_or(failed)) {
             failed = true;
             break;

@@ -742,24 +742,49 @@ struct DsaHostPlan {
 // pre_order (optional): a locality order already computed, used as it is
 // without pre_cm, and with pre_cm (the coupling pattern it was computed for,
 // [n][F]) only when the pattern of W is the same.
+// Runs body(i0, i1) over [0, n) split into contiguous ranges on host
+// threads (one range below 65,536 items); each i is written by one range.
+template <typename Body>
+static void host_ranges(int n, Body&& body) {
+    const int T = n < 65536 ? 1 : std::max(1, std::min(8, (int)std::thread::hardware_concurrency()));
+    if (T == 1) {
+        body(0, n);
+        return;
+    }
+    std::vector<std::thread> pool;
+    for (int t = 0; t < T; ++t)
+        pool.emplace_back(body, (int)((long long)n * t / T), (int)((long long)n * (t + 1) / T));
+    for (auto& th : pool) th.join();
+}
+
 static void dsa_host_plan(int n, int F, const int* nb, const double* W, int nblk, DsaHostPlan& hp,
                           std::vector<int>* pre_order = nullptr, const std::vector<int>* pre_cm = nullptr) {
     HostTimer tm("dsa_host_plan");
     hp.n = n;
     hp.F = F;
     hp.nblk = nblk;
-    std::vector<double> diag(n, 0.0), dsc(n, 0.0);
-    for (int f = 0; f < F; ++f)
-        for (int c = 0; c < n; ++c) diag[c] += W[(size_t)f * n + c];
-    for (int c = 0; c < n; ++c) dsc[c] = diag[c] > 0.0 ? 1.0 / std::sqrt(diag[c]) : 0.0;
-    // locality order: contiguous position ranges are compact groups of cells
-    std::vector<int> cm((size_t)n * F);
-    for (int f = 0; f < F; ++f)
-        for (int c = 0; c < n; ++c) cm[(size_t)c * F + f] = W[(size_t)f * n + c] > 0.0 ? nb[(size_t)f * n + c] : -1;
-    const int agg_cells = std::max(1, n / (nblk * bte::dsa::AGG));
+    std::vector<double> dsc(n, 0.0);
+    host_ranges(n, [&](int c0, int c1) {
+        for (int c = c0; c < c1; ++c) {
+            double diag = 0.0;
+            for (int f = 0; f < F; ++f) diag += W[(size_t)f * n + c];
+            dsc[c] = diag > 0.0 ? 1.0 / std::sqrt(diag) : 0.0;
+        }
+    });
     tm.lap("scaling");
-    if (pre_order && pre_order->size() == (size_t)n && (!pre_cm || *pre_cm == cm)) hp.order.swap(*pre_order);
-    else bte::locality_order(n, F, cm.data(), std::max(8, agg_cells / 2), hp.order);
+    // locality order: contiguous position ranges are compact groups of cells
+    const bool given = pre_order && pre_order->size() == (size_t)n;
+    if (given && !pre_cm) {
+        hp.order.swap(*pre_order);
+    } else {
+        std::vector<int> cm((size_t)n * F);
+        for (int f = 0; f < F; ++f)
+            for (int c = 0; c < n; ++c)
+                cm[(size_t)c * F + f] = W[(size_t)f * n + c] > 0.0 ? nb[(size_t)f * n + c] : -1;
+        const int agg_cells = std::max(1, n / (nblk * bte::dsa::AGG));
+        if (given && *pre_cm == cm) hp.order.swap(*pre_order);
+        else bte::locality_order(n, F, cm.data(), std::max(8, agg_cells / 2), hp.order);
+    }
     tm.lap("locality order");
     const std::vector<int>& order = hp.order;
     std::vector<int>& pos = hp.pos;
@@ -769,20 +794,22 @@ static void dsa_host_plan(int n, int F, const int* nb, const double* W, int nblk
     hp.dscp.assign(n, 0.0);
     hp.w.assign((size_t)F * n, 0.0f);
     hp.nbv.assign((size_t)F * n, -1);
-    for (int k = 0; k < n; ++k) {
-        const int c = order[k];
-        hp.dscp[k] = dsc[c];
-        for (int f = 0; f < F; ++f) {
-            const size_t q = (size_t)f * n + c;
-            const int o = nb[q];
-            if (o >= 0 && W[q] > 0.0) {
-                const size_t qk = (size_t)f * n + k;
-                wd[qk] = W[q] * dsc[c] * dsc[o];
-                hp.w[qk] = (float)wd[qk];
-                hp.nbv[qk] = pos[o];
+    host_ranges(n, [&](int k0, int k1) {
+        for (int k = k0; k < k1; ++k) {
+            const int c = order[k];
+            hp.dscp[k] = dsc[c];
+            for (int f = 0; f < F; ++f) {
+                const size_t q = (size_t)f * n + c;
+                const int o = nb[q];
+                if (o >= 0 && W[q] > 0.0) {
+                    const size_t qk = (size_t)f * n + k;
+                    wd[qk] = W[q] * dsc[c] * dsc[o];
+                    hp.w[qk] = (float)wd[qk];
+                    hp.nbv[qk] = pos[o];
+                }
             }
         }
-    }
+    });
     tm.lap("permuted operator");
     bte::dsa_coarse(n, F, hp.nbv.data(), wd.data(), nblk, bte::dsa::AGG, hp.co);
     hp.agg = hp.co.agg;

@@ -354,39 +354,51 @@ inline void dsa_coarse(int n, int F, const int* nb /* [F][n] */, const double* w
             const int hi = std::min(std::min(n, (k + 1) * out.chunk), lo + out.seg);
             for (int c = lo; c < hi; ++c) agg[c] = k * per_block + a;
         }
+    // Block k's cells add only to the rows of block k's aggregates, in cell
+    // order, so the blocks' rows (and their need lists) are formed on host
+    // threads independently; the result does not depend on the thread count.
     std::vector<double>& Ac = out.ac;
-    Ac.assign((size_t)m * m, 0.0);
-    std::vector<int> size(m, 0);
-    for (int c = 0; c < n; ++c) {
-        const int J = agg[c];
-        ++size[J];
-        Ac[(size_t)J * m + J] += 1.0;
-        for (int f = 0; f < F; ++f) {
-            const int o = nb[(size_t)f * n + c];
-            if (o < 0) continue;
-            Ac[(size_t)J * m + agg[o]] -= w[(size_t)f * n + c];
-        }
-    }
-    for (int J = 0; J < m; ++J)
-        if (size[J] == 0) Ac[(size_t)J * m + J] = 1.0;
-    out.need_ptr.assign(nblk + 1, 0);
-    out.need.clear();
-    std::vector<int> seen(m, -1);
-    for (int k = 0; k < nblk; ++k) {
-        const int lo = k * out.chunk, hi = std::min(n, lo + out.chunk);
-        std::vector<int> list;
+    Ac.resize((size_t)m * m);
+    std::vector<std::vector<int>> lists(nblk);
+    auto rows_of = [&](int k) {
+        std::fill(Ac.begin() + (size_t)k * per_block * m, Ac.begin() + (size_t)(k + 1) * per_block * m, 0.0);
+        const int lo = std::min(n, k * out.chunk), hi = std::min(n, lo + out.chunk);
+        std::vector<int> size(per_block, 0);
+        std::vector<char> seen(m, 0);
+        std::vector<int>& list = lists[k];
+        list.clear();
         for (int c = lo; c < hi; ++c) {
             const int J = agg[c];
-            if (seen[J] != k) { seen[J] = k; list.push_back(J); }
+            ++size[J - k * per_block];
+            Ac[(size_t)J * m + J] += 1.0;
+            if (!seen[J]) { seen[J] = 1; list.push_back(J); }
             for (int f = 0; f < F; ++f) {
                 const int o = nb[(size_t)f * n + c];
                 if (o < 0) continue;
                 const int K = agg[o];
-                if (seen[K] != k) { seen[K] = k; list.push_back(K); }
+                Ac[(size_t)J * m + K] -= w[(size_t)f * n + c];
+                if (!seen[K]) { seen[K] = 1; list.push_back(K); }
             }
         }
+        for (int a = 0; a < per_block; ++a)
+            if (size[a] == 0) Ac[(size_t)(k * per_block + a) * m + k * per_block + a] = 1.0;
         std::sort(list.begin(), list.end());
-        out.need.insert(out.need.end(), list.begin(), list.end());
+    };
+    const int T = std::max(1, std::min({(int)std::thread::hardware_concurrency(), 8, nblk}));
+    if (T == 1 || (size_t)n * F < 65536) {
+        for (int k = 0; k < nblk; ++k) rows_of(k);
+    } else {
+        std::vector<std::thread> pool;
+        for (int t = 0; t < T; ++t)
+            pool.emplace_back([&, t] {
+                for (int k = t; k < nblk; k += T) rows_of(k);
+            });
+        for (auto& th : pool) th.join();
+    }
+    out.need_ptr.assign(nblk + 1, 0);
+    out.need.clear();
+    for (int k = 0; k < nblk; ++k) {
+        out.need.insert(out.need.end(), lists[k].begin(), lists[k].end());
         out.need_ptr[k + 1] = (int)out.need.size();
     }
 }

@@ -289,3 +289,41 @@ def test_hilbert_order_matches_restatement(lib, dim):
     q = np.minimum(np.maximum((cen[:, :dim] - lo) * (steps / ext), 0.0), steps - 1).astype(np.uint64)
     want = np.argsort(_hilbert_keys(q, b), kind="stable")
     np.testing.assert_array_equal(out, want)
+
+
+def test_coarse_operator_on_host_threads(lib):
+    """dsa_coarse on a 30,000-cell operator (above the size it forms on host
+    threads): the coarse matrix P^T A P and every block's need list equal a
+    serial NumPy restatement."""
+    rng = np.random.default_rng(5)
+    n, F, nblk, per = 30000, 3, 16, 4
+    nb = np.full((F, n), -1, np.int32)
+    w = np.zeros((F, n))
+    for f, off in enumerate((1, 97, 5003)):
+        has = rng.random(n) < 0.9
+        nb[f, has] = (np.arange(n)[has] + off) % n
+        w[f, has] = rng.uniform(0.1, 1.0, has.sum())
+    m = nblk * per
+    ac = np.zeros(m * m)
+    geo = np.zeros(2, np.int32)
+    need_ptr = np.zeros(nblk + 1, np.int32)
+    need = np.zeros(m * nblk, np.int32)
+    ptr = lambda a: np.ascontiguousarray(a).ctypes.data_as(C.c_void_p)
+    got = lib.coarse_c(n, F, ptr(nb), ptr(w), nblk, per, ac.ctypes.data_as(C.c_void_p), geo.ctypes.data_as(C.c_void_p),
+                       need_ptr.ctypes.data_as(C.c_void_p), need.ctypes.data_as(C.c_void_p))
+    assert got == m
+    chunk, seg = int(geo[0]), int(geo[1])
+    k = np.arange(n) // chunk
+    agg = k * per + (np.arange(n) - k * chunk) // seg
+    want = np.zeros((m, m))
+    for c in range(n):
+        J = agg[c]
+        want[J, J] += 1.0
+        for f in range(F):
+            if nb[f, c] >= 0:
+                want[J, agg[nb[f, c]]] -= w[f, c]
+    np.testing.assert_array_equal(ac.reshape(m, m), want)
+    for b in range(nblk):
+        cells = np.arange(b * chunk, min(n, (b + 1) * chunk))
+        lst = sorted(set(agg[cells].tolist()) | set(agg[nb[:, cells][nb[:, cells] >= 0]].tolist()))
+        assert need[need_ptr[b]:need_ptr[b + 1]].tolist() == lst

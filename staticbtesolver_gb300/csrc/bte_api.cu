@@ -564,9 +564,7 @@ static bte_status setup(bte_ctx* ctx, int batch_systems) {
                 mir[t * ND + d] = d;
             }
     std::vector<double> kb(NB);
-    double Lr_sum = 0;
     for (int b = 0; b < NB; ++b) kb[b] = ctx->vg[b] * ctx->tau[b];
-    (void)Lr_sum;
     if (dlist.empty()) { dlist.push_back(0); wdiff.assign(ND, 0.0); wden.push_back(1.0); }
     if (bf_cell.empty()) { bf_cell.push_back(0); bf_kind.push_back(1); bf_bc.push_back(0); bf_diff.push_back(-1); }
 
@@ -2727,6 +2725,7 @@ constexpr size_t kNoAllocDoubles = 10 * kNoAllocNp + 7 * (size_t)kNoAllocChunks 
 constexpr size_t kNoAllocInts = 8 + (size_t)kNoAllocMaxIt + 2;
 constexpr size_t kNoAllocScratch = kNoAllocDoubles + (kNoAllocInts + 1) / 2;
 constexpr size_t kNoAllocScratchBytes = kNoAllocScratch * sizeof(double);
+static_assert(kNoAllocScratchBytes < (size_t)24 << 20, "the static scratch is documented as about 21 MB");
 }  // namespace
 
 static __device__ __align__(256) double g_noalloc_scratch[kNoAllocScratch];
